@@ -1,0 +1,173 @@
+/*
+ * dm_gb300.h -- C ABI of the GB300 Pauli-basis density-matrix engine.
+ *
+ * The state of an n-qubit register is the real vector a[4**n] of Pauli
+ * coefficients, rho = sum_s a_s sigma_{s_0} x ... x sigma_{s_{n-1}}, with
+ * flat index s = sum_q p_q * 4**(n-1-q), p in {0:I, 1:X, 2:Y, 3:Z}
+ * (qubit 0 is the slowest axis), exactly the layout of the reference's
+ * ``DmSimulatorPy._densitymatrix`` (qiskit/providers/basicaer/dm_simulator.py
+ * :62-67, :376).  It lives in GPU memory as FP64 (DM_F64) or FP32 (DM_F32).
+ *
+ * Conventions
+ *   - Every entry point returns 0 on success or a negative DM_ERR_* code; no
+ *     C++ exception crosses this boundary.  dm_error_string() names a code.
+ *   - Pointers named *_dev are device pointers; everything else is host.
+ *   - ``stream`` is a cudaStream_t passed as void* (NULL = legacy stream).
+ *     Work is enqueued asynchronously; host outputs are written before return.
+ *   - Small matrices (4x4, 16x16, row-major, output row x input column) are
+ *     passed by host pointer and copied into the kernel's parameters.
+ *   - No entry point allocates device memory; callers pass scratch buffers
+ *     sized by the matching *_scratch_bytes() query.
+ *
+ * Each entry point names the reference function it replaces.
+ */
+#ifndef DM_GB300_H
+#define DM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum dm_dtype { DM_F64 = 0, DM_F32 = 1 };
+
+enum dm_status {
+    DM_OK = 0,
+    DM_ERR_ARG = -1,      /* invalid argument (qubit index, size, dtype, pointer) */
+    DM_ERR_CUDA = -2,     /* a CUDA runtime call failed (launch, copy) */
+    DM_ERR_RANGE = -3,    /* size beyond a documented limit */
+    DM_ERR_PROGRAM = -4   /* malformed fused-pass program */
+};
+
+/* Limits of the fused-pass kernel. */
+#define DM_MAX_QUBITS 17            /* 4**17 FP64 = 137 GB: the largest state one GB300 holds */
+#define DM_MAX_TILE_AXES 7          /* resident axes of one tile (4**7 coefficients) */
+#define DM_MAX_PASS_OPS 128         /* operations applied to one tile in one pass */
+
+/* Operation kinds of a fused pass (local axes index the pass's resident axes). */
+enum dm_op_kind {
+    DM_OP_MAP1 = 1,    /* 4x4 real map on local axis a; mat = 16 entries */
+    DM_OP_MAP2 = 2,    /* 16x16 real map on local axes (a, b), index 4*p_a + p_b; mat = 256 entries */
+    DM_OP_DIAG2 = 3,   /* diagonal of a 16x16 map on (a, b); mat = 16 entries */
+    DM_OP_CX = 4       /* CX with control on local axis a, target on b; mat = 5 coefficients
+                          (c, s, c2, s2, cs) of basicaertools.py:329-336 */
+};
+
+/* flags of DM_OP_MAP1 */
+#define DM_MAP1_ROW0_IDENTITY 1   /* row 0 of the map is (1,0,0,0): the I component is unchanged */
+/* flags of DM_OP_CX */
+#define DM_CX_IDEAL 1             /* (c,s,c2,s2,cs) = (1,0,1,0,0): a signed permutation */
+
+typedef struct dm_op {
+    int32_t kind;
+    int16_t a, b;
+    int32_t flags;
+    int32_t moff;       /* offset of the op's coefficients in the pass's matrix buffer */
+} dm_op;
+
+typedef struct dm_pass {
+    int32_t k;                          /* number of resident axes, 1..DM_MAX_TILE_AXES */
+    int32_t axes[DM_MAX_TILE_AXES];     /* qubit of local axis r; strictly decreasing (local axis 0
+                                           has the smallest stride) */
+    int32_t nops;
+    dm_op ops[DM_MAX_PASS_OPS];
+} dm_pass;
+
+/* ---------------------------------------------------------------- state set-up */
+
+/* Product state a[s] = scale * prod_q v[q][s_q] (v: n x 4, host).
+ * Replaces DmSimulatorPy._initialize_densitymatrix, dm_simulator.py:284-349
+ * (all-zero, max_mixed, uniform_superpos, thermal_state and binary_string
+ * states are Kronecker products of per-qubit 4-vectors scaled by 2**-n). */
+int dm_init_product(void *state_dev, int n, int dtype, const double *v, double scale, void *stream);
+
+/* Copy a host FP64 coefficient vector (4**n) into the state (converting to dtype).
+ * Replaces the stored_density_matrix path, dm_simulator.py:337-343. */
+int dm_load_state(void *state_dev, int n, int dtype, const double *host_coeffs, void *stream);
+
+/* ------------------------------------------------------------ gates and noise */
+
+/* One 4x4 map on the Pauli axis of qubit q.
+ * Replaces rot_gate_dm_matrix (basicaertools.py:93-126) as used by
+ * DmSimulatorPy._add_unitary_single (dm_simulator.py:367-384), the per-qubit
+ * measurement updates (dm_simulator.py:574-704) and reset (:810-823). */
+int dm_apply_map1(void *state_dev, int n, int dtype, int q, const double *m4x4, void *stream);
+
+/* CX with control qc and target qt under the transition-selective-pulse error
+ * model err = (<cos a>, mean a).  Replaces cx_gate_dm_matrix,
+ * basicaertools.py:310-392 (via DmSimulatorPy._add_unitary_two, dm_simulator.py:386-395). */
+int dm_apply_cx(void *state_dev, int n, int dtype, int qc, int qt, const double *tsp_err2, void *stream);
+
+/* Memory noise on every qubit: X,Y *= sqrt(g)*f ; Z <- g*Z + (1-g)(2p-1)*I.
+ * Replaces DmSimulatorPy._add_decoherence_and_amp_decay, dm_simulator.py:397-425. */
+int dm_apply_memory_noise(void *state_dev, int n, int dtype, double f, double p, double g, void *stream);
+
+/* A fused pass: every tile of 4**k coefficients spanned by the pass's
+ * resident axes is loaded once, all of the pass's operations are applied to
+ * it on chip, and it is written back once.  mats_dev holds mats_count
+ * coefficients (in the state's dtype) that the ops index by moff.  This is the GB300 form of a run of
+ * consecutive levels of DmSimulatorPy.run_experiment (dm_simulator.py:1005-1177). */
+int dm_apply_pass(void *state_dev, int n, int dtype, const dm_pass *pass, const void *mats_dev,
+                  size_t mats_count, void *stream);
+
+/* ---------------------------------------------------------------- measurement */
+
+/* Probabilities of a measurement along one Pauli axis per qubit.
+ * mode[q] = 0: qubit q is not measured (marginalised);
+ *           1..3: measured along X, Y or Z with polarisation err.
+ * Outputs 2**m probabilities (m = number of measured qubits, the lowest
+ * measured qubit is the most significant bit) into out_dev (FP64, 2**m).
+ * With every qubit measured this replaces DmSimulatorPy._add_ensemble_measure
+ * (dm_simulator.py:427-481) for bases X/Y/Z; with some qubits unmeasured it
+ * gives the probabilities of _add_partial_measure (dm_simulator.py:492-538):
+ * only the 2**m coefficients on the measured sub-lattice are read, and a
+ * Walsh-Hadamard transform in out_dev turns them into probabilities. */
+int dm_axis_probs(const void *state_dev, int n, int dtype, const int *mode, double err,
+                  double *out_dev, void *stream);
+
+/* Probabilities of an ensemble measurement along the direction nvec (basis N,
+ * dm_simulator.py:456-462), every qubit measured: 2**n FP64 outputs.
+ * scratch_dev: dm_nbasis_probs_scratch_bytes(n) bytes. */
+size_t dm_nbasis_probs_scratch_bytes(int n);
+int dm_nbasis_probs(const void *state_dev, int n, int dtype, const double *nvec3, double err,
+                    double *out_dev, void *scratch_dev, void *stream);
+
+/* Gather count coefficients a[idx[i]] (FP64) into out_dev.  Used for the
+ * Pauli-string expectation (dm_simulator.py:569-570), the Bell reduced matrix
+ * and probabilities (:744-760) and the trace check (:363). count <= 64. */
+int dm_gather(const void *state_dev, int n, int dtype, const int64_t *idx, int count,
+              double *out_dev, void *stream);
+
+/* ------------------------------------------------------------------ outputs */
+
+/* out[s] = a[s], with |a[s]| < threshold set to 0 (FP64 output, 4**n).
+ * Replaces DmSimulatorPy._get_densitymatrix's chop, dm_simulator.py:1257-1269. */
+int dm_chop_copy(const void *state_dev, int n, int dtype, double threshold, double *out_dev, void *stream);
+
+/* Pauli basis -> 2**n x 2**n complex128 matrix (interleaved re/im, row-major).
+ * Replaces DmSimulatorPy._compute_densitymatrix, dm_simulator.py:1198-1255.
+ * scratch_dev: dm_pauli_to_matrix_scratch_bytes(n) bytes. */
+size_t dm_pauli_to_matrix_scratch_bytes(int n);
+int dm_pauli_to_matrix(const void *state_dev, int n, int dtype, double *out_dev, void *scratch_dev,
+                       void *stream);
+
+/* out_dev[0] = 2**n * sum_s a[s] b[s] (FP64).  Replaces DmSimulatorPy._state_overlap,
+ * dm_simulator.py:1277-1282.  scratch_dev: dm_overlap_scratch_bytes(n) bytes. */
+size_t dm_overlap_scratch_bytes(int n);
+int dm_overlap(const void *a_dev, const void *b_dev, int n, int dtype, double *out_dev,
+               void *scratch_dev, void *stream);
+
+/* ---------------------------------------------------------------------- misc */
+
+const char *dm_error_string(int code);
+/* Number of kernels this library has launched since load (all entry points). */
+uint64_t dm_kernel_launch_count(void);
+/* Library version, e.g. "dm_gb300 1.0 sm_103a". */
+const char *dm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DM_GB300_H */

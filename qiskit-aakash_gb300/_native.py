@@ -1,0 +1,151 @@
+"""Build and bind the C-ABI library ``libdmgb300.so`` (declared in include/dm_gb300.h).
+
+The library is compiled in-tree for sm_103a only (``build()``), with the
+translation units compiled in parallel and linked with ``nvcc -shared``.
+``lib()`` loads it with ctypes; the signatures below mirror the header.
+There is no fallback: if the library is missing or fails to load, every
+entry point of the package raises.
+"""
+import ctypes
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+REPO_DIR = os.path.dirname(PKG_DIR)
+CSRC = os.path.join(PKG_DIR, 'csrc')
+INCLUDE = os.path.join(REPO_DIR, 'include')
+BUILD_DIR = os.path.join(PKG_DIR, '_build')
+LIB_PATH = os.path.join(PKG_DIR, 'libdmgb300.so')
+SOURCES = ['dm_misc.cu', 'dm_pass.cu', 'dm_state.cu', 'dm_measure.cu']
+ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
+NVCC_FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '-Xptxas', '-warn-spills',
+              '--expt-relaxed-constexpr']
+
+DM_OK, DM_ERR_ARG, DM_ERR_CUDA, DM_ERR_RANGE, DM_ERR_PROGRAM = 0, -1, -2, -3, -4
+DM_F64, DM_F32 = 0, 1
+DM_MAX_QUBITS = 17
+DM_MAX_TILE_AXES = 7
+DM_MAX_PASS_OPS = 128
+DM_OP_MAP1, DM_OP_MAP2, DM_OP_DIAG2, DM_OP_CX = 1, 2, 3, 4
+DM_MAP1_ROW0_IDENTITY = 1
+DM_CX_IDEAL = 1
+
+
+class NativeError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, fn, code, msg):
+        super().__init__('%s failed: %s (%d)' % (fn, msg, code))
+        self.code = code
+
+
+def _nvcc():
+    for cand in (os.environ.get('NVCC'), '/usr/local/cuda/bin/nvcc', 'nvcc'):
+        if cand and (os.path.sep not in cand or os.path.exists(cand)):
+            return cand
+    return 'nvcc'
+
+
+def build(force=False, verbose=False):
+    """Compile csrc/*.cu for sm_103a and link libdmgb300.so in the package directory."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    srcs = [os.path.join(CSRC, s) for s in SOURCES]
+    deps = srcs + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith('.cuh')] \
+        + [os.path.join(INCLUDE, 'dm_gb300.h')]
+    newest = max(os.path.getmtime(d) for d in deps)
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
+        return LIB_PATH
+    nvcc = _nvcc()
+
+    def compile_one(src):
+        obj = os.path.join(BUILD_DIR, os.path.basename(src) + '.o')
+        cmd = [nvcc] + ARCH + NVCC_FLAGS + ['-I', INCLUDE, '-I', CSRC, '-c', src, '-o', obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError('nvcc failed for %s:\n%s\n%s' % (src, ' '.join(cmd), r.stderr))
+        if verbose and r.stderr:
+            sys.stderr.write(r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    tmp = LIB_PATH + '.tmp'
+    cmd = [nvcc] + ARCH + ['-shared', '-o', tmp] + objs + ['-lcudart_static', '-lrt', '-ldl', '-lpthread']
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError('nvcc link failed:\n%s\n%s' % (' '.join(cmd), r.stderr))
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+class DmOp(ctypes.Structure):
+    _fields_ = [('kind', ctypes.c_int32), ('a', ctypes.c_int16), ('b', ctypes.c_int16),
+                ('flags', ctypes.c_int32), ('moff', ctypes.c_int32)]
+
+
+class DmPass(ctypes.Structure):
+    _fields_ = [('k', ctypes.c_int32), ('axes', ctypes.c_int32 * DM_MAX_TILE_AXES),
+                ('nops', ctypes.c_int32), ('ops', DmOp * DM_MAX_PASS_OPS)]
+
+
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_d = ctypes.c_double
+_sz = ctypes.c_size_t
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+SIGNATURES = {
+    'dm_init_product': (_i, [_vp, _i, _i, _dp, _d, _vp]),
+    'dm_load_state': (_i, [_vp, _i, _i, _dp, _vp]),
+    'dm_apply_map1': (_i, [_vp, _i, _i, _i, _dp, _vp]),
+    'dm_apply_cx': (_i, [_vp, _i, _i, _i, _i, _dp, _vp]),
+    'dm_apply_memory_noise': (_i, [_vp, _i, _i, _d, _d, _d, _vp]),
+    'dm_apply_pass': (_i, [_vp, _i, _i, ctypes.POINTER(DmPass), _vp, _sz, _vp]),
+    'dm_axis_probs': (_i, [_vp, _i, _i, _ip, _d, _vp, _vp]),
+    'dm_nbasis_probs_scratch_bytes': (_sz, [_i]),
+    'dm_nbasis_probs': (_i, [_vp, _i, _i, _dp, _d, _vp, _vp, _vp]),
+    'dm_gather': (_i, [_vp, _i, _i, _i64p, _i, _vp, _vp]),
+    'dm_chop_copy': (_i, [_vp, _i, _i, _d, _vp, _vp]),
+    'dm_pauli_to_matrix_scratch_bytes': (_sz, [_i]),
+    'dm_pauli_to_matrix': (_i, [_vp, _i, _i, _vp, _vp, _vp]),
+    'dm_overlap_scratch_bytes': (_sz, [_i]),
+    'dm_overlap': (_i, [_vp, _vp, _i, _i, _vp, _vp, _vp]),
+    'dm_error_string': (ctypes.c_char_p, [_i]),
+    'dm_kernel_launch_count': (ctypes.c_uint64, []),
+    'dm_version': (ctypes.c_char_p, []),
+}
+
+_LIB = None
+
+
+def lib():
+    """Load libdmgb300.so (raises if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise NativeError('load', DM_ERR_ARG, 'libdmgb300.so is not built (run build())')
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def call(name, *args):
+    """Call an int-returning entry point and raise NativeError on a non-zero status."""
+    L = lib()
+    rc = getattr(L, name)(*args)
+    if rc != DM_OK:
+        raise NativeError(name, rc, L.dm_error_string(rc).decode())
+    return rc
+
+
+def f64_array(values):
+    arr = (ctypes.c_double * len(values))(*[float(v) for v in values])
+    return arr

@@ -1,0 +1,401 @@
+// Gates and noise on the Pauli-coefficient vector.
+//
+// * map1_kernel / cx_kernel: one operation per sweep (the reference applies
+//   every rotation, CX and noise channel as its own full-state numpy sweep,
+//   basicaertools.py:93-126, :310-392; dm_simulator.py:397-425).
+// * pass_kernel: the fused form.  The pass names k "resident" qubit axes; the
+//   4**n vector splits into 4**(n-k) tiles of 4**k coefficients that differ
+//   only in those axes.  One CTA loads a tile into shared memory, applies the
+//   pass's whole operation list to it and writes it back: one HBM read and
+//   one HBM write per coefficient for any number of operations on resident
+//   axes.  Passes always include the lowest (contiguous) axes so that loads
+//   and stores move whole 128-byte lines.
+#include <mutex>
+
+#include "dm_common.cuh"
+
+namespace dmg {
+
+// ---------------------------------------------------------------------------
+// operation bodies on a group of 4 or 16 coefficients
+// ---------------------------------------------------------------------------
+
+template <typename T>
+struct Mat4 {
+    T m[16];
+};
+
+template <typename T>
+struct CxCoef {
+    T c, s, c2, s2, cs;
+};
+
+template <typename T>
+__device__ __forceinline__ void map4(const T *m, bool row0_id, T &x0, T &x1, T &x2, T &x3) {
+    T y0 = row0_id ? x0 : fma(m[0], x0, fma(m[1], x1, fma(m[2], x2, m[3] * x3)));
+    T y1 = fma(m[4], x0, fma(m[5], x1, fma(m[6], x2, m[7] * x3)));
+    T y2 = fma(m[8], x0, fma(m[9], x1, fma(m[10], x2, m[11] * x3)));
+    T y3 = fma(m[12], x0, fma(m[13], x1, fma(m[14], x2, m[15] * x3)));
+    x0 = y0;
+    x1 = y1;
+    x2 = y2;
+    x3 = y3;
+}
+
+// x[4*pc + pt]: control Pauli pc, target Pauli pt.  basicaertools.py:346-363
+// (the control > target branch, :371-388, is the same map in (control,
+// target) coordinates).
+template <typename T>
+__device__ __forceinline__ void cx16(T *x, const CxCoef<T> &k, bool ideal) {
+    if (ideal) {
+        T t;
+        t = x[2]; x[2] = x[14]; x[14] = t;          // IY <-> ZY
+        t = x[3]; x[3] = x[15]; x[15] = t;          // IZ <-> ZZ
+        t = x[4]; x[4] = x[5]; x[5] = t;            // XI <-> XX
+        t = x[8]; x[8] = x[9]; x[9] = t;            // YI <-> YX
+        T xy = x[6], xz = x[7], yy = x[10], yz = x[11];
+        x[6] = yz;                                  // XY <-  YZ
+        x[7] = -yy;                                 // XZ <- -YY
+        x[10] = -xz;                                // YY <- -XZ
+        x[11] = xy;                                 // YZ <-  XY
+        return;
+    }
+    const T c = k.c, s = k.s, c2 = k.c2, s2 = k.s2, cs = k.cs;
+    T i2 = x[2], i3 = x[3], z2 = x[14], z3 = x[15];
+    T x0 = x[4], x1 = x[5], x2 = x[6], x3 = x[7];
+    T y0 = x[8], y1 = x[9], y2 = x[10], y3 = x[11];
+    T d3 = i3 - z3, d2 = i2 - z2;
+    x[2] = fma(s2, i2, fma(c2, z2, -cs * d3));
+    x[14] = fma(c2, i2, fma(s2, z2, cs * d3));
+    x[3] = fma(s2, i3, fma(c2, z3, cs * d2));
+    x[15] = fma(c2, i3, fma(s2, z3, -cs * d2));
+    x[4] = fma(c, x1, -s * y0);
+    x[5] = fma(c, x0, -s * y1);
+    x[6] = fma(-s, y2, c * y3);
+    x[7] = fma(-c, y2, -s * y3);
+    x[8] = fma(s, x0, c * y1);
+    x[9] = fma(s, x1, c * y0);
+    x[10] = fma(s, x2, -c * x3);
+    x[11] = fma(c, x2, s * x3);
+}
+
+// ---------------------------------------------------------------------------
+// single-operation sweeps
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void __launch_bounds__(256) map1_kernel(T *__restrict__ st, int log4s, int64_t ngroups,
+                                                   Mat4<T> m, int row0_id) {
+    const int64_t s = int64_t(1) << (2 * log4s);
+    for (int64_t g = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; g < ngroups;
+         g += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t i0 = ((g >> (2 * log4s)) << (2 * log4s + 2)) | (g & (s - 1));
+        T x0 = st[i0], x1 = st[i0 + s], x2 = st[i0 + 2 * s], x3 = st[i0 + 3 * s];
+        map4(m.m, row0_id != 0, x0, x1, x2, x3);
+        st[i0] = x0;
+        st[i0 + s] = x1;
+        st[i0 + 2 * s] = x2;
+        st[i0 + 3 * s] = x3;
+    }
+}
+
+__device__ __forceinline__ int64_t insert_zero_digit(int64_t g, int pos) {
+    const int64_t low = g & ((int64_t(1) << (2 * pos)) - 1);
+    return ((g >> (2 * pos)) << (2 * pos + 2)) | low;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) cx_kernel(T *__restrict__ st, int pos_c, int pos_t, int64_t ngroups,
+                                                 CxCoef<T> k, int ideal) {
+    const int lo = pos_c < pos_t ? pos_c : pos_t;
+    const int hi = pos_c < pos_t ? pos_t : pos_c;
+    const int64_t sc = int64_t(1) << (2 * pos_c), stt = int64_t(1) << (2 * pos_t);
+    for (int64_t g = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; g < ngroups;
+         g += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t i0 = insert_zero_digit(insert_zero_digit(g, lo), hi);
+        T x[16];
+#pragma unroll
+        for (int pc = 0; pc < 4; ++pc)
+#pragma unroll
+            for (int pt = 0; pt < 4; ++pt) x[4 * pc + pt] = st[i0 + pc * sc + pt * stt];
+        cx16(x, k, ideal != 0);
+#pragma unroll
+        for (int pc = 0; pc < 4; ++pc)
+#pragma unroll
+            for (int pt = 0; pt < 4; ++pt) st[i0 + pc * sc + pt * stt] = x[4 * pc + pt];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// fused pass
+// ---------------------------------------------------------------------------
+
+struct PassDev {
+    int n, k, low, m, nops;
+    int64_t res_stride[DM_MAX_TILE_AXES];      // global stride of local axis r
+    int64_t nonres_stride[DM_MAX_QUBITS];      // global stride of tile-index digit u
+    dm_op ops[DM_MAX_PASS_OPS];
+};
+
+__device__ __forceinline__ int64_t tile_offset(const PassDev &p, int e) {
+    int64_t off = e & ((1 << (2 * p.low)) - 1);
+    for (int r = p.low; r < p.k; ++r) off += int64_t((e >> (2 * r)) & 3) * p.res_stride[r];
+    return off;
+}
+
+template <typename T>
+__device__ void tile_map1(T *tile, int k, int r, const T *__restrict__ mg, bool row0_id) {
+    T m[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) m[i] = mg[i];
+    const int s = 1 << (2 * r);
+    const int ng = 1 << (2 * (k - 1));
+    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+        const int i0 = ((g >> (2 * r)) << (2 * r + 2)) | (g & (s - 1));
+        T x0 = tile[i0], x1 = tile[i0 + s], x2 = tile[i0 + 2 * s], x3 = tile[i0 + 3 * s];
+        map4(m, row0_id, x0, x1, x2, x3);
+        tile[i0] = x0;
+        tile[i0 + s] = x1;
+        tile[i0 + 2 * s] = x2;
+        tile[i0 + 3 * s] = x3;
+    }
+}
+
+__device__ __forceinline__ int insert_zero_digit32(int g, int pos) {
+    return ((g >> (2 * pos)) << (2 * pos + 2)) | (g & ((1 << (2 * pos)) - 1));
+}
+
+template <typename T>
+__device__ void tile_pair(T *tile, int k, const dm_op &op, const T *__restrict__ mg) {
+    const int ra = op.a, rb = op.b;
+    const int lo = ra < rb ? ra : rb, hi = ra < rb ? rb : ra;
+    const int sa = 1 << (2 * ra), sb = 1 << (2 * rb);
+    const int ng = 1 << (2 * (k - 2));
+    CxCoef<T> cx;
+    if (op.kind == DM_OP_CX) {
+        cx.c = mg[0];
+        cx.s = mg[1];
+        cx.c2 = mg[2];
+        cx.s2 = mg[3];
+        cx.cs = mg[4];
+    }
+    const bool ideal = (op.flags & DM_CX_IDEAL) != 0;
+    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+        const int i0 = insert_zero_digit32(insert_zero_digit32(g, lo), hi);
+        T x[16];
+#pragma unroll
+        for (int pa = 0; pa < 4; ++pa)
+#pragma unroll
+            for (int pb = 0; pb < 4; ++pb) x[4 * pa + pb] = tile[i0 + pa * sa + pb * sb];
+        if (op.kind == DM_OP_CX) {
+            cx16(x, cx, ideal);
+        } else {  // DM_OP_MAP2
+            T y[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                T acc = T(0);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) acc = fma(mg[16 * i + j], x[j], acc);
+                y[i] = acc;
+            }
+#pragma unroll
+            for (int i = 0; i < 16; ++i) x[i] = y[i];
+        }
+#pragma unroll
+        for (int pa = 0; pa < 4; ++pa)
+#pragma unroll
+            for (int pb = 0; pb < 4; ++pb) tile[i0 + pa * sa + pb * sb] = x[4 * pa + pb];
+    }
+}
+
+template <typename T>
+__device__ void tile_diag2(T *tile, int k, int ra, int rb, const T *__restrict__ dg) {
+    const int tsize = 1 << (2 * k);
+    for (int e = threadIdx.x; e < tsize; e += blockDim.x) {
+        const int pa = (e >> (2 * ra)) & 3, pb = (e >> (2 * rb)) & 3;
+        tile[e] *= dg[4 * pa + pb];
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) pass_kernel(T *__restrict__ st, const __grid_constant__ PassDev p,
+                                                   const T *__restrict__ mats) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *tile = reinterpret_cast<T *>(smem_raw);
+    const int tsize = 1 << (2 * p.k);
+    const int64_t ntiles = int64_t(1) << (2 * p.m);
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int64_t base = 0;
+        {
+            int64_t tt = t;
+            for (int u = 0; u < p.m; ++u) {
+                base += (tt & 3) * p.nonres_stride[u];
+                tt >>= 2;
+            }
+        }
+        for (int e = threadIdx.x; e < tsize; e += blockDim.x) tile[e] = st[base + tile_offset(p, e)];
+        __syncthreads();
+        for (int i = 0; i < p.nops; ++i) {
+            const dm_op &op = p.ops[i];
+            const T *mg = mats + op.moff;
+            if (op.kind == DM_OP_MAP1)
+                tile_map1(tile, p.k, op.a, mg, (op.flags & DM_MAP1_ROW0_IDENTITY) != 0);
+            else if (op.kind == DM_OP_DIAG2)
+                tile_diag2(tile, p.k, op.a, op.b, mg);
+            else
+                tile_pair(tile, p.k, op, mg);
+            __syncthreads();
+        }
+        for (int e = threadIdx.x; e < tsize; e += blockDim.x) st[base + tile_offset(p, e)] = tile[e];
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+static int build_pass(int n, const dm_pass *in, size_t mats_count, PassDev *out) {
+    if (!in) return DM_ERR_ARG;
+    const int k = in->k;
+    if (k < 1 || k > DM_MAX_TILE_AXES || k > n) return DM_ERR_PROGRAM;
+    if (in->nops < 0 || in->nops > DM_MAX_PASS_OPS) return DM_ERR_PROGRAM;
+    bool resident[DM_MAX_QUBITS] = {false};
+    for (int r = 0; r < k; ++r) {
+        const int q = in->axes[r];
+        if (q < 0 || q >= n) return DM_ERR_PROGRAM;
+        if (r > 0 && q >= in->axes[r - 1]) return DM_ERR_PROGRAM;  // strictly decreasing
+        resident[q] = true;
+        out->res_stride[r] = axis_stride(n, q);
+    }
+    for (int r = k; r < DM_MAX_TILE_AXES; ++r) out->res_stride[r] = 0;
+    int low = 0;
+    while (low < k && in->axes[low] == n - 1 - low) ++low;
+    int m = 0;
+    for (int q = n - 1; q >= 0; --q)
+        if (!resident[q]) out->nonres_stride[m++] = axis_stride(n, q);
+    for (int u = m; u < DM_MAX_QUBITS; ++u) out->nonres_stride[u] = 0;
+    for (int i = 0; i < in->nops; ++i) {
+        const dm_op &op = in->ops[i];
+        size_t need = 0;
+        switch (op.kind) {
+            case DM_OP_MAP1: need = 16; break;
+            case DM_OP_MAP2: need = 256; break;
+            case DM_OP_DIAG2: need = 16; break;
+            case DM_OP_CX: need = 5; break;
+            default: return DM_ERR_PROGRAM;
+        }
+        if (op.a < 0 || op.a >= k) return DM_ERR_PROGRAM;
+        if (op.kind != DM_OP_MAP1 && (op.b < 0 || op.b >= k || op.b == op.a)) return DM_ERR_PROGRAM;
+        if (op.moff < 0 || size_t(op.moff) + need > mats_count) return DM_ERR_PROGRAM;
+        out->ops[i] = op;
+    }
+    out->n = n;
+    out->k = k;
+    out->low = low;
+    out->m = n - k;
+    out->nops = in->nops;
+    return DM_OK;
+}
+
+template <typename T>
+static int launch_pass(T *st, const PassDev &p, const T *mats, cudaStream_t s) {
+    const size_t smem = (size_t(1) << (2 * p.k)) * sizeof(T);
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(pass_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int((size_t(1) << (2 * DM_MAX_TILE_AXES)) * sizeof(T)));
+    });
+    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    int per_sm = 0;
+    DM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pass_kernel<T>, 256, smem));
+    if (per_sm < 1) per_sm = 1;
+    const int64_t ntiles = int64_t(1) << (2 * p.m);
+    int64_t grid = int64_t(sm_count()) * per_sm;
+    if (grid > ntiles) grid = ntiles;
+    pass_kernel<T><<<int(grid), 256, smem, s>>>(st, p, mats);
+    count_launch();
+    return launch_status();
+}
+
+}  // namespace dmg
+
+using namespace dmg;
+
+extern "C" int dm_apply_pass(void *state_dev, int n, int dtype, const dm_pass *pass, const void *mats_dev,
+                             size_t mats_count, void *stream) {
+    DM_CHECK_ARG(state_dev && valid_n(n) && valid_dtype(dtype));
+    DM_CHECK_ARG(mats_dev || mats_count == 0);
+    PassDev p;
+    int rc = build_pass(n, pass, mats_count, &p);
+    if (rc) return rc;
+    if (dtype == DM_F64)
+        return launch_pass(static_cast<double *>(state_dev), p, static_cast<const double *>(mats_dev),
+                           as_stream(stream));
+    return launch_pass(static_cast<float *>(state_dev), p, static_cast<const float *>(mats_dev),
+                       as_stream(stream));
+}
+
+template <typename T>
+static int do_map1(void *state_dev, int n, int q, const double *m4x4, cudaStream_t s) {
+    Mat4<T> m;
+    for (int i = 0; i < 16; ++i) m.m[i] = T(m4x4[i]);
+    const bool row0_id = m4x4[0] == 1.0 && m4x4[1] == 0.0 && m4x4[2] == 0.0 && m4x4[3] == 0.0;
+    const int64_t ngroups = pow4(n - 1);
+    map1_kernel<T><<<grid_for(ngroups, 256), 256, 0, s>>>(static_cast<T *>(state_dev), n - 1 - q, ngroups, m,
+                                                          row0_id ? 1 : 0);
+    count_launch();
+    return launch_status();
+}
+
+extern "C" int dm_apply_map1(void *state_dev, int n, int dtype, int q, const double *m4x4, void *stream) {
+    DM_CHECK_ARG(state_dev && m4x4 && valid_n(n) && valid_dtype(dtype) && q >= 0 && q < n);
+    return dtype == DM_F64 ? do_map1<double>(state_dev, n, q, m4x4, as_stream(stream))
+                           : do_map1<float>(state_dev, n, q, m4x4, as_stream(stream));
+}
+
+// CX coefficients of the transition-selective-pulse model, basicaertools.py:329-336.
+static void cx_coefficients(const double *err, double *c5, bool *ideal) {
+    const double cav = err[0], mean = err[1];
+    const double c2av = 4 * cav - 3;
+    c5[0] = cav * cos(mean);
+    c5[1] = cav * sin(mean);
+    c5[2] = 0.5 * (1 + c2av * cos(2 * mean));
+    c5[3] = 0.5 * (1 - c2av * cos(2 * mean));
+    c5[4] = c2av * sin(mean) * cos(mean);
+    *ideal = c5[0] == 1.0 && c5[1] == 0.0 && c5[2] == 1.0 && c5[3] == 0.0 && c5[4] == 0.0;
+}
+
+template <typename T>
+static int do_cx(void *state_dev, int n, int qc, int qt, const double *err, cudaStream_t s) {
+    double c5[5];
+    bool ideal;
+    cx_coefficients(err, c5, &ideal);
+    CxCoef<T> k{T(c5[0]), T(c5[1]), T(c5[2]), T(c5[3]), T(c5[4])};
+    const int64_t ngroups = pow4(n - 2);
+    cx_kernel<T><<<grid_for(ngroups, 256), 256, 0, s>>>(static_cast<T *>(state_dev), n - 1 - qc, n - 1 - qt,
+                                                        ngroups, k, ideal ? 1 : 0);
+    count_launch();
+    return launch_status();
+}
+
+extern "C" int dm_apply_cx(void *state_dev, int n, int dtype, int qc, int qt, const double *tsp_err2,
+                           void *stream) {
+    DM_CHECK_ARG(state_dev && tsp_err2 && valid_n(n) && valid_dtype(dtype));
+    DM_CHECK_ARG(n >= 2 && qc >= 0 && qt >= 0 && qc < n && qt < n && qc != qt);
+    return dtype == DM_F64 ? do_cx<double>(state_dev, n, qc, qt, tsp_err2, as_stream(stream))
+                           : do_cx<float>(state_dev, n, qc, qt, tsp_err2, as_stream(stream));
+}
+
+extern "C" int dm_apply_memory_noise(void *state_dev, int n, int dtype, double f, double p, double g,
+                                     void *stream) {
+    DM_CHECK_ARG(state_dev && valid_n(n) && valid_dtype(dtype));
+    const double k = sqrt(g) * f, d = (1 - g) * (2 * p - 1);
+    const double m[16] = {1, 0, 0, 0, 0, k, 0, 0, 0, 0, k, 0, d, 0, 0, g};
+    for (int q = 0; q < n; ++q) {
+        int rc = dm_apply_map1(state_dev, n, dtype, q, m, stream);
+        if (rc) return rc;
+    }
+    return DM_OK;
+}

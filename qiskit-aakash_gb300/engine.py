@@ -1,0 +1,214 @@
+"""The device-resident Pauli-coefficient state and its operation queue.
+
+``DeviceState`` owns the 4**n coefficient vector in GPU memory (a torch
+tensor used only as a buffer) and queues gates / noise / measurement updates
+as small Pauli transfer matrices.  Queued operations are executed when a
+read-out needs the state (``flush``): the planner groups them into fused
+passes and each pass is one launch of the library's pass kernel.  Every
+numerical step runs in libdmgb300.so; there is no host fallback.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+from .exceptions import BasicAerError
+from .program import Op, cx_coefficients, encode_pass, plan_passes
+
+# Tile sizes of the fused pass: 4**6 FP64 = 32 KB and 4**7 FP32 = 64 KB of
+# shared memory per tile; the two lowest qubit axes (16 contiguous
+# coefficients, one 128-byte line in FP64) are always resident.
+DEFAULT_TILE_AXES = {'double': 6, 'single': 7}
+DEFAULT_LOW_AXES = 2
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class DeviceState:
+    """An n-qubit Pauli-coefficient vector on a CUDA device."""
+
+    def __init__(self, n, precision='double', fusion=True, tile_axes=None, low_axes=DEFAULT_LOW_AXES,
+                 device=None):
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise BasicAerError('dm_simulator (GB300) needs a CUDA device; none is visible')
+        N.lib()
+        if not 1 <= n <= N.DM_MAX_QUBITS:
+            raise BasicAerError('Number of qubits %d is outside 1..%d' % (n, N.DM_MAX_QUBITS))
+        if precision not in ('double', 'single'):
+            raise BasicAerError("precision must be 'double' or 'single'")
+        self.n = n
+        self.precision = precision
+        self.dtype = N.DM_F64 if precision == 'double' else N.DM_F32
+        self.np_dtype = np.float64 if precision == 'double' else np.float32
+        self.device = torch.device(device if device is not None else 'cuda')
+        self.torch_dtype = torch.float64 if precision == 'double' else torch.float32
+        self.state = torch.empty(4 ** n, dtype=self.torch_dtype, device=self.device)
+        self.fusion = fusion
+        self.kmax = min(tile_axes or DEFAULT_TILE_AXES[precision], N.DM_MAX_TILE_AXES)
+        self.low = low_axes
+        self.pending = []
+        self.passes_run = 0
+        self.h2d_bytes = 0
+        self.d2h_bytes = 0
+
+    # -- plumbing ------------------------------------------------------------
+    @property
+    def stream(self):
+        return ctypes.c_void_p(_torch().cuda.current_stream(self.device).cuda_stream)
+
+    @property
+    def ptr(self):
+        return ctypes.c_void_p(self.state.data_ptr())
+
+    def _to_host(self, t):
+        self.d2h_bytes += t.numel() * t.element_size()
+        return t.cpu().numpy()
+
+    # -- set-up --------------------------------------------------------------
+    def init_product(self, vectors, scale):
+        v = np.ascontiguousarray(np.asarray(vectors, dtype=np.float64).reshape(self.n, 4))
+        self.pending = []
+        N.call('dm_init_product', self.ptr, self.n, self.dtype,
+               v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), float(scale), self.stream)
+
+    def load(self, coeffs):
+        a = np.ascontiguousarray(np.asarray(coeffs, dtype=np.float64).reshape(-1))
+        if a.size != 4 ** self.n:
+            raise BasicAerError('initial densitymatrix is incorrect length: %d != %d' % (a.size, 4 ** self.n))
+        self.pending = []
+        self.h2d_bytes += a.size * (8 if self.dtype == N.DM_F64 else 4)
+        N.call('dm_load_state', self.ptr, self.n, self.dtype,
+               a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), self.stream)
+
+    # -- queued operations ---------------------------------------------------
+    def map1(self, q, m):
+        self.pending.append(Op('map1', (q,), np.asarray(m, dtype=np.float64)))
+
+    def cx(self, ctl, tgt, tsp):
+        coef, ideal = cx_coefficients(tsp)
+        self.pending.append(Op('cx', (ctl, tgt), np.array(coef), ideal))
+
+    def diag2(self, qa, qb, d):
+        self.pending.append(Op('diag2', (qa, qb), np.asarray(d, dtype=np.float64)))
+
+    def flush(self):
+        """Run every queued operation (fused passes, or one sweep per operation)."""
+        if not self.pending:
+            return
+        ops, self.pending = self.pending, []
+        if not self.fusion:
+            self._run_unfused(ops)
+            return
+        passes = plan_passes(ops, self.n, self.kmax, self.low)
+        self._run_passes(passes)
+
+    def _run_passes(self, passes):
+        torch = _torch()
+        mats = []
+        descs = [encode_pass(p, mats, self.np_dtype) for p in passes]
+        host = np.concatenate(mats) if mats else np.zeros(1, dtype=self.np_dtype)
+        h = torch.from_numpy(host)
+        if self.device.type == 'cuda':
+            h = h.pin_memory()
+        dev = h.to(self.device, non_blocking=True)
+        self.h2d_bytes += host.nbytes
+        mp = ctypes.c_void_p(dev.data_ptr())
+        for d in descs:
+            N.call('dm_apply_pass', self.ptr, self.n, self.dtype, ctypes.byref(d), mp,
+                   ctypes.c_size_t(host.size), self.stream)
+        self.passes_run += len(descs)
+        self._keep = (h, dev)    # keep both alive until the next flush
+
+    def _run_unfused(self, ops):
+        for op in ops:
+            if op.kind == 'map1':
+                m = np.ascontiguousarray(op.data, dtype=np.float64).reshape(16)
+                N.call('dm_apply_map1', self.ptr, self.n, self.dtype, op.axes[0],
+                       m.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), self.stream)
+            elif op.kind == 'cx':
+                # dm_apply_cx recomputes the coefficients from (<cos a>, mean a)
+                self._run_passes(plan_passes([op], self.n, self.kmax, self.low))
+            else:
+                self._run_passes(plan_passes([op], self.n, self.kmax, self.low))
+
+    # -- read-outs (each flushes first) --------------------------------------
+    def axis_probs(self, mode, err):
+        """Probabilities for per-qubit measurement axes mode[q] in {0 (unmeasured), 1, 2, 3}."""
+        self.flush()
+        torch = _torch()
+        m = sum(1 for x in mode if x)
+        out = torch.empty(2 ** m, dtype=torch.float64, device=self.device)
+        md = (ctypes.c_int * self.n)(*[int(x) for x in mode])
+        N.call('dm_axis_probs', self.ptr, self.n, self.dtype, md, float(err),
+               ctypes.c_void_p(out.data_ptr()), self.stream)
+        return self._to_host(out)
+
+    def nbasis_probs(self, nvec, err):
+        self.flush()
+        torch = _torch()
+        L = N.lib()
+        nbytes = L.dm_nbasis_probs_scratch_bytes(self.n)
+        scratch = torch.empty(max(nbytes, 8), dtype=torch.uint8, device=self.device)
+        out = torch.empty(2 ** self.n, dtype=torch.float64, device=self.device)
+        v = N.f64_array(nvec)
+        N.call('dm_nbasis_probs', self.ptr, self.n, self.dtype, v, float(err),
+               ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(scratch.data_ptr()), self.stream)
+        return self._to_host(out)
+
+    def gather(self, indices):
+        self.flush()
+        torch = _torch()
+        out = []
+        idx = [int(i) for i in indices]
+        for s in range(0, len(idx), 64):
+            chunk = idx[s:s + 64]
+            o = torch.empty(len(chunk), dtype=torch.float64, device=self.device)
+            arr = (ctypes.c_int64 * len(chunk))(*chunk)
+            N.call('dm_gather', self.ptr, self.n, self.dtype, arr, len(chunk),
+                   ctypes.c_void_p(o.data_ptr()), self.stream)
+            out.append(self._to_host(o))
+        return np.concatenate(out)
+
+    def coefficients(self, chop_threshold):
+        """FP64 copy of the coefficients with |a| < chop_threshold set to 0."""
+        self.flush()
+        torch = _torch()
+        out = torch.empty(4 ** self.n, dtype=torch.float64, device=self.device)
+        N.call('dm_chop_copy', self.ptr, self.n, self.dtype, float(chop_threshold),
+               ctypes.c_void_p(out.data_ptr()), self.stream)
+        return self._to_host(out)
+
+    def raw_coefficients(self):
+        """FP64 copy of the unchopped coefficients."""
+        return self.coefficients(0.0)
+
+    def density_matrix(self):
+        """2**n x 2**n complex matrix in the computational basis."""
+        self.flush()
+        torch = _torch()
+        L = N.lib()
+        scratch = torch.empty(L.dm_pauli_to_matrix_scratch_bytes(self.n), dtype=torch.uint8, device=self.device)
+        out = torch.empty((2 ** self.n, 2 ** self.n), dtype=torch.complex128, device=self.device)
+        N.call('dm_pauli_to_matrix', self.ptr, self.n, self.dtype, ctypes.c_void_p(out.data_ptr()),
+               ctypes.c_void_p(scratch.data_ptr()), self.stream)
+        return self._to_host(out)
+
+    def overlap(self, other_coeffs):
+        """2**n * <a, b> against a host coefficient vector."""
+        self.flush()
+        torch = _torch()
+        b = torch.from_numpy(np.asarray(other_coeffs, dtype=self.np_dtype).reshape(-1)).to(self.device)
+        self.h2d_bytes += b.numel() * b.element_size()
+        L = N.lib()
+        scratch = torch.empty(L.dm_overlap_scratch_bytes(self.n), dtype=torch.uint8, device=self.device)
+        out = torch.empty(1, dtype=torch.float64, device=self.device)
+        N.call('dm_overlap', self.ptr, ctypes.c_void_p(b.data_ptr()), self.n, self.dtype,
+               ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(scratch.data_ptr()), self.stream)
+        return float(self._to_host(out)[0])
+
+    def synchronize(self):
+        _torch().cuda.synchronize(self.device)

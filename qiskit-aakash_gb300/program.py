@@ -1,0 +1,256 @@
+"""Pauli transfer matrices and the fused-pass planner.
+
+Every gate, noise channel and measurement update of the reference acts on
+one or two Pauli axes of the coefficient vector as a small real linear map:
+
+* rotations Rz/Ry/Rx with the averaged-angle error model
+  (basicaertools.py:93-126): a 4x4 map mixing two of X, Y, Z;
+  U3 = Rz(lambda), Ry(theta), Rz(phi) applied in that order
+  (basicaertools.py:69-90);
+* memory noise (dm_simulator.py:397-425): X, Y scaled by sqrt(g) f and
+  Z <- g Z + (1-g)(2p-1) I, a 4x4 map with an I->Z entry;
+* X/Y/Z/N measurement updates (dm_simulator.py:574-704) and reset
+  (:810-823): 4x4 projections;
+* CX with the transition-selective-pulse error (basicaertools.py:310-392):
+  a 16-entry map on the (control, target) pair, a signed permutation when
+  ideal;
+* the Bell-basis projection (dm_simulator.py:749-756): a diagonal 16-entry map.
+
+The planner turns a run of such operations into fused passes: each pass
+names up to ``kmax`` resident qubit axes (always including the lowest
+``low`` axes, which are contiguous in memory) and the operations it applies
+to every tile of those axes.  Operations on disjoint axes commute, so an
+operation may run in an earlier pass than an operation that precedes it in
+program order, provided every earlier operation sharing one of its axes
+has run: the planner scans the pending operations in order and takes every
+operation whose axes fit in the pass and none of whose axes is held back by
+an earlier operation it could not take.  Consecutive 4x4 maps on one axis
+inside a pass are multiplied together (in FP64) into one map.
+"""
+import math
+
+import numpy as np
+
+from . import _native as N
+
+_ROT_PLANES = {'rz': (1, 2), 'ry': (3, 1), 'rx': (2, 3)}
+
+IDENTITY4 = np.eye(4)
+
+
+def rotation_ptm(axis, angle, err):
+    """4x4 map of one rotation with error (<cos>, mean): basicaertools.py:106-124."""
+    if axis not in _ROT_PLANES:
+        from .exceptions import QiskitError
+        raise QiskitError('Gate is not among the valid decomposition types: %s' % axis)
+    c = err[0] * math.cos(angle + err[1])
+    s = err[0] * math.sin(angle + err[1])
+    k0, k1 = _ROT_PLANES[axis]
+    m = np.eye(4)
+    m[k0, k0] = c
+    m[k0, k1] = -s
+    m[k1, k1] = c
+    m[k1, k0] = s
+    return m
+
+
+def u_gate_ptm(name, params, rotation_error):
+    """u1 / u3 as the product of its rotations (basicaertools.py:69-90)."""
+    p = [float(x) for x in params]
+    if name in ('U', 'u3'):
+        seq = (('rz', p[2]), ('ry', p[0]), ('rz', p[1]))
+    elif name == 'u1':
+        seq = (('rz', p[0]),)
+    else:
+        from .exceptions import QiskitError
+        raise QiskitError('Gate is not among the valid types: %s' % name)
+    m = np.eye(4)
+    for axis, ang in seq:
+        m = rotation_ptm(axis, ang, rotation_error[axis]) @ m
+    return m
+
+
+def noise_ptm(f, p, g):
+    """Per-qubit memory noise of one clock cycle (dm_simulator.py:408-422)."""
+    k = math.sqrt(g) * f
+    d = (1 - g) * (2 * p - 1)
+    m = np.zeros((4, 4))
+    m[0, 0] = 1.0
+    m[1, 1] = k
+    m[2, 2] = k
+    m[3, 3] = g
+    m[3, 0] = d
+    return m
+
+
+def measure_ptm(basis, err, nvec=None):
+    """State update of a single-qubit measurement (dm_simulator.py:574-704)."""
+    m = np.zeros((4, 4))
+    m[0, 0] = 1.0
+    if basis == 'X':
+        m[1, 1] = err
+    elif basis == 'Y':
+        m[2, 2] = err
+    elif basis == 'Z':
+        m[3, 3] = err
+    elif basis == 'N':
+        v = [float(x) for x in nvec]
+        for r in range(3):
+            for c in range(3):
+                m[r + 1, c + 1] = err * v[r] * v[c]
+    else:
+        raise ValueError(basis)
+    return m
+
+
+def reset_ptm():
+    """Reset to |0>: X, Y <- 0, Z <- I (dm_simulator.py:810-823)."""
+    m = np.zeros((4, 4))
+    m[0, 0] = 1.0
+    m[3, 0] = 1.0
+    return m
+
+
+def cx_coefficients(tsp):
+    """(c, s, c2, s2, cs) of the noisy CX, basicaertools.py:329-336, and whether it is ideal."""
+    cav, mean = float(tsp[0]), float(tsp[1])
+    c2av = 4 * cav - 3
+    coef = (cav * math.cos(mean), cav * math.sin(mean),
+            0.5 * (1 + c2av * math.cos(2 * mean)), 0.5 * (1 - c2av * math.cos(2 * mean)),
+            c2av * math.sin(mean) * math.cos(mean))
+    ideal = coef == (1.0, 0.0, 1.0, 0.0, 0.0)
+    return coef, ideal
+
+
+def bell_projection_diag(err):
+    """Diagonal of the Bell-measurement update on (slower axis, faster axis), index 4*i + j."""
+    d = np.zeros(16)
+    d[0] = 1.0
+    for i in (1, 2, 3):
+        d[5 * i] = err
+    return d
+
+
+# ---------------------------------------------------------------------------
+# operations
+# ---------------------------------------------------------------------------
+
+class Op:
+    """One pending operation: kind in {'map1', 'cx', 'diag2', 'map2'}; axes are qubits."""
+    __slots__ = ('kind', 'axes', 'data', 'ideal')
+
+    def __init__(self, kind, axes, data, ideal=False):
+        self.kind = kind
+        self.axes = tuple(axes)
+        self.data = data
+        self.ideal = ideal
+
+    def __repr__(self):
+        return 'Op(%s, %s)' % (self.kind, self.axes)
+
+
+class Pass:
+    """A planned pass: resident qubits (decreasing) and ops with local axes."""
+    __slots__ = ('axes', 'ops')
+
+    def __init__(self, axes, ops):
+        self.axes = axes
+        self.ops = ops
+
+    def local(self, q):
+        return self.axes.index(q)
+
+
+def plan_passes(ops, n, kmax, low):
+    """Group ``ops`` (program order) into fused passes.
+
+    Returns a list of Pass; each pass's op list preserves program order
+    among the ops it holds, and per axis the ops of successive passes are
+    consecutive runs of that axis's ops, so applying the passes in order
+    equals applying ``ops`` in order.
+    """
+    kmax = min(kmax, n)
+    low = min(low, kmax)
+    base = tuple(range(n - 1, n - 1 - low, -1))
+    pending = list(ops)
+    passes = []
+    while pending:
+        resident = set(base)
+        full = len(resident) >= kmax
+        blocked = set()
+        taken_idx = []
+        body = []          # list of Op (possibly composed)
+        last_on_axis = {}  # axis -> index into body of the last op touching it
+        for i, op in enumerate(pending):
+            axes = op.axes
+            if blocked.intersection(axes) or \
+                    len(resident) + sum(a not in resident for a in axes) > kmax or \
+                    len(body) >= N.DM_MAX_PASS_OPS:
+                blocked.update(axes)
+                # Once the pass is full and every resident axis is held back,
+                # no later operation can be taken.
+                if (full and blocked.issuperset(resident)) or len(blocked) >= n:
+                    break
+                continue
+            grow = [a for a in axes if a not in resident]
+            resident.update(grow)
+            taken_idx.append(i)
+            if op.kind == 'map1':
+                a = axes[0]
+                j = last_on_axis.get(a)
+                if j is not None and body[j].kind == 'map1':
+                    body[j] = Op('map1', (a,), op.data @ body[j].data)
+                    continue
+                body.append(Op('map1', axes, op.data))
+            else:
+                body.append(op)
+            for a in axes:
+                last_on_axis[a] = len(body) - 1
+            if len(resident) >= kmax:
+                full = True
+        if not taken_idx:
+            raise RuntimeError('planner made no progress')
+        keep = set(taken_idx)
+        pending = [op for i, op in enumerate(pending) if i not in keep]
+        axes = sorted(resident, reverse=True)
+        passes.append(Pass(axes, body))
+    return passes
+
+
+def encode_pass(p, mats, dtype_np):
+    """Fill a ctypes DmPass for ``p``; append its coefficients to ``mats`` (list of arrays)."""
+    dp = N.DmPass()
+    dp.k = len(p.axes)
+    for r, q in enumerate(p.axes):
+        dp.axes[r] = q
+    dp.nops = len(p.ops)
+    off = sum(m.size for m in mats)
+    for i, op in enumerate(p.ops):
+        o = dp.ops[i]
+        o.a = p.local(op.axes[0])
+        o.moff = off
+        if op.kind == 'map1':
+            o.kind = N.DM_OP_MAP1
+            m = np.ascontiguousarray(op.data, dtype=np.float64).reshape(16)
+            o.flags = N.DM_MAP1_ROW0_IDENTITY if (m[0] == 1.0 and not m[1:4].any()) else 0
+            o.b = 0
+        elif op.kind == 'cx':
+            o.kind = N.DM_OP_CX
+            o.b = p.local(op.axes[1])
+            o.flags = N.DM_CX_IDEAL if op.ideal else 0
+            m = np.asarray(op.data, dtype=np.float64)
+        elif op.kind == 'diag2':
+            o.kind = N.DM_OP_DIAG2
+            o.b = p.local(op.axes[1])
+            o.flags = 0
+            m = np.asarray(op.data, dtype=np.float64).reshape(16)
+        elif op.kind == 'map2':
+            o.kind = N.DM_OP_MAP2
+            o.b = p.local(op.axes[1])
+            o.flags = 0
+            m = np.asarray(op.data, dtype=np.float64).reshape(256)
+        else:
+            raise ValueError(op.kind)
+        mats.append(m.astype(dtype_np))
+        off += m.size
+    return dp

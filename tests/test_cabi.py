@@ -1,0 +1,89 @@
+"""The C-ABI library builds for sm_103a, loads, and exports what include/dm_gb300.h declares.
+
+No kernel runs here: only calls that the library rejects on the host
+(invalid arguments) are made.
+"""
+import ctypes
+import os
+import re
+
+import pytest
+
+from qiskit_aakash_gb300 import _native as N
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), 'include', 'dm_gb300.h')
+
+
+@pytest.fixture(scope='module')
+def lib():
+    N.build()
+    return N.lib()
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
+    return sorted(set(re.findall(r'\b(dm_[a-z0-9_]+)\s*\(', text)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert len(names) >= 18
+    for name in names:
+        assert hasattr(lib, name), name
+        assert name in N.SIGNATURES, name
+
+
+def test_struct_layout_matches_header():
+    assert ctypes.sizeof(N.DmOp) == 16
+    assert ctypes.sizeof(N.DmPass) == 4 + 4 * N.DM_MAX_TILE_AXES + 4 + 16 * N.DM_MAX_PASS_OPS
+    text = open(HEADER).read()
+    assert int(re.search(r'#define DM_MAX_TILE_AXES (\d+)', text).group(1)) == N.DM_MAX_TILE_AXES
+    assert int(re.search(r'#define DM_MAX_PASS_OPS (\d+)', text).group(1)) == N.DM_MAX_PASS_OPS
+    assert int(re.search(r'#define DM_MAX_QUBITS (\d+)', text).group(1)) == N.DM_MAX_QUBITS
+
+
+def test_error_strings_and_version(lib):
+    assert lib.dm_error_string(0) == b'ok'
+    assert b'invalid' in lib.dm_error_string(-1)
+    assert lib.dm_version().startswith(b'dm_gb300')
+
+
+def test_invalid_arguments_are_rejected_on_host(lib):
+    m = N.f64_array([0.0] * 16)
+    # null state, bad qubit, bad dtype, bad n: all rejected before any CUDA call
+    assert lib.dm_apply_map1(None, 4, 0, 0, m, None) == N.DM_ERR_ARG
+    assert lib.dm_apply_map1(ctypes.c_void_p(16), 4, 0, 7, m, None) == N.DM_ERR_ARG
+    assert lib.dm_apply_map1(ctypes.c_void_p(16), 4, 5, 0, m, None) == N.DM_ERR_ARG
+    assert lib.dm_apply_map1(ctypes.c_void_p(16), 0, 0, 0, m, None) == N.DM_ERR_ARG
+    assert lib.dm_apply_map1(ctypes.c_void_p(16), 18, 0, 0, m, None) == N.DM_ERR_ARG
+    tsp = N.f64_array([1.0, 0.0])
+    assert lib.dm_apply_cx(ctypes.c_void_p(16), 4, 0, 2, 2, tsp, None) == N.DM_ERR_ARG
+    assert lib.dm_apply_cx(ctypes.c_void_p(16), 1, 0, 0, 1, tsp, None) == N.DM_ERR_ARG
+    idx = (ctypes.c_int64 * 1)(4 ** 4)
+    assert lib.dm_gather(ctypes.c_void_p(16), 4, 0, idx, 1, ctypes.c_void_p(16), None) == N.DM_ERR_ARG
+    mode = (ctypes.c_int * 4)(0, 4, 0, 0)
+    assert lib.dm_axis_probs(ctypes.c_void_p(16), 4, 0, mode, 1.0, ctypes.c_void_p(16), None) == N.DM_ERR_ARG
+
+
+def test_malformed_pass_is_rejected_on_host(lib):
+    p = N.DmPass()
+    p.k = 3
+    p.axes[0], p.axes[1], p.axes[2] = 3, 4, 2          # not strictly decreasing
+    p.nops = 0
+    rc = lib.dm_apply_pass(ctypes.c_void_p(16), 5, 0, ctypes.byref(p), ctypes.c_void_p(16), 16, None)
+    assert rc == N.DM_ERR_PROGRAM
+    p.axes[0], p.axes[1], p.axes[2] = 4, 3, 2
+    p.nops = 1
+    p.ops[0].kind = N.DM_OP_MAP1
+    p.ops[0].a = 0
+    p.ops[0].moff = 8                                  # 8 + 16 > 16 coefficients
+    rc = lib.dm_apply_pass(ctypes.c_void_p(16), 5, 0, ctypes.byref(p), ctypes.c_void_p(16), 16, None)
+    assert rc == N.DM_ERR_PROGRAM
+    p.ops[0].moff = 0
+    p.ops[0].a = 3                                     # local axis beyond k
+    rc = lib.dm_apply_pass(ctypes.c_void_p(16), 5, 0, ctypes.byref(p), ctypes.c_void_p(16), 16, None)
+    assert rc == N.DM_ERR_PROGRAM
+    p.k = 8                                            # beyond DM_MAX_TILE_AXES
+    rc = lib.dm_apply_pass(ctypes.c_void_p(16), 9, 0, ctypes.byref(p), ctypes.c_void_p(16), 16, None)
+    assert rc == N.DM_ERR_PROGRAM

@@ -1,0 +1,178 @@
+"""Each C-ABI entry point on the GPU against the CPU oracle's numpy kernels."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import dm_oracle as O
+from qiskit_aakash_gb300 import _native as N
+from qiskit_aakash_gb300 import program as P
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module')
+def torch():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.fail('CUDA device required for the gpu tests')
+    N.build()
+    N.lib()
+    return torch
+
+
+def dev(torch, a, dtype=np.float64):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=dtype)).cuda()
+
+
+def vp(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def stream(torch):
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def dparr(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+@pytest.mark.parametrize('n', [1, 2, 3, 5, 8])
+@pytest.mark.parametrize('dtype', [N.DM_F64, N.DM_F32])
+def test_map1_cx_noise(torch, n, dtype):
+    rng = np.random.default_rng(n)
+    npdt = np.float64 if dtype == N.DM_F64 else np.float32
+    tol = 1e-13 if dtype == N.DM_F64 else 2e-6
+    st = rng.normal(size=4 ** n)
+    t = dev(torch, st, npdt)
+    ref = st.copy()
+    for q in range(n):
+        m = rng.normal(size=(4, 4))
+        keep, ptr = dparr(m.reshape(16))
+        N.call('dm_apply_map1', vp(t), n, dtype, q, ptr, stream(torch))
+        v = ref.reshape(4 ** q, 4, 4 ** (n - q - 1))
+        ref = np.einsum('ij,ajb->aib', m, v).reshape(-1)
+    if n >= 2:
+        for (c, tq) in [(0, n - 1), (n - 1, 0), (n // 2, (n // 2 + 1) % n)]:
+            if c == tq:
+                continue
+            for tsp in ([1.0, 0.0], [0.96, 0.07]):
+                keep, ptr = dparr(tsp)
+                N.call('dm_apply_cx', vp(t), n, dtype, c, tq, ptr, stream(torch))
+                ref = O.cx_apply(ref, n, c, tq, tsp)
+    N.call('dm_apply_memory_noise', vp(t), n, dtype, 0.97, 0.2, 0.93, stream(torch))
+    ref = O.memory_noise(ref, n, 0.97, 0.2, 0.93)
+    got = t.double().cpu().numpy()
+    np.testing.assert_allclose(got, ref, rtol=0, atol=tol * np.abs(ref).max() * 10)
+
+
+@pytest.mark.parametrize('n,k,low', [(4, 4, 2), (6, 6, 2), (7, 5, 2), (8, 6, 2), (9, 7, 2), (9, 7, 3), (10, 6, 0)])
+@pytest.mark.parametrize('dtype', [N.DM_F64, N.DM_F32])
+def test_fused_pass_equals_program_order(torch, n, k, low, dtype):
+    from test_planner import apply_op, random_ops
+    rng = np.random.default_rng(1000 + n * 7 + k)
+    npdt = np.float64 if dtype == N.DM_F64 else np.float32
+    ops = random_ops(rng, n, 80)
+    for op in ops:                       # keep magnitudes bounded
+        if op.kind == 'map1':
+            op.data = op.data / np.abs(op.data).sum(axis=1, keepdims=True)
+        elif op.kind == 'diag2':
+            op.data = np.clip(op.data, -1, 1)
+    st = rng.normal(size=4 ** n)
+    ref = st.copy()
+    for op in ops:
+        ref = apply_op(ref, n, op)
+    passes = P.plan_passes(ops, n, k, low)
+    mats = []
+    descs = [P.encode_pass(p, mats, npdt) for p in passes]
+    m = np.concatenate(mats)
+    md = dev(torch, m, npdt)
+    t = dev(torch, st, npdt)
+    for d in descs:
+        N.call('dm_apply_pass', vp(t), n, dtype, ctypes.byref(d), vp(md), ctypes.c_size_t(m.size), stream(torch))
+    got = t.double().cpu().numpy()
+    tol = 1e-12 if dtype == N.DM_F64 else 1e-4
+    np.testing.assert_allclose(got, ref, rtol=0, atol=tol * np.abs(ref).max())
+
+
+@pytest.mark.parametrize('n', [1, 3, 6, 11, 12, 13])
+def test_axis_probs_and_partial(torch, n):
+    rng = np.random.default_rng(n + 50)
+    st = rng.normal(size=4 ** n) / 2 ** n
+    t = dev(torch, st)
+    for basis, col in (('X', 1), ('Y', 2), ('Z', 3)):
+        out = torch.empty(2 ** n, dtype=torch.float64, device='cuda')
+        mode = (ctypes.c_int * n)(*([col] * n))
+        N.call('dm_axis_probs', vp(t), n, N.DM_F64, mode, 0.97, vp(out), stream(torch))
+        ref = O.ensemble_probabilities(st, n, basis, None, 0.97)
+        np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=0, atol=1e-12 * max(1, np.abs(ref).max()))
+    # marginal over a random subset of measured qubits
+    meas = sorted(int(x) for x in rng.choice(n, max(1, n // 2), replace=False))
+    full = O.ensemble_probabilities(st, n, 'Z', None, 0.9)
+    others = tuple(sorted(set(range(n)) - set(meas)))
+    ref = np.sum(full.reshape([2] * n), axis=others).reshape(-1)
+    out = torch.empty(2 ** len(meas), dtype=torch.float64, device='cuda')
+    mode = (ctypes.c_int * n)(*[3 if q in meas else 0 for q in range(n)])
+    N.call('dm_axis_probs', vp(t), n, N.DM_F64, mode, 0.9, vp(out), stream(torch))
+    np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=0, atol=1e-12 * max(1, np.abs(ref).max()))
+
+
+@pytest.mark.parametrize('n', [1, 2, 3, 4, 7, 10])
+def test_nbasis_probs(torch, n):
+    rng = np.random.default_rng(n + 70)
+    st = rng.normal(size=4 ** n) / 2 ** n
+    nvec = rng.normal(size=3)
+    nvec /= np.linalg.norm(nvec)
+    t = dev(torch, st)
+    L = N.lib()
+    scratch = torch.empty(max(8, L.dm_nbasis_probs_scratch_bytes(n)), dtype=torch.uint8, device='cuda')
+    out = torch.empty(2 ** n, dtype=torch.float64, device='cuda')
+    keep, ptr = dparr(nvec)
+    N.call('dm_nbasis_probs', vp(t), n, N.DM_F64, ptr, 0.95, vp(out), vp(scratch), stream(torch))
+    ref = O.ensemble_probabilities(st, n, 'N', nvec, 0.95)
+    np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=0, atol=1e-12 * max(1, np.abs(ref).max()))
+
+
+@pytest.mark.parametrize('n', [1, 2, 5, 7])
+def test_pauli_to_matrix_chop_gather_overlap(torch, n):
+    rng = np.random.default_rng(n + 90)
+    st = rng.normal(size=4 ** n)
+    st[rng.random(4 ** n) < 0.3] *= 1e-17
+    t = dev(torch, st)
+    L = N.lib()
+    scratch = torch.empty(L.dm_pauli_to_matrix_scratch_bytes(n), dtype=torch.uint8, device='cuda')
+    out = torch.empty((2 ** n, 2 ** n), dtype=torch.complex128, device='cuda')
+    N.call('dm_pauli_to_matrix', vp(t), n, N.DM_F64, vp(out), vp(scratch), stream(torch))
+    np.testing.assert_allclose(out.cpu().numpy(), O.pauli_to_matrix(st, n), rtol=0, atol=1e-12)
+    ch = torch.empty(4 ** n, dtype=torch.float64, device='cuda')
+    N.call('dm_chop_copy', vp(t), n, N.DM_F64, 1e-15, vp(ch), stream(torch))
+    ref = st.copy()
+    ref[np.abs(ref) < 1e-15] = 0
+    assert np.array_equal(ch.cpu().numpy(), ref)
+    idx = rng.integers(0, 4 ** n, size=min(64, 4 ** n))
+    g = torch.empty(len(idx), dtype=torch.float64, device='cuda')
+    N.call('dm_gather', vp(t), n, N.DM_F64, (ctypes.c_int64 * len(idx))(*idx.tolist()), len(idx), vp(g),
+           stream(torch))
+    assert np.array_equal(g.cpu().numpy(), st[idx])
+    other = rng.normal(size=4 ** n)
+    o = dev(torch, other)
+    sc = torch.empty(L.dm_overlap_scratch_bytes(n), dtype=torch.uint8, device='cuda')
+    res = torch.empty(1, dtype=torch.float64, device='cuda')
+    N.call('dm_overlap', vp(t), vp(o), n, N.DM_F64, vp(res), vp(sc), stream(torch))
+    ref = np.dot(st, other) * 2 ** n
+    assert abs(res.item() - ref) <= 1e-12 * np.abs(st * other).sum() * 2 ** n
+
+
+@pytest.mark.parametrize('n', [1, 4, 9])
+def test_init_product(torch, n):
+    rng = np.random.default_rng(n + 110)
+    vecs = rng.normal(size=(n, 4))
+    vecs[rng.random((n, 4)) < 0.4] = 0
+    t = torch.empty(4 ** n, dtype=torch.float64, device='cuda')
+    keep, ptr = dparr(vecs.reshape(-1))
+    N.call('dm_init_product', vp(t), n, N.DM_F64, ptr, 0.5 ** n, stream(torch))
+    ref = np.array([1.0])
+    for q in range(n):
+        ref = np.kron(ref, vecs[q])
+    np.testing.assert_allclose(t.cpu().numpy(), ref * 0.5 ** n, rtol=1e-15, atol=0)

@@ -1,0 +1,129 @@
+"""GPU parity of the drop-in backend against the reference's outputs and the oracle.
+
+* every golden case (produced by the unmodified reference) through
+  ``DmSimulatorGPU.run_experiment``: FP64 fused, FP64 one-sweep-per-op, and
+  FP32 fused;
+* larger seeded workloads against the CPU oracle;
+* n = 14 (the 2.1 GB FP64 state of the 14-qubit workload) through
+  size-independent properties.
+
+Tolerances: FP64 paths agree with the reference to 1e-12 on the Pauli
+expectations 2**n a_s and on probabilities; FP32 paths to 2e-5.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+import golden_cases as G
+import qiskit_aakash_gb300 as dmg
+from oracle import dm_oracle as O
+from test_oracle import compare_outputs
+
+pytestmark = pytest.mark.gpu
+
+CASES = [c for c in G.cases() if 'error' not in c]
+
+
+@pytest.fixture(scope='module', autouse=True)
+def _gpu():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.fail('CUDA device required for the gpu tests')
+    dmg.build()
+
+
+def run_gpu(exp, opts, **extra):
+    from qiskit_aakash_gb300.dm_simulator import DmSimulatorGPU
+    DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
+    b = DmSimulatorGPU()
+    o = copy.deepcopy(opts)
+    o.update(extra)
+    b._set_options(backend_options=o)
+    res = b.run_experiment(exp)
+    return res, b
+
+
+@pytest.mark.parametrize('c', CASES, ids=lambda c: c['name'])
+def test_golden_fp64_fused(c):
+    res, _ = run_gpu(G.experiment(c), G.options(c))
+    assert res['number_of_clock_cycles'] == c['number_of_clock_cycles']
+    compare_outputs(c, res['data'], rel=1e-12)
+
+
+@pytest.mark.parametrize('c', CASES[::3], ids=lambda c: c['name'])
+def test_golden_fp64_one_sweep_per_op(c):
+    res, _ = run_gpu(G.experiment(c), G.options(c), fusion=False)
+    compare_outputs(c, res['data'], rel=1e-12)
+
+
+@pytest.mark.parametrize('c', CASES[::2], ids=lambda c: c['name'])
+def test_golden_fp32_fused(c):
+    res, _ = run_gpu(G.experiment(c), G.options(c), precision='single')
+    compare_outputs(c, res['data'], rel=2e-5)
+
+
+def _oracle(exp, opts):
+    return O.OracleDmSimulator(copy.deepcopy(opts)).run_experiment(copy.deepcopy(exp))
+
+
+def _assert_close(a, b, n, rel):
+    for k, v in b['data'].items():
+        g = a['data'][k]
+        if isinstance(v, dict):
+            assert list(g.keys()) == list(v.keys())
+            np.testing.assert_allclose(list(g.values()), list(v.values()), rtol=0, atol=rel)
+        elif k == 'coeffmatrix':
+            np.testing.assert_allclose(np.asarray(g) * 2 ** n, np.asarray(v) * 2 ** n, rtol=0, atol=rel)
+        else:
+            np.testing.assert_allclose(np.asarray(g), np.asarray(v), rtol=0, atol=rel)
+
+
+@pytest.mark.parametrize('n,layers,seed,every_gate,qft', [
+    (10, 6, 11, False, False),
+    (11, 3, 12, False, False),
+    (8, 2, 13, True, True),
+    (9, 3, 14, True, False),
+])
+def test_workloads_match_oracle(n, layers, seed, every_gate, qft):
+    qc = dmg.random_layer_circuit(n, layers, seed, barrier_after_gate=every_gate, qft=qft)
+    opts = dmg.noise_options(depolarisation=1e-3, decoherence=0.995, decay=0.998, rotation_sigma=1e-3)
+    opts['compute_densitymatrix'] = False
+    ref = _oracle(qc.to_experiment(), opts)
+    for kw, tol in (({}, 1e-12), ({'tile_axes': 7}, 1e-12), ({'tile_axes': 4}, 1e-12),
+                    ({'precision': 'single'}, 2e-5)):
+        got, b = run_gpu(qc.to_experiment(), opts, **kw)
+        assert got['number_of_clock_cycles'] == ref['number_of_clock_cycles']
+        _assert_close(got, ref, n, tol)
+
+
+def test_fourteen_qubit_properties():
+    """14 qubits (2.1 GB in FP64): QFT + 2 noisy layers, noise after every gate."""
+    n = 14
+    qc = dmg.random_layer_circuit(n, 2, 5, barrier_after_gate=True, qft=True)
+    opts = dmg.noise_options(depolarisation=1e-3, decoherence=0.995, decay=0.998, rotation_sigma=1e-3)
+    opts['compute_densitymatrix'] = False
+    fused, b = run_gpu(qc.to_experiment(), opts)
+    a = fused['data']['coeffmatrix']
+    assert a[0] == 2.0 ** -n                         # trace preserved exactly
+    p = np.array(list(fused['data']['ensemble_probability'].values()))
+    assert abs(p.sum() - 1.0) < 1e-12 and p.min() > -1e-12
+    assert b.last_run_stats['passes'] < fused['number_of_clock_cycles']
+    single, _ = run_gpu(qc.to_experiment(), opts, precision='single')
+    np.testing.assert_allclose(single['data']['coeffmatrix'] * 2 ** n, a * 2 ** n, rtol=0, atol=2e-5)
+    unfused, _ = run_gpu(qc.to_experiment(), opts, fusion=False)
+    np.testing.assert_allclose(unfused['data']['coeffmatrix'] * 2 ** n, a * 2 ** n, rtol=0, atol=1e-12)
+
+
+def test_execute_and_provider_path():
+    """README example through BasicAer.get_backend('dm_simulator') and execute()."""
+    qc = dmg.QuantumCircuit(2)
+    qc.x(1)
+    qc.cx(0, 1)
+    backend = dmg.BasicAer.get_backend('dm_simulator')
+    result = dmg.execute(qc, backend).result()
+    dm = result['results'][0]['data']['densitymatrix']
+    expect = np.zeros((4, 4))
+    expect[1, 1] = 1
+    np.testing.assert_allclose(dm, expect, atol=1e-15)
+    assert result['backend_name'] == 'dm_simulator' and result['success']

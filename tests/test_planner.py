@@ -1,0 +1,164 @@
+"""Host-side checks of the transfer matrices and the fused-pass planner (no GPU).
+
+The passes the planner emits are replayed with numpy (each op applied to the
+whole state, which is what applying it to every tile does) and must equal
+the operations applied one by one in program order.
+"""
+import numpy as np
+import pytest
+
+from oracle import dm_oracle as O
+from qiskit_aakash_gb300 import program as P
+
+
+def apply_map1(st, n, q, m):
+    v = st.reshape(4 ** q, 4, 4 ** (n - q - 1))
+    return np.einsum('ij,ajb->aib', m, v).reshape(-1)
+
+
+def apply_pair(st, n, qa, qb, m16):
+    """16x16 map on (qa, qb), index 4*p_a + p_b."""
+    t = st.reshape([4] * n)
+    t = np.moveaxis(t, (qa, qb), (0, 1)).reshape(16, -1)
+    t = (m16 @ t).reshape([4, 4] + [4] * (n - 2))
+    return np.moveaxis(t, (0, 1), (qa, qb)).reshape(-1)
+
+
+def cx_matrix(coef, ideal):
+    """The CX map (control, target) as a dense 16x16 matrix, from the kernel's formulas."""
+    if ideal:
+        coef = (1.0, 0.0, 1.0, 0.0, 0.0)
+    c, s, c2, s2, cs = coef
+    M = np.eye(16)
+    rows = {
+        2: {2: s2, 14: c2, 3: -cs, 15: cs},
+        14: {2: c2, 14: s2, 3: cs, 15: -cs},
+        3: {3: s2, 15: c2, 2: cs, 14: -cs},
+        15: {3: c2, 15: s2, 2: -cs, 14: cs},
+        4: {5: c, 8: -s}, 5: {4: c, 9: -s},
+        6: {10: -s, 11: c}, 7: {10: -c, 11: -s},
+        8: {4: s, 9: c}, 9: {5: s, 8: c},
+        10: {6: s, 7: -c}, 11: {6: c, 7: s},
+    }
+    for r, entries in rows.items():
+        M[r, :] = 0
+        for col, v in entries.items():
+            M[r, col] = v
+    return M
+
+
+def apply_op(st, n, op):
+    if op.kind == 'map1':
+        return apply_map1(st, n, op.axes[0], op.data)
+    if op.kind == 'cx':
+        return apply_pair(st, n, op.axes[0], op.axes[1], cx_matrix(op.data, op.ideal))
+    if op.kind == 'diag2':
+        return apply_pair(st, n, op.axes[0], op.axes[1], np.diag(op.data))
+    if op.kind == 'map2':
+        return apply_pair(st, n, op.axes[0], op.axes[1], op.data)
+    raise ValueError(op.kind)
+
+
+def random_ops(rng, n, count):
+    ops = []
+    for _ in range(count):
+        r = rng.random()
+        if r < 0.6 or n < 2:
+            q = int(rng.integers(n))
+            ops.append(P.Op('map1', (q,), rng.normal(size=(4, 4))))
+        elif r < 0.85:
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            coef, ideal = P.cx_coefficients([rng.uniform(0.9, 1.0), rng.uniform(-0.2, 0.2)]
+                                            if rng.random() < 0.5 else [1.0, 0.0])
+            ops.append(P.Op('cx', (a, b), np.array(coef), ideal))
+        elif r < 0.95:
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            ops.append(P.Op('diag2', (a, b), rng.normal(size=16)))
+        else:
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            ops.append(P.Op('map2', (a, b), rng.normal(size=(16, 16)) / 4))
+    return ops
+
+
+def test_cx_formula_matches_oracle():
+    rng = np.random.default_rng(0)
+    n = 4
+    for tsp in ([1.0, 0.0], [0.97, 0.05], [0.9, -0.3]):
+        for (c, t) in ((0, 1), (1, 0), (0, 3), (3, 1), (2, 3)):
+            st = rng.normal(size=4 ** n)
+            ref = O.cx_apply(st.copy(), n, c, t, tsp)
+            coef, ideal = P.cx_coefficients(tsp)
+            got = apply_pair(st, n, c, t, cx_matrix(coef, ideal))
+            np.testing.assert_allclose(got, ref, atol=1e-13)
+
+
+def test_u_gate_ptm_matches_oracle_rotations():
+    rng = np.random.default_rng(1)
+    n = 3
+    err = {'rx': [0.98, 0.01], 'ry': [0.97, -0.02], 'rz': [0.99, 0.03]}
+    for _ in range(20):
+        st = rng.normal(size=4 ** n)
+        q = int(rng.integers(n))
+        params = rng.uniform(0, 2 * np.pi, 3)
+        ref = st.copy()
+        v = ref.reshape(4 ** q, 4, 4 ** (n - q - 1))
+        for name, ang in O.u_decomposition('u3', params):
+            O.rotate(v, name, ang, err[name])
+        got = apply_map1(st, n, q, P.u_gate_ptm('u3', params, err))
+        np.testing.assert_allclose(got, ref, atol=1e-13)
+
+
+def test_noise_ptm_matches_oracle():
+    rng = np.random.default_rng(2)
+    n = 3
+    st = rng.normal(size=4 ** n)
+    ref = O.memory_noise(st.copy(), n, 0.93, 0.3, 0.91)
+    got = st
+    for q in range(n):
+        got = apply_map1(got, n, q, P.noise_ptm(0.93, 0.3, 0.91))
+    np.testing.assert_allclose(got, ref, atol=1e-14)
+
+
+@pytest.mark.parametrize('n,kmax,low', [(1, 6, 2), (2, 6, 2), (3, 3, 1), (5, 4, 2), (6, 6, 2),
+                                        (7, 5, 2), (8, 6, 2), (8, 7, 3), (9, 4, 0)])
+def test_passes_equal_program_order(n, kmax, low):
+    rng = np.random.default_rng(100 + n * 10 + kmax)
+    for trial in range(6):
+        ops = random_ops(rng, n, int(rng.integers(1, 60)))
+        st0 = rng.normal(size=4 ** n)
+        ref = st0.copy()
+        for op in ops:
+            ref = apply_op(ref, n, op)
+        passes = P.plan_passes(ops, n, kmax, low)
+        got = st0.copy()
+        k = min(kmax, n)
+        lowset = set(range(n - 1, n - 1 - min(low, k), -1))
+        for p in passes:
+            assert len(p.axes) <= k
+            assert lowset.issubset(p.axes)
+            assert list(p.axes) == sorted(p.axes, reverse=True)
+            assert len(p.ops) <= 128
+            for op in p.ops:
+                assert set(op.axes).issubset(p.axes)
+                got = apply_op(got, n, op)
+        np.testing.assert_allclose(got, ref, rtol=1e-10, atol=1e-10 * np.abs(ref).max())
+
+
+def test_brick_layers_fuse_into_few_passes():
+    """n=16 random brick layers with noise after every level: passes per layer stay small."""
+    n = 16
+    rng = np.random.default_rng(3)
+    ops = []
+    noise = P.noise_ptm(0.995, 1.0, 0.998)
+    for L in range(6):
+        for q in range(n):
+            ops.append(P.Op('map1', (q,), rng.normal(size=(4, 4))))
+        for q in range(n):
+            ops.append(P.Op('map1', (q,), noise))
+        for a in range(L % 2, n - 1, 2):
+            coef, ideal = P.cx_coefficients([1.0, 0.0])
+            ops.append(P.Op('cx', (a, a + 1), np.array(coef), ideal))
+        for q in range(n):
+            ops.append(P.Op('map1', (q,), noise))
+    passes = P.plan_passes(ops, n, 7, 2)
+    assert len(passes) / 6 <= 4.0
