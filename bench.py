@@ -1,0 +1,421 @@
+"""Benchmark: gate-layers/s of the 16-qubit noisy random-layer workload on one GB300.
+
+Workload (one "step"): the seeded random brick-layer circuit at n = 16
+qubits (4**16 = 4.3e9 Pauli coefficients), 60 layers of U3 on every qubit
+then CX on the brick pairs, with the full noise model after every gate
+(depolarisation 1e-3 at measurement, decoherence 0.995, amplitude decay
+0.998, rotation error sigma 1e-3 rad; a barrier after each gate so that the
+reference's per-level memory noise follows every gate), ending with a
+Z-basis ensemble measurement of all qubits (65,536 probabilities).
+
+Reported (one JSON line on rank 0):
+* value       -- gate-layers/s of the fused FP32 form, device path with
+                 the circuit's program resident in HBM (CUDA events);
+* plain_fp64  -- the same for the FP64 form (reference parity form);
+* accuracy    -- FP32 vs FP64: max-abs error of the Pauli expectations
+                 2**n a_s and L1 error of the outcome probabilities;
+* e2e         -- the same metric through the public API
+                 (``backend.run(qobj).result()``): host planning, program
+                 upload, device work, results copied to host;
+* roofline    -- the fused pass kernel: algorithmic bytes per launch
+                 (read + write of every coefficient) / mean launch time;
+* cpu_baseline-- the CPU oracle (a numpy restatement of the reference's
+                 algorithm) timed on a bounded sample and scaled.
+
+``--impl reference`` times the reference's CPU algorithm (the oracle port)
+instead and prints its line.  Under torchrun every rank runs an independent
+replica (the path does not shard across GPUs); value sums the replicas.
+"""
+import argparse
+import copy
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import __graft_entry__  # noqa: E402
+
+METRIC = 'gate-layers/s at n=16 (random U3+CX brick layers, full noise after every gate): fused FP32 vs plain FP64'
+NOISE = dict(depolarisation=1e-3, decoherence=0.995, decay=0.998, rotation_sigma=1e-3)
+CPU_SAMPLE_N = 11
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=3)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', choices=['ours', 'reference'], default='ours')
+    ap.add_argument('--n', type=int, default=16)
+    ap.add_argument('--layers', type=int, default=60)
+    ap.add_argument('--seed', type=int, default=0)
+    ap.add_argument('--fp64-steps', type=int, default=1)
+    ap.add_argument('--e2e-steps', type=int, default=2)
+    ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline sample')
+    return ap.parse_args()
+
+
+def workload(pkg, n, layers, seed):
+    qc = pkg.random_layer_circuit(n, layers, seed, barrier_after_gate=True)
+    opts = pkg.noise_options(**NOISE)
+    opts['compute_densitymatrix'] = False
+    return qc, opts
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ('uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, uuid):
+        self.uuid = uuid
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '--query-gpu=' + self.FIELDS, '--format=csv,noheader,nounits',
+                                          '-lms', '200'], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(',')]
+            if len(parts) < 9:
+                continue
+            if self.uuid and self.uuid not in parts[0]:
+                continue
+            rows.append(parts)
+        if not rows:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['no nvidia-smi samples'], 'samples': 0}
+        sm = [float(r[1]) for r in rows if r[1].replace('.', '', 1).isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace('.', '', 1).isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == 'active'})
+        pw = [float(r[3]) for r in rows if r[3].replace('.', '', 1).isdigit()]
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': max(smax) if smax else None,
+                'reasons': reasons, 'samples': len(rows), 'power_w_max': max(pw) if pw else None}
+
+
+def gpu_uuid(torch):
+    try:
+        u = str(torch.cuda.get_device_properties(0).uuid)
+        return u.replace('GPU-', '')
+    except Exception:  # noqa: BLE001
+        return None
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    except Exception:  # noqa: BLE001
+        return 6800.0, 'fallback'
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of the pass kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, 'profiles', 'pass_kernel_fp32_n16.md')
+    try:
+        for line in open(path):
+            if line.startswith('traffic_bytes_per_launch:'):
+                return float(line.split(':', 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle, a numpy restatement of the reference's algorithm)
+# ---------------------------------------------------------------------------
+
+def cpu_sample(pkg, n_full, seed):
+    """Time one noisy random layer of the oracle at CPU_SAMPLE_N qubits; scale to n_full.
+
+    The reference's work per level is n full-state sweeps of 4**n
+    coefficients and a layer has n U3 levels plus the CX levels, so the
+    per-layer time scales by levels(n) * n * 4**n.
+    """
+    from oracle import dm_oracle
+    n = CPU_SAMPLE_N
+    qc = pkg.random_layer_circuit(n, 1, seed, barrier_after_gate=True, measure=False)
+    opts = pkg.noise_options(**NOISE)
+    opts['compute_densitymatrix'] = False
+    t0 = time.perf_counter()
+    res = dm_oracle.OracleDmSimulator(copy.deepcopy(opts)).run_experiment(qc.to_experiment())
+    dt = time.perf_counter() - t0
+    lv_small = res['number_of_clock_cycles']
+    # levels per layer at n_full: n U3 levels + CX levels (n//2 in even, (n-1)//2 in odd layers)
+    lv_full = n_full + ((n_full // 2) + ((n_full - 1) // 2)) / 2.0
+    scale = (lv_full * n_full * 4.0 ** n_full) / (lv_small * n * 4.0 ** n)
+    sec_per_layer_full = dt * scale
+    return {'value': 1.0 / sec_per_layer_full, 'unit': 'gate-layers/s', 'cores': 1, 'kind': 'port',
+            'sample': ('1 noisy random layer at n=%d (%d levels, %.2f s, numpy FP64, 1 thread), scaled to n=%d '
+                       'by levels*n*4^n (x%.0f)' % (n, lv_small, dt, n_full, scale)),
+            'sample_seconds': dt}
+
+
+# ---------------------------------------------------------------------------
+# the GPU arm
+# ---------------------------------------------------------------------------
+
+def dist_setup(args):
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return world, rank, local
+
+
+def barrier(torch, world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(torch, world, x):
+    if world <= 1:
+        return x
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device='cuda')
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def time_replays(torch, state, steps):
+    stream = torch.cuda.current_stream()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(steps):
+        state.replay()
+    end.record(stream)
+    torch.cuda.synchronize()
+    return start.elapsed_time(end) / steps
+
+
+def pass_kernel_profile(torch, state):
+    """Mean duration of the pass-kernel launches of one replay (events on the launching stream)."""
+    stream = torch.cuda.current_stream()
+    marks = []
+
+    def on_call(name, before):
+        if name == 'dm_apply_pass':
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record(stream)
+            marks.append(ev)
+
+    torch.cuda.synchronize()
+    state.replay(on_call)
+    torch.cuda.synchronize()
+    durs = [marks[i].elapsed_time(marks[i + 1]) for i in range(0, len(marks) - 1, 2)]
+    return durs
+
+
+def device_max_abs_diff(torch, a32, b64, chunk=1 << 28):
+    """max |a - b| over two device vectors (FP32 vs FP64), in chunks (measurement only)."""
+    m = 0.0
+    for s in range(0, a32.numel(), chunk):
+        d = (a32[s:s + chunk].double() - b64[s:s + chunk]).abs().max().item()
+        m = max(m, d)
+    return m
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup(args)
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    pkg = __graft_entry__.build()
+    from qiskit_aakash_gb300 import _native as N
+    from qiskit_aakash_gb300.dm_simulator import DmSimulatorGPU
+    n, layers = args.n, args.layers
+    seed = args.seed + rank
+    qc, opts = workload(pkg, n, layers, seed)
+
+    def backend_for(precision):
+        DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
+        b = DmSimulatorGPU()
+        o = copy.deepcopy(opts)
+        o['precision'] = precision
+        o['coefficients_to_host'] = False      # compared on the device below
+        b._set_options(backend_options=o)
+        return b
+
+    # --- fused FP32: record once, then time replays ---------------------------
+    b32 = backend_for('single')
+    r32 = b32.record_experiment(qc.to_experiment())
+    st32 = b32.recorded_state
+    stats32 = dict(b32.last_run_stats)
+    for _ in range(args.warmup):
+        st32.replay()
+    uuid = gpu_uuid(torch)
+    l0 = N.lib().dm_kernel_launch_count()
+    barrier(torch, world)
+    with ClockSampler(uuid) as clocks:
+        ms32 = time_replays(torch, st32, args.steps)
+    launches = (N.lib().dm_kernel_launch_count() - l0)
+    barrier(torch, world)
+    ms32 = allmax(torch, world, ms32)
+    durs = pass_kernel_profile(torch, st32)     # a full replay: leaves the final FP32 state
+    prob32 = np.array(list(r32['data']['ensemble_probability'].values()))
+
+    # --- plain FP64 (the parity form) ---------------------------------------
+    b64 = backend_for('double')
+    r64 = b64.record_experiment(qc.to_experiment())
+    st64 = b64.recorded_state
+    stats64 = dict(b64.last_run_stats)
+    st64.replay()
+    ms64 = time_replays(torch, st64, args.fp64_steps)
+    durs64 = pass_kernel_profile(torch, st64)
+    prob64 = np.array(list(r64['data']['ensemble_probability'].values()))
+    max_abs = device_max_abs_diff(torch, st32.state, st64.state) * 2.0 ** n
+    prob_l1 = float(np.abs(prob32 - prob64).sum())
+    del st64, b64, r64, st32, b32, r32
+    torch.cuda.empty_cache()
+
+    # --- e2e through the public API (FP32 form) ------------------------------
+    backend = pkg.BasicAer.get_backend('dm_simulator')
+    e2e_opts = copy.deepcopy(opts)
+    e2e_opts['precision'] = 'single'
+    DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
+    pkg.execute(qc, backend, **copy.deepcopy(e2e_opts)).result()          # warm (pinned buffers, planning)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
+        res = pkg.execute(qc, backend, **copy.deepcopy(e2e_opts)).result()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_s = allmax(torch, world, e2e_s)
+    st = backend.last_run_stats
+    del res
+
+    if rank != 0:
+        return None
+    hbm, peak_kind = measured_peaks()
+    N4 = 4.0 ** n
+    mean_pass_ms = float(np.mean(durs)) if durs else float('nan')
+    achieved = 2 * N4 * 4 / (mean_pass_ms / 1e3) / 1e9
+    mean_pass64 = float(np.mean(durs64)) if durs64 else float('nan')
+    achieved64 = 2 * N4 * 8 / (mean_pass64 / 1e3) / 1e9
+    traffic = profiled_traffic()
+    line = {
+        'metric': METRIC,
+        'value': world * layers / (ms32 / 1e3),
+        'unit': 'gate-layers/s',
+        'n_gpus': world,
+        'steps': args.steps,
+        'warmup': args.warmup,
+        'ms_per_step': ms32,
+        'higher_is_better': True,
+        'scaling': 'weak',
+        'vs_baseline': None,
+        'dtype': 'f32',
+        'data': 'synthetic: seeded random circuits (numpy default_rng), no dataset',
+        'config': {'workload': 'random brick layers n=%d, %d layers, noise after every gate, Ensemble Z' % (n, layers),
+                   'n_qubits': n, 'layers': layers, 'seed': args.seed, 'noise': NOISE,
+                   'levels': stats32['levels'], 'fused_passes': stats32['passes'],
+                   'passes_per_layer': stats32['passes'] / layers,
+                   'state_bytes_fp32': int(N4 * 4),
+                   'l2': 'inputs larger than L2: the %.1f GB state >> 129 MB L2' % (N4 * 4 / 1e9),
+                   'parallelism': 'replicas' if world > 1 else 'single GPU'},
+        'plain_fp64': {'value': world * layers / (ms64 / 1e3), 'unit': 'gate-layers/s', 'ms_per_step': ms64,
+                       'fused_passes': stats64['passes'], 'mean_pass_ms': mean_pass64,
+                       'pass_achieved_gbs': achieved64, 'pass_frac_of_hbm': achieved64 / hbm},
+        'fp32_over_fp64': ms64 / ms32,
+        'accuracy': {'max_abs_coeff_err': max_abs, 'prob_l1_err': prob_l1,
+                     'against': 'FP64 GPU plain form (itself parity-checked against the reference at n<=14)',
+                     'coeff_scale': 'Pauli expectations 2^n * a_s'},
+        'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s', 'frac': achieved / hbm,
+                     'traffic': traffic, 'kernel': 'pass_kernel<float>', 'launches_per_step': len(durs),
+                     'mean_launch_ms': mean_pass_ms,
+                     'algorithmic_bytes_per_launch': 2 * N4 * 4, 'peak_kind': peak_kind},
+        'e2e': {'value': world * layers / e2e_s, 'unit': 'gate-layers/s', 'seconds_per_step': e2e_s,
+                'h2d_bytes_per_step': int(st['h2d_bytes']), 'd2h_bytes_per_step': int(st['d2h_bytes']),
+                'api': "BasicAer.get_backend('dm_simulator') + execute(...).result()"},
+        'gpu_launches': int(launches),
+        'clocks': clocks.summary(),
+    }
+    if not args.no_cpu:
+        line['cpu_baseline'] = cpu_sample(pkg, n, args.seed)
+    return line
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return None
+    pkg = __graft_entry__.load_package()
+    samples = []
+    for i in range(args.warmup + args.steps):
+        s = cpu_sample(pkg, args.n, args.seed + i)
+        if i >= args.warmup:
+            samples.append(s)
+    value = float(np.mean([s['value'] for s in samples]))
+    cb = dict(samples[-1])
+    cb['value'] = value
+    return {
+        'impl': 'reference',
+        'metric': METRIC,
+        'value': value,
+        'unit': 'gate-layers/s',
+        'n_gpus': world,
+        'steps': args.steps,
+        'warmup': args.warmup,
+        'ms_per_step': float(np.mean([s['sample_seconds'] for s in samples])) * 1e3,
+        'higher_is_better': True,
+        'scaling': 'weak',
+        'vs_baseline': None,
+        'dtype': 'f64',
+        'data': 'synthetic: seeded random circuits (numpy default_rng), no dataset',
+        'config': {'workload': 'random brick layers n=%d, %d layers, noise after every gate, Ensemble Z'
+                               % (args.n, args.layers), 'n_qubits': args.n, 'layers': args.layers},
+        'cpu_baseline': cb,
+        'e2e': {'value': value, 'unit': 'gate-layers/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }
+
+
+def main():
+    args = parse()
+    line = run_reference(args) if args.impl == 'reference' else run_ours(args)
+    if line is not None:
+        print(json.dumps(line))
+
+
+if __name__ == '__main__':
+    main()

@@ -27,6 +27,12 @@ Differences (the reference fails on these inputs):
 * plain-string measurement parameters are treated like sympy Symbols;
 * the initial-state checks raise ``InitialStateError`` (a BasicAerError and
   an AttributeError) with a readable message.
+GB300 options (absent from the reference): ``precision`` ('double', the
+default and the parity form, or 'single'), ``fusion`` (fused tile passes,
+default True), ``tile_axes`` (resident axes per tile) and
+``coefficients_to_host`` (default True; False leaves ``coeffmatrix`` /
+``densitymatrix`` out of the result, for callers that only need the
+measurement data of a large register).
 """
 import copy
 import logging
@@ -216,7 +222,24 @@ class DmSimulatorGPU(_Base):
         self._precision = 'double'
         self._fusion = True
         self._tile_axes = None
+        self._coefficients_to_host = True
         self.last_run_stats = {}
+        self._record_next = False
+        self.recorded_state = None
+
+    def record_experiment(self, experiment):
+        """Run one experiment and keep its device state with a replayable call tape.
+
+        ``self.recorded_state.replay()`` then re-issues the experiment's device
+        work (state set-up, fused passes, measurement read-outs into the same
+        device buffers) with no host-side planning or transfers; used to time
+        the device path with its inputs resident.
+        """
+        self._record_next = True
+        try:
+            return self.run_experiment(experiment)
+        finally:
+            self._record_next = False
 
     # ------------------------------------------------------------------ options
     def _set_options(self, qobj_config=None, backend_options=None):
@@ -291,6 +314,8 @@ class DmSimulatorGPU(_Base):
             self._fusion = bool(backend_options['fusion'])
         if 'tile_axes' in backend_options:
             self._tile_axes = int(backend_options['tile_axes'])
+        if 'coefficients_to_host' in backend_options:
+            self._coefficients_to_host = bool(backend_options['coefficients_to_host'])
 
     def _initialize_errors(self):
         """dm_simulator.py:273-282."""
@@ -522,6 +547,8 @@ class DmSimulatorGPU(_Base):
         if any(op.name == 'bfunc' for op in experiment.instructions):
             raise BasicAerError('dm_simulator does not support conditional (bfunc) operations')
         self._dev = DeviceState(n, precision=self._precision, fusion=self._fusion, tile_axes=self._tile_axes)
+        if self._record_next:
+            self._dev.record()
         launches0 = N.lib().dm_kernel_launch_count()
         self._initialize_densitymatrix()
         self._validate_initial_densitymatrix()
@@ -637,7 +664,7 @@ class DmSimulatorGPU(_Base):
                     raise BasicAerError(err_msg.format(self.name(), name))
             self._add_decoherence_and_amp_decay(clock, f=mem['decoherence'], p=mem['thermalization'],
                                                 g=mem['amplitude_decay'])
-        if self.SHOW_FINAL_STATE:
+        if self.SHOW_FINAL_STATE and self._coefficients_to_host:
             if self._get_den_mat:
                 data['coeffmatrix'], data['densitymatrix'] = self._get_densitymatrix()
             else:
@@ -649,6 +676,9 @@ class DmSimulatorGPU(_Base):
         self.last_run_stats = {'passes': self._dev.passes_run, 'levels': levels,
                                'kernel_launches': N.lib().dm_kernel_launch_count() - launches0,
                                'h2d_bytes': self._dev.h2d_bytes, 'd2h_bytes': self._dev.d2h_bytes}
+        if self._record_next:
+            self.recorded_state = self._dev
+            self._record_next = False
         self._dev = None
         return {'name': experiment.header.name,
                 'number_of_clock_cycles': levels,

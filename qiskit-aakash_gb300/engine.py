@@ -54,6 +54,33 @@ class DeviceState:
         self.passes_run = 0
         self.h2d_bytes = 0
         self.d2h_bytes = 0
+        self.tape = None          # list of recorded C-ABI calls (see record())
+        self._keep_alive = []
+
+    # -- recording -----------------------------------------------------------
+    def record(self):
+        """Start recording every C-ABI call (with its argument buffers).
+
+        The calls issued from now on still run; ``replay()`` issues the same
+        device work again on the same buffers, with no host planning and no
+        host<->device copies.  A circuit's device work does not depend on
+        measurement outcomes, so the replay is the whole experiment.
+        """
+        self.tape = []
+
+    def replay(self, on_call=None):
+        for name, args in self.tape:
+            if on_call is not None:
+                on_call(name, True)
+            N.call(name, *args)
+            if on_call is not None:
+                on_call(name, False)
+
+    def _call(self, name, *args, keep=()):
+        if self.tape is not None:
+            self.tape.append((name, args))
+            self._keep_alive.append((args, keep))
+        N.call(name, *args)
 
     # -- plumbing ------------------------------------------------------------
     @property
@@ -72,8 +99,8 @@ class DeviceState:
     def init_product(self, vectors, scale):
         v = np.ascontiguousarray(np.asarray(vectors, dtype=np.float64).reshape(self.n, 4))
         self.pending = []
-        N.call('dm_init_product', self.ptr, self.n, self.dtype,
-               v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), float(scale), self.stream)
+        self._call('dm_init_product', self.ptr, self.n, self.dtype,
+                   v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), float(scale), self.stream, keep=(v,))
 
     def load(self, coeffs):
         a = np.ascontiguousarray(np.asarray(coeffs, dtype=np.float64).reshape(-1))
@@ -118,8 +145,8 @@ class DeviceState:
         self.h2d_bytes += host.nbytes
         mp = ctypes.c_void_p(dev.data_ptr())
         for d in descs:
-            N.call('dm_apply_pass', self.ptr, self.n, self.dtype, ctypes.byref(d), mp,
-                   ctypes.c_size_t(host.size), self.stream)
+            self._call('dm_apply_pass', self.ptr, self.n, self.dtype, ctypes.byref(d), mp,
+                       ctypes.c_size_t(host.size), self.stream, keep=(d, dev))
         self.passes_run += len(descs)
         self._keep = (h, dev)    # keep both alive until the next flush
 
@@ -127,12 +154,10 @@ class DeviceState:
         for op in ops:
             if op.kind == 'map1':
                 m = np.ascontiguousarray(op.data, dtype=np.float64).reshape(16)
-                N.call('dm_apply_map1', self.ptr, self.n, self.dtype, op.axes[0],
-                       m.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), self.stream)
-            elif op.kind == 'cx':
-                # dm_apply_cx recomputes the coefficients from (<cos a>, mean a)
-                self._run_passes(plan_passes([op], self.n, self.kmax, self.low))
+                self._call('dm_apply_map1', self.ptr, self.n, self.dtype, op.axes[0],
+                           m.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), self.stream, keep=(m,))
             else:
+                # pair operations: a pass holding only this operation
                 self._run_passes(plan_passes([op], self.n, self.kmax, self.low))
 
     # -- read-outs (each flushes first) --------------------------------------
@@ -143,8 +168,9 @@ class DeviceState:
         m = sum(1 for x in mode if x)
         out = torch.empty(2 ** m, dtype=torch.float64, device=self.device)
         md = (ctypes.c_int * self.n)(*[int(x) for x in mode])
-        N.call('dm_axis_probs', self.ptr, self.n, self.dtype, md, float(err),
-               ctypes.c_void_p(out.data_ptr()), self.stream)
+        self._call('dm_axis_probs', self.ptr, self.n, self.dtype, md, float(err),
+                   ctypes.c_void_p(out.data_ptr()), self.stream, keep=(out,))
+        self.last_readout = out
         return self._to_host(out)
 
     def nbasis_probs(self, nvec, err):
@@ -155,8 +181,10 @@ class DeviceState:
         scratch = torch.empty(max(nbytes, 8), dtype=torch.uint8, device=self.device)
         out = torch.empty(2 ** self.n, dtype=torch.float64, device=self.device)
         v = N.f64_array(nvec)
-        N.call('dm_nbasis_probs', self.ptr, self.n, self.dtype, v, float(err),
-               ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(scratch.data_ptr()), self.stream)
+        self._call('dm_nbasis_probs', self.ptr, self.n, self.dtype, v, float(err),
+                   ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(scratch.data_ptr()), self.stream,
+                   keep=(out, scratch))
+        self.last_readout = out
         return self._to_host(out)
 
     def gather(self, indices):
@@ -168,8 +196,8 @@ class DeviceState:
             chunk = idx[s:s + 64]
             o = torch.empty(len(chunk), dtype=torch.float64, device=self.device)
             arr = (ctypes.c_int64 * len(chunk))(*chunk)
-            N.call('dm_gather', self.ptr, self.n, self.dtype, arr, len(chunk),
-                   ctypes.c_void_p(o.data_ptr()), self.stream)
+            self._call('dm_gather', self.ptr, self.n, self.dtype, arr, len(chunk),
+                       ctypes.c_void_p(o.data_ptr()), self.stream, keep=(o,))
             out.append(self._to_host(o))
         return np.concatenate(out)
 

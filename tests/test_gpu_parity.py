@@ -117,6 +117,10 @@ def test_fourteen_qubit_properties():
 
 def test_execute_and_provider_path():
     """README example through BasicAer.get_backend('dm_simulator') and execute()."""
+    from qiskit_aakash_gb300.dm_simulator import DmSimulatorGPU
+    # rotation_error options update the class-level defaults (as in the
+    # reference, dm_simulator.py:182, :212-213): start from the true defaults.
+    DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
     qc = dmg.QuantumCircuit(2)
     qc.x(1)
     qc.cx(0, 1)
@@ -127,3 +131,16 @@ def test_execute_and_provider_path():
     expect[1, 1] = 1
     np.testing.assert_allclose(dm, expect, atol=1e-15)
     assert result['backend_name'] == 'dm_simulator' and result['success']
+
+
+def test_rotation_error_defaults_leak_like_the_reference():
+    """A run with rotation_error changes the defaults seen by later runs (dm_simulator.py:212-213)."""
+    from qiskit_aakash_gb300.dm_simulator import DmSimulatorGPU
+    DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
+    qc = dmg.QuantumCircuit(1)
+    qc.x(0)
+    backend = dmg.BasicAer.get_backend('dm_simulator')
+    dmg.execute(qc, backend, rotation_error={'ry': [0.5, 0.0]}).result()
+    r = dmg.execute(qc, backend).result()['results'][0]['data']['coeffmatrix']
+    assert abs(r[3] - (-0.25)) < 1e-12       # Z coefficient: ry contracted by 0.5
+    DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
