@@ -134,6 +134,24 @@ size_t dm_nbasis_probs_scratch_bytes(int n);
 int dm_nbasis_probs(const void *state_dev, int n, int dtype, const double *nvec3, double err,
                     double *out_dev, void *scratch_dev, void *stream);
 
+/* dm_nbasis_probs for callers that cannot allocate device memory.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc -- code whose device memory is already handed to another
+ * allocator (a framework's caching pool) where raw allocations fail or are
+ * not allowed, and code on a latency-critical path where cudaMalloc/cudaFree
+ * would synchronise the device.  The caller still passes the state and the
+ * 2**n output; the scratch is a file-scope device array of 196,608 doubles
+ * (1.5 MiB), which every GPU that loads this library holds until the process
+ * exits, enough for n <= 10.  Larger n returns DM_ERR_RANGE without touching
+ * the GPU.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current), so make that first call
+ * before any stream capture.  Every call shares the one array: calls that
+ * overlap on the GPU (other streams, other host threads) race on it.  Each
+ * call writes every scratch element it reads, so nothing left from a previous
+ * call reaches a result.  Allocates nothing (no cudaMalloc / cudaFree). */
+int dm_nbasis_probs_noalloc(const void *state_dev, int n, int dtype, const double *nvec3, double err,
+                            double *out_dev, void *stream);
+
 /* Gather count coefficients a[idx[i]] (FP64) into out_dev.  Used for the
  * Pauli-string expectation (dm_simulator.py:569-570), the Bell reduced matrix
  * and probabilities (:744-760) and the trace check (:363). count <= 64. */

@@ -108,6 +108,7 @@ SIGNATURES = {
     'dm_axis_probs': (_i, [_vp, _i, _i, _ip, _d, _vp, _vp]),
     'dm_nbasis_probs_scratch_bytes': (_sz, [_i]),
     'dm_nbasis_probs': (_i, [_vp, _i, _i, _dp, _d, _vp, _vp, _vp]),
+    'dm_nbasis_probs_noalloc': (_i, [_vp, _i, _i, _dp, _d, _vp, _vp]),
     'dm_gather': (_i, [_vp, _i, _i, _i64p, _i, _vp, _vp]),
     'dm_chop_copy': (_i, [_vp, _i, _i, _d, _vp, _vp]),
     'dm_pauli_to_matrix_scratch_bytes': (_sz, [_i]),

@@ -11,6 +11,8 @@
 // err**popcount and apply an in-place Walsh-Hadamard transform.
 #include <math.h>
 
+#include <mutex>
+
 #include "dm_common.cuh"
 
 namespace dmg {
@@ -199,6 +201,95 @@ extern "C" int dm_nbasis_probs(const void *state_dev, int n, int dtype, const do
     const size_t first = size_t(pow4(n - t)) << t;
     double *bufA = static_cast<double *>(scratch_dev);
     double *bufB = bufA ? bufA + first : nullptr;
+    double *dst = (t == n) ? out_dev : bufA;
+    const int64_t outer = pow4(n - t);
+    if (dtype == DM_F64)
+        contract_low<double><<<grid_for(outer, 256), 256, 0, s>>>(static_cast<const double *>(state_dev), t, outer,
+                                                                  R, dst);
+    else
+        contract_low<float><<<grid_for(outer, 256), 256, 0, s>>>(static_cast<const float *>(state_dev), t, outer, R,
+                                                                 dst);
+    count_launch();
+    int rc = launch_status();
+    if (rc || t == n) return rc;
+    const double *src = bufA;
+    for (int q = n - t - 1; q >= 0; --q) {
+        const int64_t o = pow4(q), inner = int64_t(1) << (n - 1 - q);
+        double *d = (q == 0) ? out_dev : (src == bufA ? bufB : bufA);
+        contract_axis<<<grid_for(o * inner, 256), 256, 0, s>>>(src, o, inner, R, d);
+        count_launch();
+        if ((rc = launch_status())) return rc;
+        src = d;
+    }
+    return DM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// dm_nbasis_probs_noalloc: the basis-N probabilities with the scratch held in
+// a file-scope device array instead of a caller buffer.
+// ---------------------------------------------------------------------------
+
+namespace dmg {
+
+constexpr int kNoallocMaxQubits = 10;
+// Contraction buffers for n <= kNoallocMaxQubits: 4**7 * 2**3 doubles after
+// the first (three-axis) step plus half that for the ping-pong partner.
+constexpr size_t kNoallocScratchDoubles = (size_t(1) << 14) * 8 * 3 / 2;   // 196,608 doubles = 1.5 MiB
+
+// Every GPU that loads this library holds this array until the process exits.
+static __device__ __align__(256) double g_nbasis_scratch[kNoallocScratchDoubles];
+
+constexpr int kMaxDevices = 64;
+
+// Device address of g_nbasis_scratch, resolved once per device with that
+// device current.  Host code must not pass the symbol itself to a kernel:
+// on the host it names a shadow variable, not device memory.
+static int noalloc_scratch(double **out) {
+    static std::mutex mu;
+    static double *addr[kMaxDevices] = {nullptr};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return DM_ERR_CUDA;
+    }
+    if (dev < 0 || dev >= kMaxDevices) return DM_ERR_RANGE;
+    std::lock_guard<std::mutex> lock(mu);
+    if (addr[dev] == nullptr) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_nbasis_scratch) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return DM_ERR_CUDA;
+        }
+        addr[dev] = static_cast<double *>(p);
+    }
+    *out = addr[dev];
+    return DM_OK;
+}
+
+}  // namespace dmg
+
+extern "C" int dm_nbasis_probs_noalloc(const void *state_dev, int n, int dtype, const double *nvec3, double err,
+                                       double *out_dev, void *stream) {
+    DM_CHECK_ARG(state_dev && nvec3 && out_dev && valid_n(n) && valid_dtype(dtype));
+    if (n > kNoallocMaxQubits) return DM_ERR_RANGE;
+    const int t = low_axes(n);
+    double *scratch = nullptr;
+    if (t < n) {
+        int rc = noalloc_scratch(&scratch);
+        if (rc) return rc;
+    }
+    NRows R;
+    R.w[0][0] = R.w[1][0] = 1.0;
+    for (int c = 0; c < 3; ++c) {
+        R.w[0][c + 1] = err * nvec3[c];
+        R.w[1][c + 1] = -err * nvec3[c];
+    }
+    cudaStream_t s = as_stream(stream);
+    // Every buffer element read below is written earlier in the same call,
+    // so the array's contents from a previous call never leak into a result.
+    const size_t first = size_t(pow4(n - t)) << t;
+    double *bufA = scratch;
+    double *bufB = scratch ? scratch + first : nullptr;
     double *dst = (t == n) ? out_dev : bufA;
     const int64_t outer = pow4(n - t);
     if (dtype == DM_F64)
