@@ -45,6 +45,7 @@ enum dm_status {
 #define DM_MAX_QUBITS 17            /* 4**17 FP64 = 137 GB: the largest state one GB300 holds */
 #define DM_MAX_TILE_AXES 7          /* resident axes of one tile (4**7 coefficients) */
 #define DM_MAX_PASS_OPS 128         /* operations applied to one tile in one pass */
+#define DM_MAX_ROUNDS 48            /* register rounds of one pass */
 
 /* Operation kinds of a fused pass (local axes index the pass's resident axes). */
 enum dm_op_kind {
@@ -72,8 +73,21 @@ typedef struct dm_pass {
     int32_t axes[DM_MAX_TILE_AXES];     /* qubit of local axis r; strictly decreasing (local axis 0
                                            has the smallest stride) */
     int32_t nops;
+    /* Register rounds.  nrounds = 0: the ops are applied one at a time to the
+     * shared-memory tile.  nrounds > 0: the ops are grouped into rounds; in
+     * round r every thread holds groups of 4**R coefficients spanning the
+     * round's R local axes round_axes[r][0..R-1] (ascending; R = 3 for FP32,
+     * 2 for FP64) in registers and applies ops [round_end[r-1], round_end[r])
+     * (each acting only on the round's axes) before writing them back. */
+    int32_t nrounds;
+    int8_t round_axes[DM_MAX_ROUNDS][4];
+    int16_t round_end[DM_MAX_ROUNDS];
     dm_op ops[DM_MAX_PASS_OPS];
 } dm_pass;
+
+/* Round width (axes held in registers per round) for a dtype. */
+#define DM_ROUND_AXES_F32 3
+#define DM_ROUND_AXES_F64 2
 
 /* ---------------------------------------------------------------- state set-up */
 

@@ -28,6 +28,8 @@ DM_F64, DM_F32 = 0, 1
 DM_MAX_QUBITS = 17
 DM_MAX_TILE_AXES = 7
 DM_MAX_PASS_OPS = 128
+DM_MAX_ROUNDS = 48
+DM_ROUND_AXES = {0: 2, 1: 3}     # dtype -> axes per register round
 DM_OP_MAP1, DM_OP_MAP2, DM_OP_DIAG2, DM_OP_CX = 1, 2, 3, 4
 DM_MAP1_ROW0_IDENTITY = 1
 DM_CX_IDEAL = 1
@@ -87,7 +89,10 @@ class DmOp(ctypes.Structure):
 
 class DmPass(ctypes.Structure):
     _fields_ = [('k', ctypes.c_int32), ('axes', ctypes.c_int32 * DM_MAX_TILE_AXES),
-                ('nops', ctypes.c_int32), ('ops', DmOp * DM_MAX_PASS_OPS)]
+                ('nops', ctypes.c_int32), ('nrounds', ctypes.c_int32),
+                ('round_axes', (ctypes.c_int8 * 4) * DM_MAX_ROUNDS),
+                ('round_end', ctypes.c_int16 * DM_MAX_ROUNDS),
+                ('ops', DmOp * DM_MAX_PASS_OPS)]
 
 
 _vp = ctypes.c_void_p

@@ -252,6 +252,242 @@ __global__ void __launch_bounds__(256) pass_kernel(T *__restrict__ st, const __g
 }
 
 // ---------------------------------------------------------------------------
+// fused pass with register rounds
+//
+// The pass's operations are grouped (on the host) into rounds; a round names
+// R local axes (R = 3 for FP32: 64 coefficients, R = 2 for FP64: 16) and the
+// consecutive operations that act only on them.  In a round every thread
+// loads groups of 4**R coefficients spanning those axes from the shared tile
+// into registers, applies all of the round's operations there and stores
+// the group back: one shared-memory round trip per round instead of one per
+// operation.
+// ---------------------------------------------------------------------------
+
+struct PassRounds {
+    int n, k, low, m, nops, nrounds;
+    int64_t res_stride[DM_MAX_TILE_AXES];
+    int64_t nonres_stride[DM_MAX_QUBITS];
+    int8_t rax[DM_MAX_ROUNDS][4];
+    int16_t rend[DM_MAX_ROUNDS];
+    dm_op ops[DM_MAX_PASS_OPS];
+};
+
+// Shared-memory position of tile element e: the low five bits are XORed
+// with the next five, which spreads the groups of a warp over the 32 banks.
+// swz is XOR-linear on elements with disjoint bits, so the position of
+// (group base | round offset) is swz(base) ^ swz(offset).
+__device__ __forceinline__ int swz(int e) { return e ^ ((e >> 5) & 31); }
+
+__device__ __forceinline__ int64_t rounds_offset(const PassRounds &p, int e) {
+    int64_t off = e & ((1 << (2 * p.low)) - 1);
+    for (int r = p.low; r < p.k; ++r) off += int64_t((e >> (2 * r)) & 3) * p.res_stride[r];
+    return off;
+}
+
+// Register index j of a group holds round digits (j & 3, (j >> 2) & 3, j >> 4).
+template <typename T, int R, int D>
+__device__ __forceinline__ void reg_map1(T (&v)[1 << (2 * R)], const T *__restrict__ mg, bool row0_id) {
+    T m[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) m[i] = mg[i];
+    constexpr int S = 1 << (2 * D);
+#pragma unroll
+    for (int o = 0; o < (1 << (2 * (R - 1))); ++o) {
+        const int j0 = ((o >> (2 * D)) << (2 * D + 2)) | (o & (S - 1));
+        map4(m, row0_id, v[j0], v[j0 + S], v[j0 + 2 * S], v[j0 + 3 * S]);
+    }
+}
+
+__host__ __device__ constexpr int ins0(int g, int pos) {
+    return ((g >> (2 * pos)) << (2 * pos + 2)) | (g & ((1 << (2 * pos)) - 1));
+}
+
+// Register index of the (0, 0) entry of pair group o for round digits (DA, DB).
+template <int DA, int DB>
+__device__ __forceinline__ constexpr int pair_base(int o) {
+    return ins0(ins0(o, DA < DB ? DA : DB), DA < DB ? DB : DA);
+}
+
+// CX on the registers of one pair group, in place.  Entry (pa, pb) of the
+// group lives at v[j0 + pa*SA + pb*SB]; (pa, pb) = (control, target) Paulis.
+template <typename T, int R, int J0, int SA, int SB>
+__device__ __forceinline__ void reg_cx_group(T (&v)[1 << (2 * R)], const CxCoef<T> &k, bool ideal) {
+#define DM_V(pa, pb) v[J0 + (pa) * SA + (pb) * SB]
+    if (ideal) {
+        T t;
+        t = DM_V(0, 2); DM_V(0, 2) = DM_V(3, 2); DM_V(3, 2) = t;
+        t = DM_V(0, 3); DM_V(0, 3) = DM_V(3, 3); DM_V(3, 3) = t;
+        t = DM_V(1, 0); DM_V(1, 0) = DM_V(1, 1); DM_V(1, 1) = t;
+        t = DM_V(2, 0); DM_V(2, 0) = DM_V(2, 1); DM_V(2, 1) = t;
+        const T xy = DM_V(1, 2), xz = DM_V(1, 3), yy = DM_V(2, 2), yz = DM_V(2, 3);
+        DM_V(1, 2) = yz;
+        DM_V(1, 3) = -yy;
+        DM_V(2, 2) = -xz;
+        DM_V(2, 3) = xy;
+    } else {
+        const T c = k.c, s = k.s, c2 = k.c2, s2 = k.s2, cs = k.cs;
+        const T i2 = DM_V(0, 2), i3 = DM_V(0, 3), z2 = DM_V(3, 2), z3 = DM_V(3, 3);
+        const T x0 = DM_V(1, 0), x1 = DM_V(1, 1), x2 = DM_V(1, 2), x3 = DM_V(1, 3);
+        const T y0 = DM_V(2, 0), y1 = DM_V(2, 1), y2 = DM_V(2, 2), y3 = DM_V(2, 3);
+        const T d3 = i3 - z3, d2 = i2 - z2;
+        DM_V(0, 2) = fma(s2, i2, fma(c2, z2, -cs * d3));
+        DM_V(3, 2) = fma(c2, i2, fma(s2, z2, cs * d3));
+        DM_V(0, 3) = fma(s2, i3, fma(c2, z3, cs * d2));
+        DM_V(3, 3) = fma(c2, i3, fma(s2, z3, -cs * d2));
+        DM_V(1, 0) = fma(c, x1, -s * y0);
+        DM_V(1, 1) = fma(c, x0, -s * y1);
+        DM_V(1, 2) = fma(-s, y2, c * y3);
+        DM_V(1, 3) = fma(-c, y2, -s * y3);
+        DM_V(2, 0) = fma(s, x0, c * y1);
+        DM_V(2, 1) = fma(s, x1, c * y0);
+        DM_V(2, 2) = fma(s, x2, -c * x3);
+        DM_V(2, 3) = fma(c, x2, s * x3);
+    }
+#undef DM_V
+}
+
+template <typename T, int R, int DA, int DB, int O>
+__device__ __forceinline__ void reg_diag_row(T (&v)[1 << (2 * R)], int pa, const T (&d)[4]) {
+    constexpr int SA = 1 << (2 * DA), SB = 1 << (2 * DB);
+    constexpr int J0 = pair_base<DA, DB>(O);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        if (q == pa) {
+#pragma unroll
+            for (int pb = 0; pb < 4; ++pb) v[J0 + q * SA + pb * SB] *= d[pb];
+        }
+}
+
+template <typename T, int R, int DA, int DB>
+__device__ __forceinline__ void reg_pair(T (&v)[1 << (2 * R)], const dm_op &op, const T *__restrict__ mg) {
+    constexpr int SA = 1 << (2 * DA), SB = 1 << (2 * DB);
+    if (op.kind == DM_OP_CX) {
+        const bool ideal = (op.flags & DM_CX_IDEAL) != 0;
+        CxCoef<T> cx{T(1), T(0), T(1), T(0), T(0)};
+        if (!ideal) {
+            cx.c = mg[0];
+            cx.s = mg[1];
+            cx.c2 = mg[2];
+            cx.s2 = mg[3];
+            cx.cs = mg[4];
+        }
+        reg_cx_group<T, R, pair_base<DA, DB>(0), SA, SB>(v, cx, ideal);
+        if constexpr (R > 2) {
+            reg_cx_group<T, R, pair_base<DA, DB>(1), SA, SB>(v, cx, ideal);
+            reg_cx_group<T, R, pair_base<DA, DB>(2), SA, SB>(v, cx, ideal);
+            reg_cx_group<T, R, pair_base<DA, DB>(3), SA, SB>(v, cx, ideal);
+        }
+    } else {  // DM_OP_DIAG2: one row of four coefficients at a time
+#pragma unroll
+        for (int pa = 0; pa < 4; ++pa) {
+            T d[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) d[i] = mg[4 * pa + i];
+            reg_diag_row<T, R, DA, DB, 0>(v, pa, d);
+            if constexpr (R > 2) {
+                reg_diag_row<T, R, DA, DB, 1>(v, pa, d);
+                reg_diag_row<T, R, DA, DB, 2>(v, pa, d);
+                reg_diag_row<T, R, DA, DB, 3>(v, pa, d);
+            }
+        }
+    }
+}
+
+// Digit positions of an op inside its round: flags bits 8-9 (axis a), 12-13 (axis b).
+template <typename T, int R>
+__device__ __forceinline__ void reg_apply(T (&v)[1 << (2 * R)], const dm_op &op, const T *__restrict__ mats) {
+    const T *mg = mats + op.moff;
+    const int da = (op.flags >> 8) & 3, db = (op.flags >> 12) & 3;
+    if (op.kind == DM_OP_MAP1) {
+        const bool row0 = (op.flags & DM_MAP1_ROW0_IDENTITY) != 0;
+        if (da == 0) reg_map1<T, R, 0>(v, mg, row0);
+        else if (da == 1) reg_map1<T, R, 1>(v, mg, row0);
+        else if constexpr (R > 2) reg_map1<T, R, 2>(v, mg, row0);
+        return;
+    }
+    if constexpr (R == 2) {
+        if (da == 0) reg_pair<T, R, 0, 1>(v, op, mg);
+        else reg_pair<T, R, 1, 0>(v, op, mg);
+    } else {
+        const int code = da * 4 + db;
+        switch (code) {
+            case 1: reg_pair<T, R, 0, 1>(v, op, mg); break;
+            case 2: reg_pair<T, R, 0, 2>(v, op, mg); break;
+            case 4: reg_pair<T, R, 1, 0>(v, op, mg); break;
+            case 6: reg_pair<T, R, 1, 2>(v, op, mg); break;
+            case 8: reg_pair<T, R, 2, 0>(v, op, mg); break;
+            case 9: reg_pair<T, R, 2, 1>(v, op, mg); break;
+            default: break;
+        }
+    }
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(256, 2) pass_rounds_kernel(T *__restrict__ st, const __grid_constant__ PassRounds p,
+                                                             const T *__restrict__ mats) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *tile = reinterpret_cast<T *>(smem_raw);
+    constexpr int G = 1 << (2 * R);
+    const int tsize = 1 << (2 * p.k);
+    const int ngroups = 1 << (2 * (p.k - R));
+    const int64_t ntiles = int64_t(1) << (2 * p.m);
+    const int tid = threadIdx.x;
+    const int64_t off_tid = rounds_offset(p, tid & (tsize - 1));
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int64_t base = 0;
+        {
+            int64_t tt = t;
+            for (int u = 0; u < p.m; ++u) {
+                base += (tt & 3) * p.nonres_stride[u];
+                tt >>= 2;
+            }
+        }
+        base += off_tid;
+        // tile <- state: element e = e0 + tid; the offset is additive over the digits of e0 and tid
+#pragma unroll 8
+        for (int e0 = 0; e0 < tsize; e0 += 256) {
+            const int e = e0 + tid;
+            if (e < tsize) tile[swz(e)] = st[base + rounds_offset(p, e0)];
+        }
+        __syncthreads();
+        int opb = 0;
+        for (int r = 0; r < p.nrounds; ++r) {
+            const int a0 = p.rax[r][0], a1 = p.rax[r][1], a2 = R > 2 ? p.rax[r][2] : 0;
+            int t0[4], t1[4], t2[4];
+#pragma unroll
+            for (int d = 0; d < 4; ++d) {
+                t0[d] = swz(d << (2 * a0));
+                t1[d] = swz(d << (2 * a1));
+                t2[d] = R > 2 ? swz(d << (2 * a2)) : 0;
+            }
+            const int ope = p.rend[r];
+            for (int g = tid; g < ngroups; g += blockDim.x) {
+                int b = insert_zero_digit32(g, a0);
+                b = insert_zero_digit32(b, a1);
+                if (R > 2) b = insert_zero_digit32(b, a2);
+                int pb = swz(b);
+                T v[G];
+#pragma unroll
+                for (int j = 0; j < G; ++j) v[j] = tile[pb ^ t0[j & 3] ^ t1[(j >> 2) & 3] ^ t2[(j >> 4) & 3]];
+                for (int i = opb; i < ope; ++i) reg_apply<T, R>(v, p.ops[i], mats);
+                // recompute the addresses below instead of keeping 4**R of them live
+                asm volatile("" : "+r"(pb));
+#pragma unroll
+                for (int j = 0; j < G; ++j) tile[pb ^ t0[j & 3] ^ t1[(j >> 2) & 3] ^ t2[(j >> 4) & 3]] = v[j];
+            }
+            opb = ope;
+            __syncthreads();
+        }
+#pragma unroll 8
+        for (int e0 = 0; e0 < tsize; e0 += 256) {
+            const int e = e0 + tid;
+            if (e < tsize) st[base + rounds_offset(p, e0)] = tile[swz(e)];
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 
@@ -298,6 +534,67 @@ static int build_pass(int n, const dm_pass *in, size_t mats_count, PassDev *out)
     return DM_OK;
 }
 
+// Validate the round structure of a pass and fill the kernel parameters.
+static int build_rounds(const dm_pass *in, const PassDev &pd, int R, PassRounds *out) {
+    const int nr = in->nrounds;
+    if (nr < 1 || nr > DM_MAX_ROUNDS || pd.k < R) return DM_ERR_PROGRAM;
+    int prev_end = 0;
+    for (int r = 0; r < nr; ++r) {
+        int last = -1;
+        for (int i = 0; i < R; ++i) {
+            const int a = in->round_axes[r][i];
+            if (a <= last || a >= pd.k) return DM_ERR_PROGRAM;   // ascending, inside the tile
+            last = a;
+            out->rax[r][i] = int8_t(a);
+        }
+        for (int i = R; i < 4; ++i) out->rax[r][i] = -1;
+        const int end = in->round_end[r];
+        if (end < prev_end || end > pd.nops) return DM_ERR_PROGRAM;
+        for (int o = prev_end; o < end; ++o) {
+            const dm_op &op = in->ops[o];
+            if (op.kind == DM_OP_MAP2) return DM_ERR_PROGRAM;   // not held in registers
+            const int da = (op.flags >> 8) & 3, db = (op.flags >> 12) & 3;
+            if (da >= R || in->round_axes[r][da] != op.a) return DM_ERR_PROGRAM;
+            if (op.kind != DM_OP_MAP1 && (db >= R || db == da || in->round_axes[r][db] != op.b))
+                return DM_ERR_PROGRAM;
+        }
+        out->rend[r] = int16_t(end);
+        prev_end = end;
+    }
+    if (prev_end != pd.nops) return DM_ERR_PROGRAM;
+    out->n = pd.n;
+    out->k = pd.k;
+    out->low = pd.low;
+    out->m = pd.m;
+    out->nops = pd.nops;
+    out->nrounds = nr;
+    for (int r = 0; r < DM_MAX_TILE_AXES; ++r) out->res_stride[r] = pd.res_stride[r];
+    for (int u = 0; u < DM_MAX_QUBITS; ++u) out->nonres_stride[u] = pd.nonres_stride[u];
+    for (int i = 0; i < pd.nops; ++i) out->ops[i] = pd.ops[i];
+    return DM_OK;
+}
+
+template <typename T, int R>
+static int launch_rounds(T *st, const PassRounds &p, const T *mats, cudaStream_t s) {
+    const size_t smem = (size_t(1) << (2 * p.k)) * sizeof(T);
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(pass_rounds_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int((size_t(1) << (2 * DM_MAX_TILE_AXES)) * sizeof(T)));
+    });
+    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    int per_sm = 0;
+    DM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pass_rounds_kernel<T, R>, 256, smem));
+    if (per_sm < 1) per_sm = 1;
+    const int64_t ntiles = int64_t(1) << (2 * p.m);
+    int64_t grid = int64_t(sm_count()) * per_sm;
+    if (grid > ntiles) grid = ntiles;
+    pass_rounds_kernel<T, R><<<int(grid), 256, smem, s>>>(st, p, mats);
+    count_launch();
+    return launch_status();
+}
+
 template <typename T>
 static int launch_pass(T *st, const PassDev &p, const T *mats, cudaStream_t s) {
     const size_t smem = (size_t(1) << (2 * p.k)) * sizeof(T);
@@ -330,6 +627,16 @@ extern "C" int dm_apply_pass(void *state_dev, int n, int dtype, const dm_pass *p
     PassDev p;
     int rc = build_pass(n, pass, mats_count, &p);
     if (rc) return rc;
+    if (pass->nrounds > 0) {
+        static thread_local PassRounds pr;   // ~2.5 KB: keep it off the host stack
+        const int R = dtype == DM_F64 ? DM_ROUND_AXES_F64 : DM_ROUND_AXES_F32;
+        if ((rc = build_rounds(pass, p, R, &pr))) return rc;
+        if (dtype == DM_F64)
+            return launch_rounds<double, DM_ROUND_AXES_F64>(static_cast<double *>(state_dev), pr,
+                                                            static_cast<const double *>(mats_dev), as_stream(stream));
+        return launch_rounds<float, DM_ROUND_AXES_F32>(static_cast<float *>(state_dev), pr,
+                                                       static_cast<const float *>(mats_dev), as_stream(stream));
+    }
     if (dtype == DM_F64)
         return launch_pass(static_cast<double *>(state_dev), p, static_cast<const double *>(mats_dev),
                            as_stream(stream));

@@ -29,7 +29,8 @@ Differences (the reference fails on these inputs):
   an AttributeError) with a readable message.
 GB300 options (absent from the reference): ``precision`` ('double', the
 default and the parity form, or 'single'), ``fusion`` (fused tile passes,
-default True), ``tile_axes`` (resident axes per tile) and
+default True), ``tile_axes`` (resident axes per tile), ``register_rounds``
+(apply a pass's operations in register rounds, default True) and
 ``coefficients_to_host`` (default True; False leaves ``coeffmatrix`` /
 ``densitymatrix`` out of the result, for callers that only need the
 measurement data of a large register).
@@ -223,6 +224,7 @@ class DmSimulatorGPU(_Base):
         self._fusion = True
         self._tile_axes = None
         self._coefficients_to_host = True
+        self._register_rounds = True
         self.last_run_stats = {}
         self._record_next = False
         self.recorded_state = None
@@ -314,6 +316,8 @@ class DmSimulatorGPU(_Base):
             self._fusion = bool(backend_options['fusion'])
         if 'tile_axes' in backend_options:
             self._tile_axes = int(backend_options['tile_axes'])
+        if 'register_rounds' in backend_options:
+            self._register_rounds = bool(backend_options['register_rounds'])
         if 'coefficients_to_host' in backend_options:
             self._coefficients_to_host = bool(backend_options['coefficients_to_host'])
 
@@ -546,7 +550,8 @@ class DmSimulatorGPU(_Base):
         data = {}
         if any(op.name == 'bfunc' for op in experiment.instructions):
             raise BasicAerError('dm_simulator does not support conditional (bfunc) operations')
-        self._dev = DeviceState(n, precision=self._precision, fusion=self._fusion, tile_axes=self._tile_axes)
+        self._dev = DeviceState(n, precision=self._precision, fusion=self._fusion, tile_axes=self._tile_axes,
+                                rounds=self._register_rounds)
         if self._record_next:
             self._dev.record()
         launches0 = N.lib().dm_kernel_launch_count()

@@ -31,7 +31,7 @@ class DeviceState:
     """An n-qubit Pauli-coefficient vector on a CUDA device."""
 
     def __init__(self, n, precision='double', fusion=True, tile_axes=None, low_axes=DEFAULT_LOW_AXES,
-                 device=None):
+                 device=None, rounds=True):
         torch = _torch()
         if not torch.cuda.is_available():
             raise BasicAerError('dm_simulator (GB300) needs a CUDA device; none is visible')
@@ -48,6 +48,7 @@ class DeviceState:
         self.torch_dtype = torch.float64 if precision == 'double' else torch.float32
         self.state = torch.empty(4 ** n, dtype=self.torch_dtype, device=self.device)
         self.fusion = fusion
+        self.rounds = rounds
         self.kmax = min(tile_axes or DEFAULT_TILE_AXES[precision], N.DM_MAX_TILE_AXES)
         self.low = low_axes
         self.pending = []
@@ -136,7 +137,8 @@ class DeviceState:
     def _run_passes(self, passes):
         torch = _torch()
         mats = []
-        descs = [encode_pass(p, mats, self.np_dtype) for p in passes]
+        width = N.DM_ROUND_AXES[self.dtype] if self.rounds else None
+        descs = [encode_pass(p, mats, self.np_dtype, width) for p in passes]
         host = np.concatenate(mats) if mats else np.zeros(1, dtype=self.np_dtype)
         h = torch.from_numpy(host)
         if self.device.type == 'cuda':

@@ -217,40 +217,91 @@ def plan_passes(ops, n, kmax, low):
     return passes
 
 
-def encode_pass(p, mats, dtype_np):
-    """Fill a ctypes DmPass for ``p``; append its coefficients to ``mats`` (list of arrays)."""
+def plan_rounds(p, width):
+    """Group a pass's ops into register rounds of ``width`` local axes.
+
+    Returns a list of (axes, ops): ``axes`` the round's local axes (ascending,
+    exactly ``width`` of them, padded with untouched axes), ``ops`` the ops
+    (axes in local numbering) in the order they run.  Built with the same
+    dependency-respecting scan as the passes themselves, over the tile's
+    local axes with no mandatory axes.
+    """
+    k = len(p.axes)
+    local = [Op(op.kind, tuple(p.local(a) for a in op.axes), op.data, op.ideal) for op in p.ops]
+    rounds = []
+    for r in plan_passes(local, k, width, 0):
+        axes = sorted(r.axes)
+        for a in range(k):
+            if len(axes) >= width:
+                break
+            if a not in axes:
+                axes.append(a)
+        rounds.append((sorted(axes), r.ops))
+    return rounds
+
+
+def encode_pass(p, mats, dtype_np, round_width=None):
+    """Fill a ctypes DmPass for ``p``; append its coefficients to ``mats`` (list of arrays).
+
+    With ``round_width`` the ops are grouped into register rounds (when the
+    pass has at least that many axes and the rounds fit the descriptor).
+    """
     dp = N.DmPass()
     dp.k = len(p.axes)
     for r, q in enumerate(p.axes):
         dp.axes[r] = q
-    dp.nops = len(p.ops)
+    rounds = None
+    if round_width and dp.k >= round_width and all(op.kind != 'map2' for op in p.ops):
+        rounds = plan_rounds(p, round_width)
+        if len(rounds) > N.DM_MAX_ROUNDS or sum(len(ops) for _, ops in rounds) > N.DM_MAX_PASS_OPS:
+            rounds = None
+    if rounds is not None:
+        ops_local = []
+        dp.nrounds = len(rounds)
+        for ri, (axes, rops) in enumerate(rounds):
+            for i, a in enumerate(axes):
+                dp.round_axes[ri][i] = a
+            for i in range(len(axes), 4):
+                dp.round_axes[ri][i] = -1
+            for op in rops:
+                ops_local.append((op, [axes.index(a) for a in op.axes]))
+            dp.round_end[ri] = len(ops_local)
+    else:
+        dp.nrounds = 0
+        ops_local = [(Op(op.kind, tuple(p.local(a) for a in op.axes), op.data, op.ideal), None) for op in p.ops]
+    dp.nops = len(ops_local)
     off = sum(m.size for m in mats)
-    for i, op in enumerate(p.ops):
+    for i, (op, digits) in enumerate(ops_local):
         o = dp.ops[i]
-        o.a = p.local(op.axes[0])
+        o.a = op.axes[0]
         o.moff = off
         if op.kind == 'map1':
             o.kind = N.DM_OP_MAP1
             m = np.ascontiguousarray(op.data, dtype=np.float64).reshape(16)
-            o.flags = N.DM_MAP1_ROW0_IDENTITY if (m[0] == 1.0 and not m[1:4].any()) else 0
+            flags = N.DM_MAP1_ROW0_IDENTITY if (m[0] == 1.0 and not m[1:4].any()) else 0
             o.b = 0
         elif op.kind == 'cx':
             o.kind = N.DM_OP_CX
-            o.b = p.local(op.axes[1])
-            o.flags = N.DM_CX_IDEAL if op.ideal else 0
+            o.b = op.axes[1]
+            flags = N.DM_CX_IDEAL if op.ideal else 0
             m = np.asarray(op.data, dtype=np.float64)
         elif op.kind == 'diag2':
             o.kind = N.DM_OP_DIAG2
-            o.b = p.local(op.axes[1])
-            o.flags = 0
+            o.b = op.axes[1]
+            flags = 0
             m = np.asarray(op.data, dtype=np.float64).reshape(16)
         elif op.kind == 'map2':
             o.kind = N.DM_OP_MAP2
-            o.b = p.local(op.axes[1])
-            o.flags = 0
+            o.b = op.axes[1]
+            flags = 0
             m = np.asarray(op.data, dtype=np.float64).reshape(256)
         else:
             raise ValueError(op.kind)
+        if digits is not None:              # round digit positions of the op's axes
+            flags |= digits[0] << 8
+            if len(digits) > 1:
+                flags |= digits[1] << 12
+        o.flags = flags
         mats.append(m.astype(dtype_np))
         off += m.size
     return dp

@@ -6,6 +6,7 @@ No kernel runs here: only calls that the library rejects on the host
 import ctypes
 import os
 import re
+import subprocess
 
 import pytest
 
@@ -34,13 +35,25 @@ def test_every_declared_symbol_is_exported(lib):
         assert name in N.SIGNATURES, name
 
 
-def test_struct_layout_matches_header():
-    assert ctypes.sizeof(N.DmOp) == 16
-    assert ctypes.sizeof(N.DmPass) == 4 + 4 * N.DM_MAX_TILE_AXES + 4 + 16 * N.DM_MAX_PASS_OPS
+def test_struct_layout_matches_header(tmp_path):
+    """ctypes mirrors of dm_op / dm_pass have the C compiler's sizes and offsets."""
+    src = tmp_path / 'layout.c'
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "dm_gb300.h"\n'
+        'int main(void) { printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(dm_op), sizeof(dm_pass), '
+        'offsetof(dm_pass, nops), offsetof(dm_pass, nrounds), offsetof(dm_pass, round_axes), '
+        'offsetof(dm_pass, round_end), offsetof(dm_pass, ops)); return 0; }\n')
+    exe = tmp_path / 'layout'
+    subprocess.run(['gcc', '-I', os.path.dirname(HEADER), str(src), '-o', str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    want = [ctypes.sizeof(N.DmOp), ctypes.sizeof(N.DmPass), N.DmPass.nops.offset, N.DmPass.nrounds.offset,
+            N.DmPass.round_axes.offset, N.DmPass.round_end.offset, N.DmPass.ops.offset]
+    assert got == want
     text = open(HEADER).read()
     assert int(re.search(r'#define DM_MAX_TILE_AXES (\d+)', text).group(1)) == N.DM_MAX_TILE_AXES
     assert int(re.search(r'#define DM_MAX_PASS_OPS (\d+)', text).group(1)) == N.DM_MAX_PASS_OPS
     assert int(re.search(r'#define DM_MAX_QUBITS (\d+)', text).group(1)) == N.DM_MAX_QUBITS
+    assert int(re.search(r'#define DM_MAX_ROUNDS (\d+)', text).group(1)) == N.DM_MAX_ROUNDS
 
 
 def test_error_strings_and_version(lib):

@@ -69,11 +69,14 @@ def test_map1_cx_noise(torch, n, dtype):
 
 @pytest.mark.parametrize('n,k,low', [(4, 4, 2), (6, 6, 2), (7, 5, 2), (8, 6, 2), (9, 7, 2), (9, 7, 3), (10, 6, 0)])
 @pytest.mark.parametrize('dtype', [N.DM_F64, N.DM_F32])
-def test_fused_pass_equals_program_order(torch, n, k, low, dtype):
+@pytest.mark.parametrize('rounds', [False, True])
+def test_fused_pass_equals_program_order(torch, n, k, low, dtype, rounds):
     from test_planner import apply_op, random_ops
     rng = np.random.default_rng(1000 + n * 7 + k)
     npdt = np.float64 if dtype == N.DM_F64 else np.float32
     ops = random_ops(rng, n, 80)
+    if rounds:
+        ops = [op for op in ops if op.kind != 'map2']
     for op in ops:                       # keep magnitudes bounded
         if op.kind == 'map1':
             op.data = op.data / np.abs(op.data).sum(axis=1, keepdims=True)
@@ -85,7 +88,9 @@ def test_fused_pass_equals_program_order(torch, n, k, low, dtype):
         ref = apply_op(ref, n, op)
     passes = P.plan_passes(ops, n, k, low)
     mats = []
-    descs = [P.encode_pass(p, mats, npdt) for p in passes]
+    descs = [P.encode_pass(p, mats, npdt, N.DM_ROUND_AXES[dtype] if rounds else None) for p in passes]
+    if rounds:
+        assert any(d.nrounds > 0 for d in descs)
     m = np.concatenate(mats)
     md = dev(torch, m, npdt)
     t = dev(torch, st, npdt)

@@ -91,7 +91,8 @@ def test_workloads_match_oracle(n, layers, seed, every_gate, qft):
     opts['compute_densitymatrix'] = False
     ref = _oracle(qc.to_experiment(), opts)
     for kw, tol in (({}, 1e-12), ({'tile_axes': 7}, 1e-12), ({'tile_axes': 4}, 1e-12),
-                    ({'precision': 'single'}, 2e-5)):
+                    ({'register_rounds': False}, 1e-12), ({'precision': 'single'}, 2e-5),
+                    ({'precision': 'single', 'register_rounds': False}, 2e-5)):
         got, b = run_gpu(qc.to_experiment(), opts, **kw)
         assert got['number_of_clock_cycles'] == ref['number_of_clock_cycles']
         _assert_close(got, ref, n, tol)

@@ -162,3 +162,30 @@ def test_brick_layers_fuse_into_few_passes():
             ops.append(P.Op('map1', (q,), noise))
     passes = P.plan_passes(ops, n, 7, 2)
     assert len(passes) / 6 <= 4.0
+
+
+@pytest.mark.parametrize('width', [2, 3])
+@pytest.mark.parametrize('n,kmax,low', [(5, 4, 2), (7, 6, 2), (8, 7, 2), (9, 7, 3)])
+def test_register_rounds_equal_program_order(n, kmax, low, width):
+    """Rounds regroup a pass's ops; replaying them in round order equals program order."""
+    rng = np.random.default_rng(7 * n + kmax + width)
+    for trial in range(4):
+        ops = [op for op in random_ops(rng, n, int(rng.integers(5, 60))) if op.kind != 'map2']
+        st0 = rng.normal(size=4 ** n)
+        ref = st0.copy()
+        for op in ops:
+            ref = apply_op(ref, n, op)
+        got = st0.copy()
+        for p in P.plan_passes(ops, n, kmax, low):
+            rounds = P.plan_rounds(p, width)
+            for axes, rops in rounds:
+                assert len(axes) == min(width, len(p.axes)) and axes == sorted(axes)
+                for op in rops:
+                    assert set(op.axes).issubset(axes)
+                    glob = P.Op(op.kind, tuple(p.axes[a] for a in op.axes), op.data, op.ideal)
+                    got = apply_op(got, n, glob)
+            dp = P.encode_pass(p, [], np.float64, width)
+            if len(p.axes) >= width:
+                assert dp.nrounds == len(rounds)
+                assert dp.round_end[dp.nrounds - 1] == dp.nops
+        np.testing.assert_allclose(got, ref, rtol=1e-10, atol=1e-10 * np.abs(ref).max())
