@@ -122,7 +122,10 @@ int dm_apply_memory_noise(void *state_dev, int n, int dtype, double f, double p,
  * resident axes is loaded once, all of the pass's operations are applied to
  * it on chip, and it is written back once.  mats_dev holds mats_count
  * coefficients (in the state's dtype) that the ops index by moff.  This is the GB300 form of a run of
- * consecutive levels of DmSimulatorPy.run_experiment (dm_simulator.py:1005-1177). */
+ * consecutive levels of DmSimulatorPy.run_experiment (dm_simulator.py:1005-1177).
+ * With nrounds > 0 the pass runs on the pipelined round kernel, which needs
+ * the lowest qubit axis (n-1) resident, at most 7 (FP32) / 6 (FP64)
+ * resident axes, no DM_OP_MAP2, and a 16-byte aligned state. */
 int dm_apply_pass(void *state_dev, int n, int dtype, const dm_pass *pass, const void *mats_dev,
                   size_t mats_count, void *stream);
 

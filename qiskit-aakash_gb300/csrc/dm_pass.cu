@@ -422,69 +422,125 @@ __device__ __forceinline__ void reg_apply(T (&v)[1 << (2 * R)], const dm_op &op,
     }
 }
 
+// Chunk-preserving swizzle: the 16-byte chunk index inside each 128-byte row
+// is XORed with bits of the two next rows, so whole 16-byte chunks stay
+// contiguous (cp.async / 128-bit accesses) while a warp's round groups
+// spread over the banks.  XOR-linear on elements with disjoint bits.
+template <typename T>
+__device__ __forceinline__ int swz16(int e) {
+    constexpr int C = sizeof(T) == 4 ? 2 : 1;   // log2(elements per 16-byte chunk)
+    constexpr int S = C + 3;                      // first row bit (8 chunks per 128-byte row)
+    return e ^ ((((e >> S) ^ (e >> (S + 3))) & 7) << C);
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+constexpr int kPipeBuffers = 3;
+constexpr int kPipeThreads = 256;
+
+// Largest tile the pipelined kernel holds per buffer: 4**7 FP32 (64 KB) or 4**6 FP64 (32 KB).
+template <typename T>
+__host__ __device__ constexpr int pipe_tile_axes() { return sizeof(T) == 4 ? 7 : 6; }
+
+// One persistent CTA per SM streams the pass's tiles through kPipeBuffers
+// shared-memory buffers: while the rounds of tile i run, the 16-byte
+// cp.async copies of the next tiles are in flight; each finished tile is
+// written back with 128-bit stores.
 template <typename T, int R>
-__global__ void __launch_bounds__(256, 2) pass_rounds_kernel(T *__restrict__ st, const __grid_constant__ PassRounds p,
-                                                             const T *__restrict__ mats) {
+__global__ void __launch_bounds__(kPipeThreads, 1) pass_pipe_kernel(T *__restrict__ st, const __grid_constant__ PassRounds p,
+                                                                    const T *__restrict__ mats) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *tile = reinterpret_cast<T *>(smem_raw);
     constexpr int G = 1 << (2 * R);
+    constexpr int CE = 16 / sizeof(T);                       // elements per 16-byte chunk
+    constexpr int TMAX = 1 << (2 * pipe_tile_axes<T>());
+    __shared__ int64_t hi_off[64];                           // offsets of chunk-index digits above the thread's
+    T *bufs = reinterpret_cast<T *>(smem_raw);
     const int tsize = 1 << (2 * p.k);
+    const int nchunks = tsize / CE;
     const int ngroups = 1 << (2 * (p.k - R));
     const int64_t ntiles = int64_t(1) << (2 * p.m);
     const int tid = threadIdx.x;
-    const int64_t off_tid = rounds_offset(p, tid & (tsize - 1));
-    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    // chunk c = tid + kPipeThreads * i covers elements e = CE * c ...: offset(e) = offset(CE*tid) + offset(CE*kPipeThreads*i)
+    const int64_t off_tid = rounds_offset(p, (CE * tid) & (tsize - 1));
+    for (int i = tid; i < 64; i += kPipeThreads) {
+        const int e = CE * kPipeThreads * i;
+        hi_off[i] = e < tsize ? rounds_offset(p, e) : 0;
+    }
+    __syncthreads();
+
+    auto tile_base = [&](int64_t t) {
         int64_t base = 0;
-        {
-            int64_t tt = t;
-            for (int u = 0; u < p.m; ++u) {
-                base += (tt & 3) * p.nonres_stride[u];
-                tt >>= 2;
+        for (int u = 0; u < p.m; ++u) {
+            base += (t & 3) * p.nonres_stride[u];
+            t >>= 2;
+        }
+        return base;
+    };
+    auto issue_load = [&](int64_t t, int b) {
+        if (t < ntiles) {
+            T *buf = bufs + b * TMAX;
+            const T *src = st + tile_base(t) + off_tid;
+            for (int i = 0; tid + kPipeThreads * i < nchunks; ++i) {
+                const int e = CE * (tid + kPipeThreads * i);
+                cp_async16(buf + swz16<T>(e), src + hi_off[i]);
             }
         }
-        base += off_tid;
-        // tile <- state: element e = e0 + tid; the offset is additive over the digits of e0 and tid
-#pragma unroll 8
-        for (int e0 = 0; e0 < tsize; e0 += 256) {
-            const int e = e0 + tid;
-            if (e < tsize) tile[swz(e)] = st[base + rounds_offset(p, e0)];
-        }
+        cp_async_commit();
+    };
+
+    const int64_t t0 = blockIdx.x, dt = gridDim.x;
+#pragma unroll
+    for (int s = 0; s < kPipeBuffers - 1; ++s) issue_load(t0 + s * dt, s);
+    int b = 0;
+    for (int64_t t = t0; t < ntiles; t += dt) {
+        cp_async_wait<kPipeBuffers - 2>();
         __syncthreads();
+        // the buffer of the previous tile is free: start the copy that reuses it
+        issue_load(t + (kPipeBuffers - 1) * dt, (b + kPipeBuffers - 1) % kPipeBuffers);
+        T *tile = bufs + b * TMAX;
         int opb = 0;
         for (int r = 0; r < p.nrounds; ++r) {
             const int a0 = p.rax[r][0], a1 = p.rax[r][1], a2 = R > 2 ? p.rax[r][2] : 0;
-            int t0[4], t1[4], t2[4];
+            int t0s[4], t1s[4], t2s[4];
 #pragma unroll
             for (int d = 0; d < 4; ++d) {
-                t0[d] = swz(d << (2 * a0));
-                t1[d] = swz(d << (2 * a1));
-                t2[d] = R > 2 ? swz(d << (2 * a2)) : 0;
+                t0s[d] = swz16<T>(d << (2 * a0));
+                t1s[d] = swz16<T>(d << (2 * a1));
+                t2s[d] = R > 2 ? swz16<T>(d << (2 * a2)) : 0;
             }
             const int ope = p.rend[r];
-            for (int g = tid; g < ngroups; g += blockDim.x) {
-                int b = insert_zero_digit32(g, a0);
-                b = insert_zero_digit32(b, a1);
-                if (R > 2) b = insert_zero_digit32(b, a2);
-                int pb = swz(b);
+            for (int g = tid; g < ngroups; g += kPipeThreads) {
+                int gb = insert_zero_digit32(g, a0);
+                gb = insert_zero_digit32(gb, a1);
+                if (R > 2) gb = insert_zero_digit32(gb, a2);
+                int pb = swz16<T>(gb);
                 T v[G];
 #pragma unroll
-                for (int j = 0; j < G; ++j) v[j] = tile[pb ^ t0[j & 3] ^ t1[(j >> 2) & 3] ^ t2[(j >> 4) & 3]];
+                for (int j = 0; j < G; ++j) v[j] = tile[pb ^ t0s[j & 3] ^ t1s[(j >> 2) & 3] ^ t2s[(j >> 4) & 3]];
                 for (int i = opb; i < ope; ++i) reg_apply<T, R>(v, p.ops[i], mats);
-                // recompute the addresses below instead of keeping 4**R of them live
-                asm volatile("" : "+r"(pb));
+                asm volatile("" : "+r"(pb));   // recompute the addresses instead of keeping them live
 #pragma unroll
-                for (int j = 0; j < G; ++j) tile[pb ^ t0[j & 3] ^ t1[(j >> 2) & 3] ^ t2[(j >> 4) & 3]] = v[j];
+                for (int j = 0; j < G; ++j) tile[pb ^ t0s[j & 3] ^ t1s[(j >> 2) & 3] ^ t2s[(j >> 4) & 3]] = v[j];
             }
             opb = ope;
             __syncthreads();
         }
-#pragma unroll 8
-        for (int e0 = 0; e0 < tsize; e0 += 256) {
-            const int e = e0 + tid;
-            if (e < tsize) st[base + rounds_offset(p, e0)] = tile[swz(e)];
+        // write back with 128-bit stores (the next iteration's barrier orders
+        // these reads before the buffer is refilled)
+        T *dst = st + tile_base(t) + off_tid;
+        for (int i = 0; tid + kPipeThreads * i < nchunks; ++i) {
+            const int e = CE * (tid + kPipeThreads * i);
+            *reinterpret_cast<float4 *>(dst + hi_off[i]) = *reinterpret_cast<const float4 *>(tile + swz16<T>(e));
         }
-        __syncthreads();
+        b = (b + 1) % kPipeBuffers;
     }
+    cp_async_wait<0>();
 }
 
 // ---------------------------------------------------------------------------
@@ -538,6 +594,8 @@ static int build_pass(int n, const dm_pass *in, size_t mats_count, PassDev *out)
 static int build_rounds(const dm_pass *in, const PassDev &pd, int R, PassRounds *out) {
     const int nr = in->nrounds;
     if (nr < 1 || nr > DM_MAX_ROUNDS || pd.k < R) return DM_ERR_PROGRAM;
+    // the pipelined kernel streams 16-byte chunks: the lowest qubit axis must be resident
+    if (pd.low < 1 || pd.k > (R == DM_ROUND_AXES_F32 ? 7 : 6)) return DM_ERR_PROGRAM;
     int prev_end = 0;
     for (int r = 0; r < nr; ++r) {
         int last = -1;
@@ -576,21 +634,17 @@ static int build_rounds(const dm_pass *in, const PassDev &pd, int R, PassRounds 
 
 template <typename T, int R>
 static int launch_rounds(T *st, const PassRounds &p, const T *mats, cudaStream_t s) {
-    const size_t smem = (size_t(1) << (2 * p.k)) * sizeof(T);
+    const size_t smem = size_t(kPipeBuffers) * (size_t(1) << (2 * pipe_tile_axes<T>())) * sizeof(T);
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [] {
-        attr_err = cudaFuncSetAttribute(pass_rounds_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        int((size_t(1) << (2 * DM_MAX_TILE_AXES)) * sizeof(T)));
+    std::call_once(once, [smem] {
+        attr_err = cudaFuncSetAttribute(pass_pipe_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     });
     if (attr_err != cudaSuccess) return DM_ERR_CUDA;
-    int per_sm = 0;
-    DM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pass_rounds_kernel<T, R>, 256, smem));
-    if (per_sm < 1) per_sm = 1;
     const int64_t ntiles = int64_t(1) << (2 * p.m);
-    int64_t grid = int64_t(sm_count()) * per_sm;
+    int64_t grid = sm_count();
     if (grid > ntiles) grid = ntiles;
-    pass_rounds_kernel<T, R><<<int(grid), 256, smem, s>>>(st, p, mats);
+    pass_pipe_kernel<T, R><<<int(grid), kPipeThreads, smem, s>>>(st, p, mats);
     count_launch();
     return launch_status();
 }
@@ -628,6 +682,8 @@ extern "C" int dm_apply_pass(void *state_dev, int n, int dtype, const dm_pass *p
     int rc = build_pass(n, pass, mats_count, &p);
     if (rc) return rc;
     if (pass->nrounds > 0) {
+        // the round kernel copies 16-byte chunks: the state must be 16-byte aligned
+        if (reinterpret_cast<uintptr_t>(state_dev) & 15) return DM_ERR_ARG;
         static thread_local PassRounds pr;   // ~2.5 KB: keep it off the host stack
         const int R = dtype == DM_F64 ? DM_ROUND_AXES_F64 : DM_ROUND_AXES_F32;
         if ((rc = build_rounds(pass, p, R, &pr))) return rc;

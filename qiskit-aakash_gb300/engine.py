@@ -138,7 +138,7 @@ class DeviceState:
         torch = _torch()
         mats = []
         width = N.DM_ROUND_AXES[self.dtype] if self.rounds else None
-        descs = [encode_pass(p, mats, self.np_dtype, width) for p in passes]
+        descs = [encode_pass(p, mats, self.np_dtype, width, self.n) for p in passes]
         host = np.concatenate(mats) if mats else np.zeros(1, dtype=self.np_dtype)
         h = torch.from_numpy(host)
         if self.device.type == 'cuda':

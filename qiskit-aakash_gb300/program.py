@@ -240,18 +240,26 @@ def plan_rounds(p, width):
     return rounds
 
 
-def encode_pass(p, mats, dtype_np, round_width=None):
+# Largest pass (resident axes) the pipelined round kernel holds per dtype.
+ROUND_MAX_AXES = {np.dtype(np.float32): 7, np.dtype(np.float64): 6}
+
+
+def encode_pass(p, mats, dtype_np, round_width=None, n=None):
     """Fill a ctypes DmPass for ``p``; append its coefficients to ``mats`` (list of arrays).
 
-    With ``round_width`` the ops are grouped into register rounds (when the
-    pass has at least that many axes and the rounds fit the descriptor).
+    With ``round_width`` (and the register count ``n``) the ops are grouped
+    into register rounds when the pipelined round kernel can run the pass:
+    at least ``round_width`` and at most ROUND_MAX_AXES resident axes, the
+    lowest qubit axis resident (16-byte chunks are contiguous), no 16x16
+    general maps, and the rounds fit the descriptor.
     """
     dp = N.DmPass()
     dp.k = len(p.axes)
     for r, q in enumerate(p.axes):
         dp.axes[r] = q
     rounds = None
-    if round_width and dp.k >= round_width and all(op.kind != 'map2' for op in p.ops):
+    if round_width and n is not None and round_width <= dp.k <= ROUND_MAX_AXES[np.dtype(dtype_np)] \
+            and p.axes[0] == n - 1 and all(op.kind != 'map2' for op in p.ops):
         rounds = plan_rounds(p, round_width)
         if len(rounds) > N.DM_MAX_ROUNDS or sum(len(ops) for _, ops in rounds) > N.DM_MAX_PASS_OPS:
             rounds = None

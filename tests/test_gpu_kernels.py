@@ -88,8 +88,8 @@ def test_fused_pass_equals_program_order(torch, n, k, low, dtype, rounds):
         ref = apply_op(ref, n, op)
     passes = P.plan_passes(ops, n, k, low)
     mats = []
-    descs = [P.encode_pass(p, mats, npdt, N.DM_ROUND_AXES[dtype] if rounds else None) for p in passes]
-    if rounds:
+    descs = [P.encode_pass(p, mats, npdt, N.DM_ROUND_AXES[dtype] if rounds else None, n) for p in passes]
+    if rounds and low > 0 and k <= P.ROUND_MAX_AXES[np.dtype(npdt)]:
         assert any(d.nrounds > 0 for d in descs)
     m = np.concatenate(mats)
     md = dev(torch, m, npdt)
