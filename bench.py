@@ -204,13 +204,26 @@ def barrier(torch, world):
         dist.barrier()
 
 
-def allmax(torch, world, x):
+def allmax(torch, world, x, device='cuda'):
+    """Max of x over the ranks (the slowest replica's time defines the job's time)."""
     if world <= 1:
         return x
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device='cuda')
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(torch, world, units_local, ms_local, device='cuda'):
+    """Whole-job throughput of independent replicas: all units / the slowest rank's time."""
+    ms = allmax(torch, world, ms_local, device)
+    units = units_local
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([units_local], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        units = float(t.item())
+    return units / (ms / 1e3), ms
 
 
 def time_replays(torch, state, steps):
@@ -290,7 +303,7 @@ def run_ours(args):
         ms32 = time_replays(torch, st32, args.steps)
     launches = (N.lib().dm_kernel_launch_count() - l0)
     barrier(torch, world)
-    ms32 = allmax(torch, world, ms32)
+    value32, ms32 = replica_throughput(torch, world, float(layers), ms32)
     durs = pass_kernel_profile(torch, st32)     # a full replay: leaves the final FP32 state
     prob32 = np.array(list(r32['data']['ensemble_probability'].values()))
 
@@ -336,7 +349,7 @@ def run_ours(args):
     traffic = profiled_traffic()
     line = {
         'metric': METRIC,
-        'value': world * layers / (ms32 / 1e3),
+        'value': value32,
         'unit': 'gate-layers/s',
         'n_gpus': world,
         'steps': args.steps,
