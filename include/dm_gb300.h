@@ -83,6 +83,11 @@ typedef struct dm_pass {
     int8_t round_axes[DM_MAX_ROUNDS][4];
     int16_t round_end[DM_MAX_ROUNDS];
     dm_op ops[DM_MAX_PASS_OPS];
+    /* dm_apply_pass_tc only: float offset of round r's transfer-matrix image
+     * (the 64x64 map of the round's composed ops, as 4096 TF32-rounded "hi"
+     * floats then 4096 "lo" remainder floats, each in the K-major core-matrix
+     * order (n%8)*4 + k%4 + (k/4)*32 + (n/8)*512 for output n, input k). */
+    int32_t round_moff[DM_MAX_ROUNDS];
 } dm_pass;
 
 /* Round width (axes held in registers per round) for a dtype. */
@@ -128,6 +133,17 @@ int dm_apply_memory_noise(void *state_dev, int n, int dtype, double f, double p,
  * resident axes, no DM_OP_MAP2, and a 16-byte aligned state. */
 int dm_apply_pass(void *state_dev, int n, int dtype, const dm_pass *pass, const void *mats_dev,
                   size_t mats_count, void *stream);
+
+/* The fused pass on the tensor cores (FP32 state only).  The pass must hold
+ * exactly 7 resident axes including the lowest qubit axis, and n >= 7; its
+ * rounds (round_axes[r][0..2], 3 local axes each) are applied as 64x64
+ * transfer matrices (round_moff[r] into umats_dev, umats_count floats) by
+ * tcgen05.mma kind::tf32 in 3xTF32 (hi/lo split of state and matrix, FP32
+ * accumulation in tensor memory).  The ops list is not read.  status_dev
+ * (device int, 0 before the first call) is set to 1 if the kernel abandons a
+ * bounded wait.  Same role as dm_apply_pass (dm_simulator.py:1005-1177). */
+int dm_apply_pass_tc(void *state_dev, int n, const dm_pass *pass, const float *umats_dev, size_t umats_count,
+                     int *status_dev, void *stream);
 
 /* ---------------------------------------------------------------- measurement */
 

@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG_DIR, 'csrc')
 INCLUDE = os.path.join(REPO_DIR, 'include')
 BUILD_DIR = os.path.join(PKG_DIR, '_build')
 LIB_PATH = os.path.join(PKG_DIR, 'libdmgb300.so')
-SOURCES = ['dm_misc.cu', 'dm_pass.cu', 'dm_state.cu', 'dm_measure.cu']
+SOURCES = ['dm_misc.cu', 'dm_pass.cu', 'dm_state.cu', 'dm_measure.cu', 'dm_tc.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '-Xptxas', '-warn-spills',
               '--expt-relaxed-constexpr']
@@ -92,7 +92,8 @@ class DmPass(ctypes.Structure):
                 ('nops', ctypes.c_int32), ('nrounds', ctypes.c_int32),
                 ('round_axes', (ctypes.c_int8 * 4) * DM_MAX_ROUNDS),
                 ('round_end', ctypes.c_int16 * DM_MAX_ROUNDS),
-                ('ops', DmOp * DM_MAX_PASS_OPS)]
+                ('ops', DmOp * DM_MAX_PASS_OPS),
+                ('round_moff', ctypes.c_int32 * DM_MAX_ROUNDS)]
 
 
 _vp = ctypes.c_void_p
@@ -110,6 +111,7 @@ SIGNATURES = {
     'dm_apply_cx': (_i, [_vp, _i, _i, _i, _i, _dp, _vp]),
     'dm_apply_memory_noise': (_i, [_vp, _i, _i, _d, _d, _d, _vp]),
     'dm_apply_pass': (_i, [_vp, _i, _i, ctypes.POINTER(DmPass), _vp, _sz, _vp]),
+    'dm_apply_pass_tc': (_i, [_vp, _i, ctypes.POINTER(DmPass), _vp, _sz, _vp, _vp]),
     'dm_axis_probs': (_i, [_vp, _i, _i, _ip, _d, _vp, _vp]),
     'dm_nbasis_probs_scratch_bytes': (_sz, [_i]),
     'dm_nbasis_probs': (_i, [_vp, _i, _i, _dp, _d, _vp, _vp, _vp]),

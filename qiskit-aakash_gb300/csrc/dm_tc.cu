@@ -1,0 +1,412 @@
+// Tensor-core fused pass (FP32 state, 3xTF32 on tcgen05).
+//
+// A pass holds 7 resident qubit axes: every tile of 4**7 = 16,384
+// coefficients is streamed into shared memory (cp.async, 16-byte chunks),
+// then the pass's register rounds run as matrix products on the tensor
+// cores.  A round names 3 of the tile's axes; the round's operations,
+// composed on the host in FP64, form one 64x64 real transfer matrix U acting
+// on the 64 coefficients that differ only in those axes.  With the tile
+// viewed as 256 groups x 64 (one row per group), the round is
+//     D[g][j'] = sum_j X[g][j] * U[j'][j]           (M = 256, N = 64, K = 64)
+// issued as two M = 128 tcgen05.mma.kind::tf32 chains into TMEM.  FP32
+// accuracy comes from the 3xTF32 split X = Xh + Xl, U = Uh + Ul:
+//     D = Xh Uh^T + Xl Uh^T + Xh Ul^T             (the Xl Ul term is below FP32)
+// The epilogue reads D from TMEM (tcgen05.ld, one group per thread) and
+// writes the hi/lo split directly in the operand layout of the next round;
+// after the last round it writes the tile back in its natural layout for
+// 128-bit stores.  Every wait on an mbarrier is bounded: a wait that gives up
+// records an error in *status and the kernel drains and returns.
+//
+// Shared memory (dynamic, 224 KB): NAT 64 KB (cp.async landing buffer of
+// the next tile), AH / AL 64 KB each (round operand hi / lo, K-major
+// core-matrix layout, 256 rows x 64), BH / BL 16 KB each (U hi / lo).
+#include <mutex>
+
+#include "dm_common.cuh"
+
+namespace dmg {
+
+namespace tc {
+
+constexpr int kThreads = 256;
+constexpr int kAxes = 7;                       // resident axes per tile
+constexpr int kTile = 1 << (2 * kAxes);        // 16384 coefficients
+constexpr int kGroups = kTile / 64;            // 256 rows per round
+constexpr uint32_t kNatBytes = kTile * 4;      // 64 KB
+constexpr uint32_t kABytes = kGroups * 64 * 4; // 64 KB
+constexpr uint32_t kBBytes = 64 * 64 * 4;      // 16 KB
+constexpr uint32_t kSmemBytes = kNatBytes + 2 * kABytes + 2 * kBBytes;   // 224 KB
+constexpr uint32_t kTmemCols = 128;            // two M = 128 blocks x N = 64
+constexpr int kSpinLimit = 1 << 24;            // bounded waits (about a second)
+
+// K-major core-matrix layout (no swizzle) of a rows x 64 operand: element
+// (row, k) lives at byte (row%8)*16 + (k%4)*4 + (k/4)*128 + (row/8)*2048.
+// LBO (next 16-byte core matrix along K) = 128 B, SBO (next 8 rows) = 2048 B.
+constexpr uint32_t kLBO = 128, kSBO = 2048;
+
+__device__ __forceinline__ uint32_t row_off(int row) { return (row & 7) * 16 + (row >> 3) * kSBO; }
+__device__ __forceinline__ uint32_t k_off(int k) { return (k & 3) * 4 + (k >> 2) * kLBO; }
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+    uint64_t d = uint64_t((saddr >> 4) & 0x3FFF);
+    d |= uint64_t((kLBO >> 4) & 0x3FFF) << 16;
+    d |= uint64_t((kSBO >> 4) & 0x3FFF) << 32;
+    d |= uint64_t(1) << 46;   // sm_100 descriptor version; base offset 0, no swizzle
+    return d;
+}
+
+// kind::tf32, D = F32, A = B = TF32, both K-major, M = 128, N = 64.
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ float tf32_rn(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Natural-layout swizzle of the tile (16-byte chunks intact), as in dm_pass.cu.
+__device__ __forceinline__ int nat_swz(int e) { return e ^ ((((e >> 5) ^ (e >> 8)) & 7) << 2); }
+
+__device__ __forceinline__ int ins0(int g, int pos) {
+    return ((g >> (2 * pos)) << (2 * pos + 2)) | (g & ((1 << (2 * pos)) - 1));
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    for (int it = 0; it < kSpinLimit; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+struct Pass {
+    int n, m, low, nrounds;
+    int64_t res_stride[kAxes];
+    int64_t nonres_stride[DM_MAX_QUBITS];
+    int8_t rax[DM_MAX_ROUNDS][4];
+    int32_t umoff[DM_MAX_ROUNDS];   // float offset of round r's U image (hi 4096 floats, then lo 4096)
+};
+
+__device__ __forceinline__ int64_t tile_offset(const Pass &p, int e) {
+    int64_t off = e & ((1 << (2 * p.low)) - 1);
+    for (int r = p.low; r < kAxes; ++r) off += int64_t((e >> (2 * r)) & 3) * p.res_stride[r];
+    return off;
+}
+
+// Byte offset, in round r's operand layout, of the contribution of one set
+// bit: local axis a, digit bit b (value 1 << b).  Offsets are additive over
+// elements with disjoint bits (row_off and k_off are linear in their bits).
+__device__ __forceinline__ uint32_t bit_contrib(const int8_t *rax, int a, int b) {
+    int k_digit = -1;
+    for (int i = 0; i < 3; ++i)
+        if (rax[i] == a) k_digit = i;
+    if (k_digit >= 0) return k_off((1 << b) << (2 * k_digit));
+    int c = 0;   // rank of a among the non-round axes = its digit in the group (row) index
+    for (int x = 0; x < a; ++x)
+        if (x != rax[0] && x != rax[1] && x != rax[2]) ++c;
+    return row_off((1 << b) << (2 * c));
+}
+
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
+    uint32_t r[64];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,"
+        "%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,"
+        "%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+          "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+          "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+          "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
+          "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 64; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict__ st, const __grid_constant__ Pass p,
+                                                              const float *__restrict__ umats, int *status) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *NAT = smem;
+    unsigned char *AH = smem + kNatBytes;
+    unsigned char *AL = AH + kABytes;
+    unsigned char *BH = AL + kABytes;
+    unsigned char *BL = BH + kBBytes;
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int64_t hi_off[16];
+    __shared__ int abort_s;
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int64_t ntiles = int64_t(1) << (2 * p.m);
+    // natural-layout chunk c = tid + 256 i (4 floats each): offset additive over tid / i bits
+    const int64_t off_tid = tile_offset(p, 4 * tid);
+    if (tid < 16) hi_off[tid] = tile_offset(p, 4 * kThreads * tid);
+    if (tid == 0) {
+        abort_s = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                     "n"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base_s;
+    uint32_t phase = 0;
+
+    auto tile_base = [&](int64_t t) {
+        int64_t base = 0;
+        for (int u = 0; u < p.m; ++u) {
+            base += (t & 3) * p.nonres_stride[u];
+            t >>= 2;
+        }
+        return base;
+    };
+    auto load_tile = [&](int64_t t) {   // into NAT
+        if (t < ntiles) {
+            const float *src = st + tile_base(t) + off_tid;
+#pragma unroll
+            for (int i = 0; i < kTile / 4 / kThreads; ++i)
+                cp_async16(NAT + 4 * nat_swz(4 * (tid + kThreads * i)), src + hi_off[i]);
+        }
+        cp_async_commit();
+    };
+    auto load_u = [&](int r) {          // round r's U images into BH / BL
+        const float *src = umats + p.umoff[r];
+#pragma unroll
+        for (int i = 0; i < 2 * 64 * 64 / 4 / kThreads; ++i) {
+            const int c = tid + kThreads * i;   // 16-byte chunk; BH and BL are contiguous
+            cp_async16(BH + 16 * c, src + 4 * c);
+        }
+        cp_async_commit();
+    };
+
+    const int64_t t0 = blockIdx.x, dt = gridDim.x;
+    load_tile(t0);
+    load_u(0);
+    for (int64_t t = t0; t < ntiles; t += dt) {
+        cp_async_wait_all();
+        __syncthreads();
+        if (abort_s) break;
+        // ---- convert the natural tile into round 0's operand (hi / lo) ----
+        {
+            const int8_t *rx = p.rax[0];
+            const int a0 = rx[0], a1 = rx[1], a2 = rx[2];
+            int gb = ins0(ins0(ins0(tid, a0), a1), a2);
+            const int pb = nat_swz(gb);
+            const uint32_t ro = row_off(tid);
+            int t0s[4], t1s[4], t2s[4];
+#pragma unroll
+            for (int d = 0; d < 4; ++d) {
+                t0s[d] = nat_swz(d << (2 * a0));
+                t1s[d] = nat_swz(d << (2 * a1));
+                t2s[d] = nat_swz(d << (2 * a2));
+            }
+            const float *nat = reinterpret_cast<const float *>(NAT);
+#pragma unroll
+            for (int j = 0; j < 64; ++j) {
+                const float x = nat[pb ^ t0s[j & 3] ^ t1s[(j >> 2) & 3] ^ t2s[j >> 4]];
+                const float h = tf32_rn(x);
+                const uint32_t o = ro + k_off(j);
+                *reinterpret_cast<float *>(AH + o) = h;
+                *reinterpret_cast<float *>(AL + o) = x - h;
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        load_tile(t + dt);   // NAT is free: stream the next tile during the rounds
+        for (int r = 0; r < p.nrounds; ++r) {
+            // round 0's U was waited for with the tile; later rounds wait for their U
+            // (which also completes the older next-tile group)
+            if (r > 0) cp_async_wait_all();
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (tid == 0) {
+                const uint32_t ah = smem_u32(AH), al = smem_u32(AL), bh = smem_u32(BH), bl = smem_u32(BL);
+#pragma unroll
+                for (int mb = 0; mb < 2; ++mb) {
+                    const uint32_t d = tmem + mb * 64;
+                    const uint32_t aoff = mb * (kABytes / 2);
+#pragma unroll
+                    for (int term = 0; term < 3; ++term) {
+                        const uint32_t a = (term == 1 ? al : ah) + aoff;
+                        const uint32_t b = term == 2 ? bl : bh;
+#pragma unroll
+                        for (int ks = 0; ks < 8; ++ks) {
+                            const uint64_t da = smem_desc(a + ks * 2 * kLBO);
+                            const uint64_t db = smem_desc(b + ks * 2 * kLBO);
+                            const uint32_t acc = (term | ks) ? 1u : 0u;
+                            asm volatile(
+                                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+                                "l"(da), "l"(db), "r"(kIdesc), "r"(acc));
+                        }
+                    }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                    smem_u32(&mbar)));
+            }
+            const bool ok = mbar_wait(smem_u32(&mbar), phase);
+            phase ^= 1;
+            if (!__all_sync(0xffffffffu, ok)) {
+                if ((tid & 31) == 0) {
+                    atomicExch(status, 1);
+                    abort_s = 1;
+                }
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            __syncthreads();
+            if (abort_s) break;
+            // B is free: fetch the next round's U (or round 0's, for the next tile)
+            load_u(r + 1 < p.nrounds ? r + 1 : 0);
+            // ---- epilogue: D -> next operand (or natural layout after the last round) ----
+            float v[64];
+            tmem_ld64(tmem + (uint32_t(32 * (warp & 3)) << 16) + uint32_t((warp >> 2) * 64), v);
+            const int g = tid;   // row of this round (warps 0-3: rows 0-127, warps 4-7: rows 128-255)
+            const int8_t *rx = p.rax[r];
+            const int a0 = rx[0], a1 = rx[1], a2 = rx[2];
+            const int gb = ins0(ins0(ins0(g, a0), a1), a2);   // tile index bits of this group
+            __syncthreads();   // every thread has read TMEM and the old operand is consumed
+            if (r + 1 < p.nrounds) {
+                const int8_t *nx = p.rax[r + 1];
+                uint32_t base = 0;
+                for (int a = 0; a < kAxes; ++a) {
+                    const int dg = (gb >> (2 * a)) & 3;
+                    if (dg & 1) base += bit_contrib(nx, a, 0);
+                    if (dg & 2) base += bit_contrib(nx, a, 1);
+                }
+                uint32_t c0[4], c1[4], c2[4];
+                {
+                    const uint32_t x0 = bit_contrib(nx, a0, 0), y0 = bit_contrib(nx, a0, 1);
+                    const uint32_t x1 = bit_contrib(nx, a1, 0), y1 = bit_contrib(nx, a1, 1);
+                    const uint32_t x2 = bit_contrib(nx, a2, 0), y2 = bit_contrib(nx, a2, 1);
+                    c0[0] = 0; c0[1] = x0; c0[2] = y0; c0[3] = x0 + y0;
+                    c1[0] = 0; c1[1] = x1; c1[2] = y1; c1[3] = x1 + y1;
+                    c2[0] = 0; c2[1] = x2; c2[2] = y2; c2[3] = x2 + y2;
+                }
+#pragma unroll
+                for (int j = 0; j < 64; ++j) {
+                    const uint32_t o = base + c0[j & 3] + c1[(j >> 2) & 3] + c2[j >> 4];
+                    const float h = tf32_rn(v[j]);
+                    *reinterpret_cast<float *>(AH + o) = h;
+                    *reinterpret_cast<float *>(AL + o) = v[j] - h;
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            } else {
+                // natural layout into AH (the operand space is free after the last round)
+                float *out = reinterpret_cast<float *>(AH);
+                const int pb = nat_swz(gb);
+                int t0s[4], t1s[4], t2s[4];
+#pragma unroll
+                for (int d = 0; d < 4; ++d) {
+                    t0s[d] = nat_swz(d << (2 * a0));
+                    t1s[d] = nat_swz(d << (2 * a1));
+                    t2s[d] = nat_swz(d << (2 * a2));
+                }
+#pragma unroll
+                for (int j = 0; j < 64; ++j) out[pb ^ t0s[j & 3] ^ t1s[(j >> 2) & 3] ^ t2s[j >> 4]] = v[j];
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        }
+        if (abort_s) break;
+        __syncthreads();
+        // ---- write the tile back with 128-bit stores ----
+        {
+            float *dst = st + tile_base(t) + off_tid;
+            const float *out = reinterpret_cast<const float *>(AH);
+#pragma unroll
+            for (int i = 0; i < kTile / 4 / kThreads; ++i) {
+                const int e = 4 * (tid + kThreads * i);
+                *reinterpret_cast<float4 *>(dst + hi_off[i]) = *reinterpret_cast<const float4 *>(out + nat_swz(e));
+            }
+        }
+        // the next iteration's barrier orders these reads before AH is rewritten
+    }
+    cp_async_wait_all();
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(kTmemCols));
+}
+
+}  // namespace tc
+
+}  // namespace dmg
+
+using namespace dmg;
+
+extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_pass *pass, const float *umats_dev,
+                                size_t umats_count, int *status_dev, void *stream) {
+    DM_CHECK_ARG(state_dev && pass && umats_dev && status_dev && valid_n(n));
+    if (reinterpret_cast<uintptr_t>(state_dev) & 15 || reinterpret_cast<uintptr_t>(umats_dev) & 15) return DM_ERR_ARG;
+    if (n < tc::kAxes || pass->k != tc::kAxes) return DM_ERR_PROGRAM;
+    const int nr = pass->nrounds;
+    if (nr < 1 || nr > DM_MAX_ROUNDS) return DM_ERR_PROGRAM;
+    tc::Pass p;
+    bool resident[DM_MAX_QUBITS] = {false};
+    for (int r = 0; r < tc::kAxes; ++r) {
+        const int q = pass->axes[r];
+        if (q < 0 || q >= n || (r > 0 && q >= pass->axes[r - 1])) return DM_ERR_PROGRAM;
+        resident[q] = true;
+        p.res_stride[r] = axis_stride(n, q);
+    }
+    int low = 0;
+    while (low < tc::kAxes && pass->axes[low] == n - 1 - low) ++low;
+    if (low < 1) return DM_ERR_PROGRAM;   // 16-byte chunks need the lowest axis resident
+    p.low = low;
+    p.n = n;
+    p.m = n - tc::kAxes;
+    int m = 0;
+    for (int q = n - 1; q >= 0; --q)
+        if (!resident[q]) p.nonres_stride[m++] = axis_stride(n, q);
+    for (int u = m; u < DM_MAX_QUBITS; ++u) p.nonres_stride[u] = 0;
+    p.nrounds = nr;
+    for (int r = 0; r < nr; ++r) {
+        int last = -1;
+        for (int i = 0; i < 3; ++i) {
+            const int a = pass->round_axes[r][i];
+            if (a <= last || a >= tc::kAxes) return DM_ERR_PROGRAM;
+            last = a;
+            p.rax[r][i] = int8_t(a);
+        }
+        p.rax[r][3] = -1;
+        const int32_t off = pass->round_moff[r];
+        if (off < 0 || (off & 3) || size_t(off) + 2 * 64 * 64 > umats_count) return DM_ERR_PROGRAM;
+        p.umoff[r] = off;
+    }
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(tc::pass_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int(tc::kSmemBytes));
+    });
+    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    const int64_t ntiles = int64_t(1) << (2 * p.m);
+    int64_t grid = sm_count();
+    if (grid > ntiles) grid = ntiles;
+    tc::pass_tc_kernel<<<int(grid), tc::kThreads, tc::kSmemBytes, as_stream(stream)>>>(
+        static_cast<float *>(state_dev), p, umats_dev, status_dev);
+    count_launch();
+    return launch_status();
+}

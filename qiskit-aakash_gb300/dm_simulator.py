@@ -30,7 +30,8 @@ Differences (the reference fails on these inputs):
 GB300 options (absent from the reference): ``precision`` ('double', the
 default and the parity form, or 'single'), ``fusion`` (fused tile passes,
 default True), ``tile_axes`` (resident axes per tile), ``register_rounds``
-(apply a pass's operations in register rounds, default True) and
+(apply a pass's operations in register rounds, default True), ``tensor_cores``
+(FP32 passes on tcgen05 as 3xTF32 64x64 transfer matrices, default True) and
 ``coefficients_to_host`` (default True; False leaves ``coeffmatrix`` /
 ``densitymatrix`` out of the result, for callers that only need the
 measurement data of a large register).
@@ -225,6 +226,7 @@ class DmSimulatorGPU(_Base):
         self._tile_axes = None
         self._coefficients_to_host = True
         self._register_rounds = True
+        self._tensor_cores = True
         self.last_run_stats = {}
         self._record_next = False
         self.recorded_state = None
@@ -316,6 +318,8 @@ class DmSimulatorGPU(_Base):
             self._fusion = bool(backend_options['fusion'])
         if 'tile_axes' in backend_options:
             self._tile_axes = int(backend_options['tile_axes'])
+        if 'tensor_cores' in backend_options:
+            self._tensor_cores = bool(backend_options['tensor_cores'])
         if 'register_rounds' in backend_options:
             self._register_rounds = bool(backend_options['register_rounds'])
         if 'coefficients_to_host' in backend_options:
@@ -551,7 +555,7 @@ class DmSimulatorGPU(_Base):
         if any(op.name == 'bfunc' for op in experiment.instructions):
             raise BasicAerError('dm_simulator does not support conditional (bfunc) operations')
         self._dev = DeviceState(n, precision=self._precision, fusion=self._fusion, tile_axes=self._tile_axes,
-                                rounds=self._register_rounds)
+                                rounds=self._register_rounds, tensor_cores=self._tensor_cores)
         if self._record_next:
             self._dev.record()
         launches0 = N.lib().dm_kernel_launch_count()

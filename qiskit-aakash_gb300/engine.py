@@ -13,7 +13,7 @@ import numpy as np
 
 from . import _native as N
 from .exceptions import BasicAerError
-from .program import Op, cx_coefficients, encode_pass, plan_passes
+from .program import TC_AXES, Op, cx_coefficients, encode_pass, encode_pass_tc, plan_passes
 
 # Tile sizes of the fused pass: 4**6 FP64 = 32 KB and 4**7 FP32 = 64 KB of
 # shared memory per tile; the two lowest qubit axes (16 contiguous
@@ -31,7 +31,7 @@ class DeviceState:
     """An n-qubit Pauli-coefficient vector on a CUDA device."""
 
     def __init__(self, n, precision='double', fusion=True, tile_axes=None, low_axes=DEFAULT_LOW_AXES,
-                 device=None, rounds=True):
+                 device=None, rounds=True, tensor_cores=True):
         torch = _torch()
         if not torch.cuda.is_available():
             raise BasicAerError('dm_simulator (GB300) needs a CUDA device; none is visible')
@@ -49,6 +49,9 @@ class DeviceState:
         self.state = torch.empty(4 ** n, dtype=self.torch_dtype, device=self.device)
         self.fusion = fusion
         self.rounds = rounds
+        # FP32 passes of 7 resident axes run on the tensor cores (3xTF32)
+        self.tensor_cores = bool(tensor_cores) and precision == 'single' and n >= TC_AXES
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.device) if self.tensor_cores else None
         self.kmax = min(tile_axes or DEFAULT_TILE_AXES[precision], N.DM_MAX_TILE_AXES)
         self.low = low_axes
         self.pending = []
@@ -132,7 +135,28 @@ class DeviceState:
             self._run_unfused(ops)
             return
         passes = plan_passes(ops, self.n, self.kmax, self.low)
-        self._run_passes(passes)
+        if self.tensor_cores:
+            self._run_passes_tc(passes)
+        else:
+            self._run_passes(passes)
+
+    def _run_passes_tc(self, passes):
+        torch = _torch()
+        umats = []
+        descs = [encode_pass_tc(p, self.n, umats) for p in passes]
+        host = np.concatenate(umats)
+        h = torch.from_numpy(host).pin_memory()
+        dev = h.to(self.device, non_blocking=True)
+        self.h2d_bytes += host.nbytes
+        mp = ctypes.c_void_p(dev.data_ptr())
+        sp = ctypes.c_void_p(self.status.data_ptr())
+        for d in descs:
+            self._call('dm_apply_pass_tc', self.ptr, self.n, ctypes.byref(d), mp, ctypes.c_size_t(host.size), sp,
+                       self.stream, keep=(d, dev))
+        self.passes_run += len(descs)
+        self._keep = (h, dev)
+        if int(self.status.item()) != 0:
+            raise BasicAerError('a tensor-core pass abandoned a bounded wait (status %d)' % int(self.status.item()))
 
     def _run_passes(self, passes):
         torch = _torch()

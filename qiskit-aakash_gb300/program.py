@@ -313,3 +313,125 @@ def encode_pass(p, mats, dtype_np, round_width=None, n=None):
         mats.append(m.astype(dtype_np))
         off += m.size
     return dp
+
+
+# ---------------------------------------------------------------------------
+# tensor-core rounds
+# ---------------------------------------------------------------------------
+
+TC_AXES = 7   # resident axes of a tensor-core pass (tiles of 4**7 FP32 coefficients)
+
+# digits (d0, d1, d2) of the 64 round indices j = d0 + 4 d1 + 16 d2
+_J = np.arange(64)
+_DIG = np.stack([_J & 3, (_J >> 2) & 3, _J >> 4])
+
+
+def _with_digit(d, pos, val):
+    out = d.copy()
+    out[pos] = val
+    return out[0] + 4 * out[1] + 16 * out[2]
+
+
+def op_matrix64(op, axes3):
+    """64x64 map of one op on the round index j (digit i <-> local axis axes3[i])."""
+    M = np.zeros((64, 64))
+    if op.kind == 'map1':
+        d = axes3.index(op.axes[0])
+        src = _DIG[d]
+        for p in range(4):
+            M[_with_digit(_DIG, d, p), _J] += op.data[p, src]
+        return M
+    da, db = axes3.index(op.axes[0]), axes3.index(op.axes[1])
+    if op.kind == 'cx':
+        m16 = cx_matrix16(op.data, op.ideal)
+    elif op.kind == 'diag2':
+        m16 = np.diag(op.data)
+    else:
+        m16 = np.asarray(op.data)
+    src = 4 * _DIG[da] + _DIG[db]
+    for dst in range(16):
+        w = m16[dst, src]
+        nz = w != 0
+        d2 = _DIG.copy()
+        d2[da] = dst >> 2
+        d2[db] = dst & 3
+        M[(d2[0] + 4 * d2[1] + 16 * d2[2])[nz], _J[nz]] += w[nz]
+    return M
+
+
+def cx_matrix16(coef, ideal):
+    """The CX transfer matrix on (control, target) Paulis, index 4*pc + pt (basicaertools.py:346-363)."""
+    c, s, c2, s2, cs = (1.0, 0.0, 1.0, 0.0, 0.0) if ideal else coef
+    M = np.eye(16)
+    rows = {
+        2: {2: s2, 14: c2, 3: -cs, 15: cs}, 14: {2: c2, 14: s2, 3: cs, 15: -cs},
+        3: {3: s2, 15: c2, 2: cs, 14: -cs}, 15: {3: c2, 15: s2, 2: -cs, 14: cs},
+        4: {5: c, 8: -s}, 5: {4: c, 9: -s}, 6: {10: -s, 11: c}, 7: {10: -c, 11: -s},
+        8: {4: s, 9: c}, 9: {5: s, 8: c}, 10: {6: s, 7: -c}, 11: {6: c, 7: s},
+    }
+    for r, ent in rows.items():
+        M[r, :] = 0
+        for col, v in ent.items():
+            M[r, col] = v
+    return M
+
+
+def _tf32_rn(x32):
+    u = np.ascontiguousarray(x32, dtype=np.float32).view(np.uint32)
+    return ((u + np.uint32(0x1000)) & np.uint32(0xFFFFE000)).view(np.float32)
+
+
+# float index of B[n][k] in the K-major core-matrix layout (LBO 128 B, SBO 2048 B)
+_N, _K = np.meshgrid(np.arange(64), np.arange(64), indexing='ij')
+_KMAJOR = ((_N % 8) * 4 + (_K % 4) + (_K // 4) * 32 + (_N // 8) * 512).reshape(-1)
+
+
+def tc_round_image(U):
+    """8192 float32: TF32-rounded hi image then lo remainder image of U (64x64, FP64)."""
+    hi = _tf32_rn(U.astype(np.float32))
+    lo = (U - hi.astype(np.float64)).astype(np.float32)
+    img = np.zeros(8192, dtype=np.float32)
+    img[_KMAJOR] = hi.reshape(-1)
+    img[4096 + _KMAJOR] = lo.reshape(-1)
+    return img
+
+
+def pad_pass(p, n, k=TC_AXES):
+    """Grow a pass's resident set to exactly k axes (adding the lowest free qubits)."""
+    axes = set(p.axes)
+    q = n - 1
+    while len(axes) < k and q >= 0:
+        axes.add(q)
+        q -= 1
+    return Pass(sorted(axes, reverse=True), p.ops)
+
+
+def encode_pass_tc(p, n, umats):
+    """DmPass for dm_apply_pass_tc: 7 resident axes, rounds with composed 64x64 images.
+
+    Appends the rounds' images to ``umats`` (list of float32 arrays); the
+    offsets are relative to the concatenation of ``umats``.
+    """
+    p = pad_pass(p, n)
+    dp = N.DmPass()
+    dp.k = len(p.axes)
+    for r, q in enumerate(p.axes):
+        dp.axes[r] = q
+    rounds = plan_rounds(p, 3)
+    if len(rounds) > N.DM_MAX_ROUNDS:
+        raise RuntimeError('pass needs %d rounds (> %d)' % (len(rounds), N.DM_MAX_ROUNDS))
+    off = sum(m.size for m in umats)
+    dp.nrounds = len(rounds)
+    dp.nops = 0
+    for ri, (axes3, rops) in enumerate(rounds):
+        U = np.eye(64)
+        for op in rops:
+            U = op_matrix64(op, axes3) @ U
+        for i in range(3):
+            dp.round_axes[ri][i] = axes3[i]
+        dp.round_axes[ri][3] = -1
+        dp.round_moff[ri] = off
+        img = tc_round_image(U)
+        umats.append(img)
+        off += img.size
+    return dp

@@ -181,3 +181,59 @@ def test_init_product(torch, n):
     for q in range(n):
         ref = np.kron(ref, vecs[q])
     np.testing.assert_allclose(t.cpu().numpy(), ref * 0.5 ** n, rtol=1e-15, atol=0)
+
+
+@pytest.mark.parametrize('n', [7, 8, 10])
+def test_tensor_core_pass_equals_program_order(torch, n):
+    """dm_apply_pass_tc (3xTF32 tcgen05 rounds) against the ops applied one by one in FP64."""
+    from test_planner import apply_op, random_ops
+    rng = np.random.default_rng(3000 + n)
+    ops = random_ops(rng, n, 60)
+    for op in ops:
+        if op.kind == 'map1':
+            op.data = op.data / np.abs(op.data).sum(axis=1, keepdims=True)
+        elif op.kind == 'diag2':
+            op.data = np.clip(op.data, -1, 1)
+        elif op.kind == 'map2':
+            op.data = op.data / np.abs(op.data).sum(axis=1, keepdims=True)
+    st = rng.normal(size=4 ** n)
+    ref = st.copy()
+    for op in ops:
+        ref = apply_op(ref, n, op)
+    passes = P.plan_passes(ops, n, 7, 2)
+    umats = []
+    descs = [P.encode_pass_tc(p, n, umats) for p in passes]
+    m = np.concatenate(umats)
+    md = dev(torch, m, np.float32)
+    t = dev(torch, st, np.float32)
+    status = torch.zeros(1, dtype=torch.int32, device='cuda')
+    for d in descs:
+        N.call('dm_apply_pass_tc', vp(t), n, ctypes.byref(d), vp(md), ctypes.c_size_t(m.size), vp(status),
+               stream(torch))
+    got = t.double().cpu().numpy()
+    assert status.item() == 0
+    np.testing.assert_allclose(got, ref, rtol=0, atol=2e-5 * np.abs(ref).max())
+
+
+def test_tensor_core_pass_rejects_bad_programs(torch):
+    n = 8
+    t = torch.zeros(4 ** n, dtype=torch.float32, device='cuda')
+    u = torch.zeros(8192, dtype=torch.float32, device='cuda')
+    status = torch.zeros(1, dtype=torch.int32, device='cuda')
+    d = N.DmPass()
+    d.k = 6                                  # a tensor-core pass holds exactly 7 axes
+    for r, q in enumerate(range(n - 1, n - 7, -1)):
+        d.axes[r] = q
+    d.nrounds = 1
+    rc = N.lib().dm_apply_pass_tc(vp(t), n, ctypes.byref(d), vp(u), 8192, vp(status), stream(torch))
+    assert rc == N.DM_ERR_PROGRAM
+    d.k = 7
+    for r, q in enumerate(range(n - 1, n - 8, -1)):
+        d.axes[r] = q
+    d.round_axes[0][0], d.round_axes[0][1], d.round_axes[0][2] = 0, 2, 1   # not ascending
+    rc = N.lib().dm_apply_pass_tc(vp(t), n, ctypes.byref(d), vp(u), 8192, vp(status), stream(torch))
+    assert rc == N.DM_ERR_PROGRAM
+    d.round_axes[0][0], d.round_axes[0][1], d.round_axes[0][2] = 0, 1, 2
+    d.round_moff[0] = 4                      # image would overrun the 8192-float buffer
+    rc = N.lib().dm_apply_pass_tc(vp(t), n, ctypes.byref(d), vp(u), 8192, vp(status), stream(torch))
+    assert rc == N.DM_ERR_PROGRAM

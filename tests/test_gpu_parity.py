@@ -92,7 +92,8 @@ def test_workloads_match_oracle(n, layers, seed, every_gate, qft):
     ref = _oracle(qc.to_experiment(), opts)
     for kw, tol in (({}, 1e-12), ({'tile_axes': 7}, 1e-12), ({'tile_axes': 4}, 1e-12),
                     ({'register_rounds': False}, 1e-12), ({'precision': 'single'}, 2e-5),
-                    ({'precision': 'single', 'register_rounds': False}, 2e-5)):
+                    ({'precision': 'single', 'tensor_cores': False}, 2e-5),
+                    ({'precision': 'single', 'tensor_cores': False, 'register_rounds': False}, 2e-5)):
         got, b = run_gpu(qc.to_experiment(), opts, **kw)
         assert got['number_of_clock_cycles'] == ref['number_of_clock_cycles']
         _assert_close(got, ref, n, tol)
@@ -112,6 +113,8 @@ def test_fourteen_qubit_properties():
     assert b.last_run_stats['passes'] < fused['number_of_clock_cycles']
     single, _ = run_gpu(qc.to_experiment(), opts, precision='single')
     np.testing.assert_allclose(single['data']['coeffmatrix'] * 2 ** n, a * 2 ** n, rtol=0, atol=2e-5)
+    cuda_cores, _ = run_gpu(qc.to_experiment(), opts, precision='single', tensor_cores=False)
+    np.testing.assert_allclose(cuda_cores['data']['coeffmatrix'] * 2 ** n, a * 2 ** n, rtol=0, atol=2e-5)
     unfused, _ = run_gpu(qc.to_experiment(), opts, fusion=False)
     np.testing.assert_allclose(unfused['data']['coeffmatrix'] * 2 ** n, a * 2 ** n, rtol=0, atol=1e-12)
 

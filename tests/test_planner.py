@@ -189,3 +189,40 @@ def test_register_rounds_equal_program_order(n, kmax, low, width):
                 assert dp.nrounds == len(rounds)
                 assert dp.round_end[dp.nrounds - 1] == dp.nops
         np.testing.assert_allclose(got, ref, rtol=1e-10, atol=1e-10 * np.abs(ref).max())
+
+
+def test_tensor_core_round_images_equal_program_order():
+    """Composed 64x64 round matrices (as the tensor-core pass applies them) equal program order."""
+    n = 8
+    rng = np.random.default_rng(21)
+    ops = random_ops(rng, n, 50)
+    st0 = rng.normal(size=4 ** n)
+    ref = st0.copy()
+    for op in ops:
+        ref = apply_op(ref, n, op)
+    got = st0.copy()
+    for p in P.plan_passes(ops, n, 7, 2):
+        pp = P.pad_pass(p, n)
+        assert len(pp.axes) == 7 and pp.axes[0] == n - 1
+        for axes3, rops in P.plan_rounds(pp, 3):
+            U = np.eye(64)
+            for op in rops:
+                U = P.op_matrix64(op, axes3) @ U
+            qs = [pp.axes[a] for a in axes3]
+            t = np.moveaxis(got.reshape([4] * n), (qs[2], qs[1], qs[0]), (0, 1, 2)).reshape(64, -1)
+            t = (U @ t).reshape([4, 4, 4] + [4] * (n - 3))
+            got = np.moveaxis(t, (0, 1, 2), (qs[2], qs[1], qs[0])).reshape(-1)
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-10 * np.abs(ref).max())
+
+
+def test_tc_image_layout_and_split():
+    U = np.random.default_rng(2).normal(size=(64, 64))
+    img = P.tc_round_image(U)
+    hi = np.zeros((64, 64), np.float32)
+    lo = np.zeros((64, 64), np.float32)
+    hi.reshape(-1)[:] = img[P._KMAJOR]
+    lo.reshape(-1)[:] = img[4096 + P._KMAJOR]
+    assert len(set(P._KMAJOR.tolist())) == 4096
+    assert (hi.view(np.uint32) & 0x1FFF == 0).all()          # TF32: low 13 mantissa bits clear
+    # lo is FP32 of U - hi (|.| <= 2^-11 |U|): hi + lo carries U to ~2^-35 relative
+    np.testing.assert_allclose(hi.astype(np.float64) + lo, U, rtol=0, atol=1e-10 * np.abs(U).max())
