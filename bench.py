@@ -62,6 +62,7 @@ def parse():
     ap.add_argument('--fp64-steps', type=int, default=1)
     ap.add_argument('--e2e-steps', type=int, default=2)
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline sample')
+    ap.add_argument('--no-gate-kinds', action='store_true', help='skip the per-gate-kind bandwidth table')
     return ap.parse_args()
 
 
@@ -147,7 +148,7 @@ def measured_peaks():
 
 def profiled_traffic():
     """Per-launch DRAM bytes of the pass kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, 'profiles', 'pass_kernel_fp32_n16.md')
+    path = os.path.join(ROOT, 'profiles', 'pass_tc_kernel_fp32_n16.md')
     try:
         for line in open(path):
             if line.startswith('traffic_bytes_per_launch:'):
@@ -245,7 +246,7 @@ def pass_kernel_profile(torch, state):
     marks = []
 
     def on_call(name, before):
-        if name == 'dm_apply_pass':
+        if name in ('dm_apply_pass', 'dm_apply_pass_tc'):
             ev = torch.cuda.Event(enable_timing=True)
             ev.record(stream)
             marks.append(ev)
@@ -266,6 +267,68 @@ def device_max_abs_diff(torch, a32, b64, chunk=1 << 28):
     return m
 
 
+def per_gate_kind(torch, N, n=14, reps=3):
+    """HBM GB/s of each single-operation sweep at n qubits, FP64 (2 * 4**n * 8 bytes per sweep)."""
+    import ctypes
+    L = N.lib()
+    st = torch.empty(4 ** n, dtype=torch.float64, device='cuda')
+    v = np.tile(np.array([1.0, 0.0, 0.0, 1.0]), n)
+    N.call('dm_init_product', ctypes.c_void_p(st.data_ptr()), n, N.DM_F64,
+           v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 0.5 ** n, None)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ptr = ctypes.c_void_p(st.data_ptr())
+    rng = np.random.default_rng(0)
+    u3 = np.eye(4)
+    u3[1:, 1:] = np.linalg.qr(rng.normal(size=(3, 3)))[0]
+    noise = np.diag([1.0, 0.99, 0.99, 0.998])
+    noise[3, 0] = 0.001
+    out = torch.empty(2 ** n, dtype=torch.float64, device='cuda')
+    scratch = torch.empty(max(8, L.dm_nbasis_probs_scratch_bytes(n)), dtype=torch.uint8, device='cuda')
+    mode = (ctypes.c_int * n)(*([3] * n))
+    nvec = N.f64_array([0.6, 0.0, 0.8])
+    keep = []
+
+    def arr(a):
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+        keep.append(a)
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+    kinds = {
+        'u3 (4x4 map, one qubit)': (lambda: N.call('dm_apply_map1', ptr, n, N.DM_F64, n // 2, arr(u3), s), 1),
+        'memory noise (one qubit)': (lambda: N.call('dm_apply_map1', ptr, n, N.DM_F64, 0, arr(noise), s), 1),
+        'cx ideal (signed permutation)': (lambda: N.call('dm_apply_cx', ptr, n, N.DM_F64, 3, 4, arr([1.0, 0.0]), s), 1),
+        'cx with tsp error': (lambda: N.call('dm_apply_cx', ptr, n, N.DM_F64, 3, 4, arr([0.98, 0.02]), s), 1),
+        'memory noise, every qubit (n sweeps)': (
+            lambda: N.call('dm_apply_memory_noise', ptr, n, N.DM_F64, 0.995, 1.0, 0.998, s), n),
+        'ensemble Z probabilities (2^n gather + WHT)': (
+            lambda: N.call('dm_axis_probs', ptr, n, N.DM_F64, mode, 0.999, ctypes.c_void_p(out.data_ptr()), s), None),
+        'ensemble N probabilities (full contraction)': (
+            lambda: N.call('dm_nbasis_probs', ptr, n, N.DM_F64, nvec, 0.999, ctypes.c_void_p(out.data_ptr()),
+                           ctypes.c_void_p(scratch.data_ptr()), s), 0.5),
+    }
+    hbm, _ = measured_peaks()
+    res = {}
+    for name, (fn, sweeps) in kinds.items():
+        fn()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / reps
+        ent = {'ms': ms}
+        if sweeps:
+            gbs = sweeps * 2 * 4 ** n * 8 / (ms / 1e3) / 1e9
+            ent.update(gbs=gbs, frac_of_hbm=gbs / hbm)
+        res[name] = ent
+    del st, out, scratch
+    torch.cuda.empty_cache()
+    return {'n_qubits': n, 'dtype': 'f64', 'bytes_per_sweep': 2 * 4 ** n * 8, 'kinds': res}
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_setup(args)
@@ -280,14 +343,25 @@ def run_ours(args):
     seed = args.seed + rank
     qc, opts = workload(pkg, n, layers, seed)
 
-    def backend_for(precision):
+    def backend_for(precision, tensor_cores=True):
         DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
         b = DmSimulatorGPU()
         o = copy.deepcopy(opts)
         o['precision'] = precision
+        o['tensor_cores'] = tensor_cores
         o['coefficients_to_host'] = False      # compared on the device below
         b._set_options(backend_options=o)
         return b
+
+    # --- FP32 on the CUDA cores (the register-round kernel), for comparison ----
+    bcc = backend_for('single', tensor_cores=False)
+    bcc.record_experiment(qc.to_experiment())
+    stcc = bcc.recorded_state
+    stcc.replay()
+    ms_cc = time_replays(torch, stcc, 1)
+    durs_cc = pass_kernel_profile(torch, stcc)
+    del stcc, bcc
+    torch.cuda.empty_cache()
 
     # --- fused FP32: record once, then time replays ---------------------------
     b32 = backend_for('single')
@@ -371,11 +445,15 @@ def run_ours(args):
                        'fused_passes': stats64['passes'], 'mean_pass_ms': mean_pass64,
                        'pass_achieved_gbs': achieved64, 'pass_frac_of_hbm': achieved64 / hbm},
         'fp32_over_fp64': ms64 / ms32,
+        'fp32_cuda_cores': {'value': world * layers / (ms_cc / 1e3), 'unit': 'gate-layers/s', 'ms_per_step': ms_cc,
+                            'kernel': 'pass_pipe_kernel<float,3>',
+                            'mean_pass_ms': float(np.mean(durs_cc)) if durs_cc else None,
+                            'pass_achieved_gbs': (2 * N4 * 4 / (float(np.mean(durs_cc)) / 1e3) / 1e9) if durs_cc else None},
         'accuracy': {'max_abs_coeff_err': max_abs, 'prob_l1_err': prob_l1,
                      'against': 'FP64 GPU plain form (itself parity-checked against the reference at n<=14)',
                      'coeff_scale': 'Pauli expectations 2^n * a_s'},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s', 'frac': achieved / hbm,
-                     'traffic': traffic, 'kernel': 'pass_kernel<float>', 'launches_per_step': len(durs),
+                     'traffic': traffic, 'kernel': 'pass_tc_kernel (tcgen05 3xTF32)', 'launches_per_step': len(durs),
                      'mean_launch_ms': mean_pass_ms,
                      'algorithmic_bytes_per_launch': 2 * N4 * 4, 'peak_kind': peak_kind},
         'e2e': {'value': world * layers / e2e_s, 'unit': 'gate-layers/s', 'seconds_per_step': e2e_s,
@@ -384,6 +462,8 @@ def run_ours(args):
         'gpu_launches': int(launches),
         'clocks': clocks.summary(),
     }
+    if not args.no_gate_kinds:
+        line['per_gate_kind_fp64'] = per_gate_kind(torch, N)
     if not args.no_cpu:
         line['cpu_baseline'] = cpu_sample(pkg, n, args.seed)
     return line
