@@ -83,11 +83,6 @@ typedef struct dm_pass {
     int8_t round_axes[DM_MAX_ROUNDS][4];
     int16_t round_end[DM_MAX_ROUNDS];
     dm_op ops[DM_MAX_PASS_OPS];
-    /* dm_apply_pass_tc only: float offset of round r's transfer-matrix image
-     * (the 64x64 map of the round's composed ops, as 4096 TF32-rounded "hi"
-     * floats then 4096 "lo" remainder floats, each in the K-major core-matrix
-     * order (n%8)*4 + k%4 + (k/4)*32 + (n/8)*512 for output n, input k). */
-    int32_t round_moff[DM_MAX_ROUNDS];
 } dm_pass;
 
 /* Round width (axes held in registers per round) for a dtype. */
@@ -134,15 +129,40 @@ int dm_apply_memory_noise(void *state_dev, int n, int dtype, double f, double p,
 int dm_apply_pass(void *state_dev, int n, int dtype, const dm_pass *pass, const void *mats_dev,
                   size_t mats_count, void *stream);
 
-/* The fused pass on the tensor cores (FP32 state only).  The pass must hold
- * exactly 7 resident axes including the lowest qubit axis, and n >= 7; its
- * rounds (round_axes[r][0..2], 3 local axes each) are applied as 64x64
- * transfer matrices (round_moff[r] into umats_dev, umats_count floats) by
- * tcgen05.mma kind::tf32 in 3xTF32 (hi/lo split of state and matrix, FP32
- * accumulation in tensor memory).  The ops list is not read.  status_dev
- * (device int, 0 before the first call) is set to 1 if the kernel abandons a
- * bounded wait.  Same role as dm_apply_pass (dm_simulator.py:1005-1177). */
-int dm_apply_pass_tc(void *state_dev, int n, const dm_pass *pass, const float *umats_dev, size_t umats_count,
+/* A tensor-core pass.  Every tile of 4**7 coefficients (the 7 resident
+ * axes) is viewed, round by round, as a 256 x 64 operand: rows are groups,
+ * K the 64 coefficients of the round's 3 axes, stored in the K-major
+ * core-matrix layout byte(row, k) = (row%8)*16 + (k%4)*4 + (k/4)*128 +
+ * (row/8)*2048.  A round is D = X U^T with U the 64x64 transfer matrix of
+ * its composed operations.  Layout offsets are XOR-combinations of one
+ * offset per index bit (every operand-layout bit contributes a distinct
+ * power of two, and the natural tile layout is XOR-linear). */
+typedef struct dm_tc_round {
+    int8_t digits[3];     /* local axes of K digits 0, 1, 2 (j = d0 + 4 d1 + 16 d2) */
+    int8_t vec;           /* digit whose 4 values this round's epilogue stores as one 128-bit vector, or -1 */
+    int32_t umoff;        /* float offset of the round's matrix image: 4096 TF32-rounded hi floats then 4096
+                             lo remainders, float (n%8)*4 + k%4 + (k/4)*32 + (n/8)*512 for output n, input k */
+    uint32_t rowc[8];     /* destination offset of row bit i of this round: bytes into the next round's
+                             operand, or, after the last round, elements of the natural tile */
+    uint32_t kc[6];       /* destination offset of K bit i of this round */
+} dm_tc_round;
+
+typedef struct dm_tc_pass {
+    int32_t axes[7];      /* resident qubits, strictly decreasing; axes[0] must be n-1 */
+    int32_t nrounds;
+    int8_t vec0;          /* 0 when round 0's digit 0 is local axis 0 (128-bit conversion loads), else -1 */
+    int8_t pad[3];
+    uint32_t natrow[8];   /* natural-tile element offset of round 0's row bit i */
+    uint32_t natk[6];     /* natural-tile element offset of round 0's K bit i */
+    dm_tc_round rounds[DM_MAX_ROUNDS];
+} dm_tc_pass;
+
+/* The fused pass on the tensor cores (FP32 state only, n >= 7): the rounds
+ * run as tcgen05.mma kind::tf32 in 3xTF32 (hi/lo split of state and matrix,
+ * FP32 accumulation in tensor memory).  umats_dev holds umats_count floats.
+ * status_dev (device int, 0 before the first call) is set to 1 if the kernel
+ * abandons a bounded wait.  Same role as dm_apply_pass (dm_simulator.py:1005-1177). */
+int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, const float *umats_dev, size_t umats_count,
                      int *status_dev, void *stream);
 
 /* ---------------------------------------------------------------- measurement */

@@ -92,8 +92,18 @@ class DmPass(ctypes.Structure):
                 ('nops', ctypes.c_int32), ('nrounds', ctypes.c_int32),
                 ('round_axes', (ctypes.c_int8 * 4) * DM_MAX_ROUNDS),
                 ('round_end', ctypes.c_int16 * DM_MAX_ROUNDS),
-                ('ops', DmOp * DM_MAX_PASS_OPS),
-                ('round_moff', ctypes.c_int32 * DM_MAX_ROUNDS)]
+                ('ops', DmOp * DM_MAX_PASS_OPS)]
+
+
+class DmTcRound(ctypes.Structure):
+    _fields_ = [('digits', ctypes.c_int8 * 3), ('vec', ctypes.c_int8), ('umoff', ctypes.c_int32),
+                ('rowc', ctypes.c_uint32 * 8), ('kc', ctypes.c_uint32 * 6)]
+
+
+class DmTcPass(ctypes.Structure):
+    _fields_ = [('axes', ctypes.c_int32 * 7), ('nrounds', ctypes.c_int32), ('vec0', ctypes.c_int8),
+                ('pad', ctypes.c_int8 * 3), ('natrow', ctypes.c_uint32 * 8), ('natk', ctypes.c_uint32 * 6),
+                ('rounds', DmTcRound * DM_MAX_ROUNDS)]
 
 
 _vp = ctypes.c_void_p
@@ -111,7 +121,7 @@ SIGNATURES = {
     'dm_apply_cx': (_i, [_vp, _i, _i, _i, _i, _dp, _vp]),
     'dm_apply_memory_noise': (_i, [_vp, _i, _i, _d, _d, _d, _vp]),
     'dm_apply_pass': (_i, [_vp, _i, _i, ctypes.POINTER(DmPass), _vp, _sz, _vp]),
-    'dm_apply_pass_tc': (_i, [_vp, _i, ctypes.POINTER(DmPass), _vp, _sz, _vp, _vp]),
+    'dm_apply_pass_tc': (_i, [_vp, _i, ctypes.POINTER(DmTcPass), _vp, _sz, _vp, _vp]),
     'dm_axis_probs': (_i, [_vp, _i, _i, _ip, _d, _vp, _vp]),
     'dm_nbasis_probs_scratch_bytes': (_sz, [_i]),
     'dm_nbasis_probs': (_i, [_vp, _i, _i, _dp, _d, _vp, _vp, _vp]),

@@ -75,10 +75,6 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // Natural-layout swizzle of the tile (16-byte chunks intact), as in dm_pass.cu.
 __device__ __forceinline__ int nat_swz(int e) { return e ^ ((((e >> 5) ^ (e >> 8)) & 7) << 2); }
 
-__device__ __forceinline__ int ins0(int g, int pos) {
-    return ((g >> (2 * pos)) << (2 * pos + 2)) | (g & ((1 << (2 * pos)) - 1));
-}
-
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     for (int it = 0; it < kSpinLimit; ++it) {
         uint32_t ok;
@@ -92,12 +88,21 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     return false;
 }
 
+struct Round {
+    int8_t digits[3];
+    int8_t vec;
+    int32_t umoff;
+    uint32_t rowc[8];
+    uint32_t kc[6];
+};
+
 struct Pass {
     int n, m, low, nrounds;
+    int vec0;
     int64_t res_stride[kAxes];
     int64_t nonres_stride[DM_MAX_QUBITS];
-    int8_t rax[DM_MAX_ROUNDS][4];
-    int32_t umoff[DM_MAX_ROUNDS];   // float offset of round r's U image (hi 4096 floats, then lo 4096)
+    uint32_t natrow[8], natk[6];
+    Round rounds[DM_MAX_ROUNDS];
 };
 
 __device__ __forceinline__ int64_t tile_offset(const Pass &p, int e) {
@@ -106,18 +111,25 @@ __device__ __forceinline__ int64_t tile_offset(const Pass &p, int e) {
     return off;
 }
 
-// Byte offset, in round r's operand layout, of the contribution of one set
-// bit: local axis a, digit bit b (value 1 << b).  Offsets are additive over
-// elements with disjoint bits (row_off and k_off are linear in their bits).
-__device__ __forceinline__ uint32_t bit_contrib(const int8_t *rax, int a, int b) {
-    int k_digit = -1;
-    for (int i = 0; i < 3; ++i)
-        if (rax[i] == a) k_digit = i;
-    if (k_digit >= 0) return k_off((1 << b) << (2 * k_digit));
-    int c = 0;   // rank of a among the non-round axes = its digit in the group (row) index
-    for (int x = 0; x < a; ++x)
-        if (x != rax[0] && x != rax[1] && x != rax[2]) ++c;
-    return row_off((1 << b) << (2 * c));
+// XOR-combination of the offsets of the set bits of x (nbits of them).
+template <int NB>
+__device__ __forceinline__ uint32_t xor_bits(uint32_t x, const uint32_t *c) {
+    uint32_t o = 0;
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+        if ((x >> i) & 1) o ^= c[i];
+    return o;
+}
+
+// Per-digit XOR tables of the 64 K indices: k -> t0[d0] ^ t1[d1] ^ t2[d2].
+__device__ __forceinline__ void digit_tables(const uint32_t *kc, uint32_t (&t)[3][4]) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        t[d][0] = 0;
+        t[d][1] = kc[2 * d];
+        t[d][2] = kc[2 * d + 1];
+        t[d][3] = kc[2 * d] ^ kc[2 * d + 1];
+    }
 }
 
 __device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
@@ -141,6 +153,61 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
     for (int j = 0; j < 64; ++j) v[j] = __uint_as_float(r[j]);
 }
 
+__device__ __forceinline__ void put_split(unsigned char *AH, unsigned char *AL, uint32_t o, float x) {
+    const float h = tf32_rn(x);
+    *reinterpret_cast<float *>(AH + o) = h;
+    *reinterpret_cast<float *>(AL + o) = x - h;
+}
+
+__device__ __forceinline__ void put_split4(unsigned char *AH, unsigned char *AL, uint32_t o, float a, float b,
+                                           float c, float d) {
+    const float ha = tf32_rn(a), hb = tf32_rn(b), hc = tf32_rn(c), hd = tf32_rn(d);
+    *reinterpret_cast<float4 *>(AH + o) = make_float4(ha, hb, hc, hd);
+    *reinterpret_cast<float4 *>(AL + o) = make_float4(a - ha, b - hb, c - hc, d - hd);
+}
+
+// Epilogue stores of one thread's 64 values (K index j = d0 + 4 d1 + 16 d2)
+// at base ^ t[0][d0] ^ t[1][d1] ^ t[2][d2].  With a vector digit D the four
+// values along D are adjacent in the destination: one 128-bit store.
+template <int D, bool SPLIT>
+__device__ __forceinline__ void store_vec(const float (&v)[64], uint32_t base, const uint32_t (&t)[3][4],
+                                          unsigned char *AH, unsigned char *AL) {
+    constexpr int S = 1 << (2 * D);
+    constexpr int X = D == 0 ? 1 : 0, Y = D == 2 ? 1 : 2;   // the two other digits
+#pragma unroll
+    for (int x = 0; x < 4; ++x)
+#pragma unroll
+        for (int y = 0; y < 4; ++y) {
+            const int j0 = (x << (2 * X)) | (y << (2 * Y));
+            const uint32_t o = base ^ t[X][x] ^ t[Y][y];
+            if (SPLIT)
+                put_split4(AH, AL, o, v[j0], v[j0 + S], v[j0 + 2 * S], v[j0 + 3 * S]);
+            else
+                *reinterpret_cast<float4 *>(AH + 4 * o) = make_float4(v[j0], v[j0 + S], v[j0 + 2 * S], v[j0 + 3 * S]);
+        }
+}
+
+template <bool SPLIT>
+__device__ __forceinline__ void store_all(const float (&v)[64], int vec, uint32_t base, const uint32_t (&t)[3][4],
+                                          unsigned char *AH, unsigned char *AL) {
+    if (vec == 0) {
+        store_vec<0, SPLIT>(v, base, t, AH, AL);
+    } else if (vec == 1) {
+        store_vec<1, SPLIT>(v, base, t, AH, AL);
+    } else if (vec == 2) {
+        store_vec<2, SPLIT>(v, base, t, AH, AL);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 64; ++j) {
+            const uint32_t o = base ^ t[0][j & 3] ^ t[1][(j >> 2) & 3] ^ t[2][j >> 4];
+            if (SPLIT)
+                put_split(AH, AL, o, v[j]);
+            else
+                reinterpret_cast<float *>(AH)[o] = v[j];
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict__ st, const __grid_constant__ Pass p,
                                                               const float *__restrict__ umats, int *status) {
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -148,7 +215,6 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
     unsigned char *AH = smem + kNatBytes;
     unsigned char *AL = AH + kABytes;
     unsigned char *BH = AL + kABytes;
-    unsigned char *BL = BH + kBBytes;
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base_s;
     __shared__ int64_t hi_off[16];
@@ -156,7 +222,6 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int64_t ntiles = int64_t(1) << (2 * p.m);
-    // natural-layout chunk c = tid + 256 i (4 floats each): offset additive over tid / i bits
     const int64_t off_tid = tile_offset(p, 4 * tid);
     if (tid < 16) hi_off[tid] = tile_offset(p, 4 * kThreads * tid);
     if (tid == 0) {
@@ -174,6 +239,9 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_s;
     uint32_t phase = 0;
+    // this thread's row in every round (warps 0-3: rows 0-127 = M block 0, warps 4-7: M block 1)
+    const uint32_t row = uint32_t(tid);
+    const uint32_t row_bytes = row_off(int(row));
 
     auto tile_base = [&](int64_t t) {
         int64_t base = 0;
@@ -192,11 +260,11 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
         }
         cp_async_commit();
     };
-    auto load_u = [&](int r) {          // round r's U images into BH / BL
-        const float *src = umats + p.umoff[r];
+    auto load_u = [&](int r) {          // round r's U images into BH / BL (contiguous)
+        const float *src = umats + p.rounds[r].umoff;
 #pragma unroll
         for (int i = 0; i < 2 * 64 * 64 / 4 / kThreads; ++i) {
-            const int c = tid + kThreads * i;   // 16-byte chunk; BH and BL are contiguous
+            const int c = tid + kThreads * i;
             cp_async16(BH + 16 * c, src + 4 * c);
         }
         cp_async_commit();
@@ -209,29 +277,27 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
         cp_async_wait_all();
         __syncthreads();
         if (abort_s) break;
-        // ---- convert the natural tile into round 0's operand (hi / lo) ----
+        // ---- natural tile -> round 0's operand (hi / lo) ----
         {
-            const int8_t *rx = p.rax[0];
-            const int a0 = rx[0], a1 = rx[1], a2 = rx[2];
-            int gb = ins0(ins0(ins0(tid, a0), a1), a2);
-            const int pb = nat_swz(gb);
-            const uint32_t ro = row_off(tid);
-            int t0s[4], t1s[4], t2s[4];
-#pragma unroll
-            for (int d = 0; d < 4; ++d) {
-                t0s[d] = nat_swz(d << (2 * a0));
-                t1s[d] = nat_swz(d << (2 * a1));
-                t2s[d] = nat_swz(d << (2 * a2));
-            }
+            const uint32_t nb = xor_bits<8>(row, p.natrow);
+            uint32_t tn[3][4], tk[3][4];
+            digit_tables(p.natk, tn);
             const float *nat = reinterpret_cast<const float *>(NAT);
+            if (p.vec0 == 0) {
+                // digit 0 is local axis 0: four adjacent natural elements = four adjacent K
 #pragma unroll
-            for (int j = 0; j < 64; ++j) {
-                const float x = nat[pb ^ t0s[j & 3] ^ t1s[(j >> 2) & 3] ^ t2s[j >> 4]];
-                const float h = tf32_rn(x);
-                const uint32_t o = ro + k_off(j);
-                *reinterpret_cast<float *>(AH + o) = h;
-                *reinterpret_cast<float *>(AL + o) = x - h;
+                for (int x = 0; x < 4; ++x)
+#pragma unroll
+                    for (int y = 0; y < 4; ++y) {
+                        const float4 q = *reinterpret_cast<const float4 *>(nat + (nb ^ tn[1][x] ^ tn[2][y]));
+                        put_split4(AH, AL, row_bytes + k_off(4 * x + 16 * y), q.x, q.y, q.z, q.w);
+                    }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 64; ++j)
+                    put_split(AH, AL, row_bytes + k_off(j), nat[nb ^ tn[0][j & 3] ^ tn[1][(j >> 2) & 3] ^ tn[2][j >> 4]]);
             }
+            (void)tk;
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
@@ -244,7 +310,7 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (tid == 0) {
-                const uint32_t ah = smem_u32(AH), al = smem_u32(AL), bh = smem_u32(BH), bl = smem_u32(BL);
+                const uint32_t ah = smem_u32(AH), al = smem_u32(AL), bh = smem_u32(BH), bl = bh + kBBytes;
 #pragma unroll
                 for (int mb = 0; mb < 2; ++mb) {
                     const uint32_t d = tmem + mb * 64;
@@ -281,52 +347,18 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
             if (abort_s) break;
             // B is free: fetch the next round's U (or round 0's, for the next tile)
             load_u(r + 1 < p.nrounds ? r + 1 : 0);
-            // ---- epilogue: D -> next operand (or natural layout after the last round) ----
+            // ---- epilogue: D -> next operand (hi / lo), or the natural tile after the last round ----
             float v[64];
             tmem_ld64(tmem + (uint32_t(32 * (warp & 3)) << 16) + uint32_t((warp >> 2) * 64), v);
-            const int g = tid;   // row of this round (warps 0-3: rows 0-127, warps 4-7: rows 128-255)
-            const int8_t *rx = p.rax[r];
-            const int a0 = rx[0], a1 = rx[1], a2 = rx[2];
-            const int gb = ins0(ins0(ins0(g, a0), a1), a2);   // tile index bits of this group
-            __syncthreads();   // every thread has read TMEM and the old operand is consumed
+            const Round &R = p.rounds[r];
+            uint32_t tk[3][4];
+            digit_tables(R.kc, tk);
+            const uint32_t base = xor_bits<8>(row, R.rowc);
             if (r + 1 < p.nrounds) {
-                const int8_t *nx = p.rax[r + 1];
-                uint32_t base = 0;
-                for (int a = 0; a < kAxes; ++a) {
-                    const int dg = (gb >> (2 * a)) & 3;
-                    if (dg & 1) base += bit_contrib(nx, a, 0);
-                    if (dg & 2) base += bit_contrib(nx, a, 1);
-                }
-                uint32_t c0[4], c1[4], c2[4];
-                {
-                    const uint32_t x0 = bit_contrib(nx, a0, 0), y0 = bit_contrib(nx, a0, 1);
-                    const uint32_t x1 = bit_contrib(nx, a1, 0), y1 = bit_contrib(nx, a1, 1);
-                    const uint32_t x2 = bit_contrib(nx, a2, 0), y2 = bit_contrib(nx, a2, 1);
-                    c0[0] = 0; c0[1] = x0; c0[2] = y0; c0[3] = x0 + y0;
-                    c1[0] = 0; c1[1] = x1; c1[2] = y1; c1[3] = x1 + y1;
-                    c2[0] = 0; c2[1] = x2; c2[2] = y2; c2[3] = x2 + y2;
-                }
-#pragma unroll
-                for (int j = 0; j < 64; ++j) {
-                    const uint32_t o = base + c0[j & 3] + c1[(j >> 2) & 3] + c2[j >> 4];
-                    const float h = tf32_rn(v[j]);
-                    *reinterpret_cast<float *>(AH + o) = h;
-                    *reinterpret_cast<float *>(AL + o) = v[j] - h;
-                }
+                store_all<true>(v, R.vec, base, tk, AH, AL);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             } else {
-                // natural layout into AH (the operand space is free after the last round)
-                float *out = reinterpret_cast<float *>(AH);
-                const int pb = nat_swz(gb);
-                int t0s[4], t1s[4], t2s[4];
-#pragma unroll
-                for (int d = 0; d < 4; ++d) {
-                    t0s[d] = nat_swz(d << (2 * a0));
-                    t1s[d] = nat_swz(d << (2 * a1));
-                    t2s[d] = nat_swz(d << (2 * a2));
-                }
-#pragma unroll
-                for (int j = 0; j < 64; ++j) out[pb ^ t0s[j & 3] ^ t1s[(j >> 2) & 3] ^ t2s[j >> 4]] = v[j];
+                store_all<false>(v, R.vec, base, tk, AH, AL);   // natural layout into AH
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         }
@@ -356,14 +388,40 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
 
 using namespace dmg;
 
-extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_pass *pass, const float *umats_dev,
+// Offsets must be distinct powers of two (operand) so that their XOR stays inside
+// a 64 KB operand region, or natural-tile element offsets below 4**7.
+static bool valid_tables(const uint32_t *rowc, const uint32_t *kc, int vec, bool natural) {
+    uint32_t seen = 0;
+    for (int i = 0; i < 14; ++i) {
+        const uint32_t c = i < 8 ? rowc[i] : kc[i - 8];
+        if (natural) {
+            if (c == 0 || c >= uint32_t(tc::kTile)) return false;
+        } else {
+            if (c == 0 || (c & (c - 1)) || c >= tc::kABytes || (seen & c)) return false;
+            seen |= c;
+        }
+    }
+    if (vec >= 0) {
+        if (vec > 2) return false;
+        const uint32_t lo = natural ? 1 : 4, hi = natural ? 2 : 8, align = natural ? 4 : 16;
+        if (kc[2 * vec] != lo || kc[2 * vec + 1] != hi) return false;
+        for (int i = 0; i < 14; ++i) {   // the other bits keep 16-byte alignment
+            if (i >= 8 && (i - 8) / 2 == vec) continue;
+            const uint32_t c = i < 8 ? rowc[i] : kc[i - 8];
+            if (c % align) return false;
+        }
+    }
+    return true;
+}
+
+extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, const float *umats_dev,
                                 size_t umats_count, int *status_dev, void *stream) {
     DM_CHECK_ARG(state_dev && pass && umats_dev && status_dev && valid_n(n));
     if (reinterpret_cast<uintptr_t>(state_dev) & 15 || reinterpret_cast<uintptr_t>(umats_dev) & 15) return DM_ERR_ARG;
-    if (n < tc::kAxes || pass->k != tc::kAxes) return DM_ERR_PROGRAM;
+    if (n < tc::kAxes) return DM_ERR_PROGRAM;
     const int nr = pass->nrounds;
     if (nr < 1 || nr > DM_MAX_ROUNDS) return DM_ERR_PROGRAM;
-    tc::Pass p;
+    static thread_local tc::Pass p;   // ~3.5 KB: keep it off the host stack
     bool resident[DM_MAX_QUBITS] = {false};
     for (int r = 0; r < tc::kAxes; ++r) {
         const int q = pass->axes[r];
@@ -382,18 +440,24 @@ extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_pass *pass, con
         if (!resident[q]) p.nonres_stride[m++] = axis_stride(n, q);
     for (int u = m; u < DM_MAX_QUBITS; ++u) p.nonres_stride[u] = 0;
     p.nrounds = nr;
+    p.vec0 = pass->vec0 == 0 ? 0 : -1;
+    // round 0 conversion reads: natural offsets of round 0's bits
+    if (!valid_tables(pass->natrow, pass->natk, p.vec0, true)) return DM_ERR_PROGRAM;
+    for (int i = 0; i < 8; ++i) p.natrow[i] = pass->natrow[i];
+    for (int i = 0; i < 6; ++i) p.natk[i] = pass->natk[i];
     for (int r = 0; r < nr; ++r) {
-        int last = -1;
+        const dm_tc_round &in = pass->rounds[r];
+        tc::Round &o = p.rounds[r];
         for (int i = 0; i < 3; ++i) {
-            const int a = pass->round_axes[r][i];
-            if (a <= last || a >= tc::kAxes) return DM_ERR_PROGRAM;
-            last = a;
-            p.rax[r][i] = int8_t(a);
+            if (in.digits[i] < 0 || in.digits[i] >= tc::kAxes) return DM_ERR_PROGRAM;
+            o.digits[i] = in.digits[i];
         }
-        p.rax[r][3] = -1;
-        const int32_t off = pass->round_moff[r];
-        if (off < 0 || (off & 3) || size_t(off) + 2 * 64 * 64 > umats_count) return DM_ERR_PROGRAM;
-        p.umoff[r] = off;
+        o.vec = in.vec;
+        if (!valid_tables(in.rowc, in.kc, in.vec, r + 1 == nr)) return DM_ERR_PROGRAM;
+        for (int i = 0; i < 8; ++i) o.rowc[i] = in.rowc[i];
+        for (int i = 0; i < 6; ++i) o.kc[i] = in.kc[i];
+        if (in.umoff < 0 || (in.umoff & 3) || size_t(in.umoff) + 2 * 64 * 64 > umats_count) return DM_ERR_PROGRAM;
+        o.umoff = in.umoff;
     }
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;

@@ -406,31 +406,180 @@ def pad_pass(p, n, k=TC_AXES):
     return Pass(sorted(axes, reverse=True), p.ops)
 
 
-def encode_pass_tc(p, n, umats):
-    """DmPass for dm_apply_pass_tc: 7 resident axes, rounds with composed 64x64 images.
+# ---------------------------------------------------------------------------
+# tensor-core round layouts
+#
+# A tensor-core round views the 4**7-coefficient tile as a 256 x 64 operand
+# (rows: groups, K: the round's 64 coefficients) in the K-major core-matrix
+# layout: byte(row, k) = (row%8)*16 + (k%4)*4 + (k/4)*128 + (row/8)*2048.
+# Which tile bits form the row index, and in which order the round's three
+# axes form the K digits, is free: the host picks them so that the epilogue
+# of each round (one row per thread) writes the next round's operand with
+# 128-bit stores whose 8-thread phases hit distinct bank groups.  Tile bit
+# 2a / 2a+1 is the low / high bit of local axis a's digit.
+# ---------------------------------------------------------------------------
 
-    Appends the rounds' images to ``umats`` (list of float32 arrays); the
-    offsets are relative to the concatenation of ``umats``.
-    """
-    p = pad_pass(p, n)
-    dp = N.DmPass()
-    dp.k = len(p.axes)
-    for r, q in enumerate(p.axes):
-        dp.axes[r] = q
-    rounds = plan_rounds(p, 3)
-    if len(rounds) > N.DM_MAX_ROUNDS:
-        raise RuntimeError('pass needs %d rounds (> %d)' % (len(rounds), N.DM_MAX_ROUNDS))
-    off = sum(m.size for m in umats)
-    dp.nrounds = len(rounds)
-    dp.nops = 0
-    for ri, (axes3, rops) in enumerate(rounds):
+def _row_off(row):
+    return (row & 7) * 16 + (row >> 3) * 2048
+
+
+def _k_off(k):
+    return (k & 3) * 4 + (k >> 2) * 128
+
+
+def nat_swz(e):
+    """Shared-memory element position of tile element e in the natural (streamed) layout."""
+    return e ^ ((((e >> 5) ^ (e >> 8)) & 7) << 2)
+
+
+class TcLayout:
+    """Digit order (3 local axes) and row-bit order (8 tile bits) of one round's operand."""
+
+    def __init__(self, digits, rowbits):
+        self.digits = list(digits)
+        self.rowbits = list(rowbits)
+        self.kbits = [2 * a + b for a in self.digits for b in (0, 1)]
+        self._byte = {}
+        for i, tb in enumerate(self.rowbits):
+            self._byte[tb] = _row_off(1 << i)
+        for i, tb in enumerate(self.kbits):
+            self._byte[tb] = _k_off(1 << i)
+
+    def byte_of_bit(self, tb):
+        return self._byte[tb]
+
+
+def _choose_layouts(rounds_axes):
+    """Pick each round's digit order and row order (greedy along the round sequence)."""
+    layouts = []
+    prev = None
+    for axes in rounds_axes:
+        axes = sorted(axes)
+        nonround = [tb for tb in range(2 * TC_AXES) if tb // 2 not in axes]
+        if prev is None:
+            digits = ([0] + [a for a in axes if a != 0]) if 0 in axes else axes
+            layouts.append(TcLayout(digits, nonround))
+            prev = layouts[-1]
+            continue
+        # rows follow the previous round's row order where possible (lane bits stay lane bits)
+        keep = [tb for tb in prev.rowbits if tb in nonround]
+        rowbits = keep + [tb for tb in nonround if tb not in keep]
+        best = None
+        for first in axes:
+            digits = [first] + [a for a in axes if a != first]
+            cand = TcLayout(digits, rowbits)
+            score = epilogue_wavefronts(prev, cand)
+            if best is None or score < best[0]:
+                best = (score, cand)
+        layouts.append(best[1])
+        prev = best[1]
+    return layouts
+
+
+def _vec_digit(src, dst_first_axis):
+    """Digit of ``src`` holding the destination's 4-vector axis, or -1."""
+    return src.digits.index(dst_first_axis) if dst_first_axis in src.digits else -1
+
+
+def epilogue_wavefronts(src, dst, natural=False):
+    """Shared-memory store wavefronts of one warp writing src's rows 0..31 into dst's layout."""
+    lanes = np.arange(32)
+
+    def addr_bytes(row, k):
+        e = 0
+        for i, tb in enumerate(src.rowbits):
+            if (row >> i) & 1:
+                e |= 1 << tb
+        for i, tb in enumerate(src.kbits):
+            if (k >> i) & 1:
+                e |= 1 << tb
+        if natural:
+            return 4 * nat_swz(e)
+        return sum(dst.byte_of_bit(tb) for tb in range(2 * TC_AXES) if (e >> tb) & 1)
+
+    vec_axis = 0 if natural else dst.digits[0]
+    d = _vec_digit(src, vec_axis)
+    total = 0
+    if d >= 0:
+        others = [j for j in range(64) if (j >> (2 * d)) & 3 == 0]
+        for j in others:
+            chunks = [addr_bytes(int(r), j) // 16 for r in lanes]
+            for ph in range(4):          # 8-thread phases of a 128-bit store
+                grp = chunks[8 * ph:8 * ph + 8]
+                cnt = {}
+                for c in grp:
+                    cnt.setdefault(c % 8, set()).add(c)
+                total += max(len(v) for v in cnt.values())
+    else:
+        for j in range(64):
+            words = [addr_bytes(int(r), j) // 4 for r in lanes]
+            cnt = {}
+            for w in words:
+                cnt.setdefault(w % 32, set()).add(w)
+            total += max(len(v) for v in cnt.values())
+    return total
+
+
+def plan_tc_pass(p, n):
+    """Pad a pass to 7 axes, plan its rounds and their layouts, compose each round's U (FP64)."""
+    pp = pad_pass(p, n)
+    rounds = plan_rounds(pp, 3)
+    layouts = _choose_layouts([axes for axes, _ in rounds])
+    mats = []
+    for (axes, rops), lay in zip(rounds, layouts):
         U = np.eye(64)
         for op in rops:
-            U = op_matrix64(op, axes3) @ U
+            U = op_matrix64(op, lay.digits) @ U
+        mats.append(U)
+    return pp, layouts, mats
+
+
+def tc_tables(layouts):
+    """Conversion and per-round epilogue tables of a tensor-core pass (see dm_tc_pass)."""
+    L0 = layouts[0]
+    conv = {'natrow': [nat_swz(1 << tb) for tb in L0.rowbits], 'natk': [nat_swz(1 << tb) for tb in L0.kbits],
+            'vec0': 0 if L0.digits[0] == 0 else -1}
+    rounds = []
+    for r, L in enumerate(layouts):
+        if r + 1 < len(layouts):
+            nxt = layouts[r + 1]
+            rowc = [nxt.byte_of_bit(tb) for tb in L.rowbits]
+            kc = [nxt.byte_of_bit(tb) for tb in L.kbits]
+            vec = _vec_digit(L, nxt.digits[0])
+        else:
+            rowc = [nat_swz(1 << tb) for tb in L.rowbits]
+            kc = [nat_swz(1 << tb) for tb in L.kbits]
+            vec = _vec_digit(L, 0)
+        rounds.append({'digits': L.digits, 'rowc': rowc, 'kc': kc, 'vec': vec})
+    return conv, rounds
+
+
+def encode_pass_tc(p, n, umats):
+    """DmTcPass for dm_apply_pass_tc; appends the rounds' matrix images to ``umats``."""
+    pp, layouts, mats = plan_tc_pass(p, n)
+    if len(layouts) > N.DM_MAX_ROUNDS:
+        raise RuntimeError('pass needs %d rounds (> %d)' % (len(layouts), N.DM_MAX_ROUNDS))
+    conv, rounds = tc_tables(layouts)
+    dp = N.DmTcPass()
+    for r, q in enumerate(pp.axes):
+        dp.axes[r] = q
+    dp.nrounds = len(layouts)
+    dp.vec0 = conv['vec0']
+    for i in range(8):
+        dp.natrow[i] = conv['natrow'][i]
+    for i in range(6):
+        dp.natk[i] = conv['natk'][i]
+    off = sum(m.size for m in umats)
+    for ri, (rd, U) in enumerate(zip(rounds, mats)):
+        o = dp.rounds[ri]
         for i in range(3):
-            dp.round_axes[ri][i] = axes3[i]
-        dp.round_axes[ri][3] = -1
-        dp.round_moff[ri] = off
+            o.digits[i] = rd['digits'][i]
+        o.vec = rd['vec']
+        for i in range(8):
+            o.rowc[i] = rd['rowc'][i]
+        for i in range(6):
+            o.kc[i] = rd['kc'][i]
+        o.umoff = off
         img = tc_round_image(U)
         umats.append(img)
         off += img.size

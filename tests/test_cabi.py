@@ -42,12 +42,12 @@ def test_struct_layout_matches_header(tmp_path):
         '#include <stdio.h>\n#include <stddef.h>\n#include "dm_gb300.h"\n'
         'int main(void) { printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(dm_op), sizeof(dm_pass), '
         'offsetof(dm_pass, nops), offsetof(dm_pass, nrounds), offsetof(dm_pass, round_axes), '
-        'offsetof(dm_pass, round_end), offsetof(dm_pass, ops), offsetof(dm_pass, round_moff)); return 0; }\n')
+        'offsetof(dm_pass, round_end), offsetof(dm_pass, ops), sizeof(dm_tc_pass)); return 0; }\n')
     exe = tmp_path / 'layout'
     subprocess.run(['gcc', '-I', os.path.dirname(HEADER), str(src), '-o', str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     want = [ctypes.sizeof(N.DmOp), ctypes.sizeof(N.DmPass), N.DmPass.nops.offset, N.DmPass.nrounds.offset,
-            N.DmPass.round_axes.offset, N.DmPass.round_end.offset, N.DmPass.ops.offset, N.DmPass.round_moff.offset]
+            N.DmPass.round_axes.offset, N.DmPass.round_end.offset, N.DmPass.ops.offset, ctypes.sizeof(N.DmTcPass)]
     assert got == want
     text = open(HEADER).read()
     assert int(re.search(r'#define DM_MAX_TILE_AXES (\d+)', text).group(1)) == N.DM_MAX_TILE_AXES

@@ -216,24 +216,30 @@ def test_tensor_core_pass_equals_program_order(torch, n):
 
 
 def test_tensor_core_pass_rejects_bad_programs(torch):
+    """Malformed tensor-core descriptors are refused on the host (no launch)."""
     n = 8
     t = torch.zeros(4 ** n, dtype=torch.float32, device='cuda')
     u = torch.zeros(8192, dtype=torch.float32, device='cuda')
     status = torch.zeros(1, dtype=torch.int32, device='cuda')
-    d = N.DmPass()
-    d.k = 6                                  # a tensor-core pass holds exactly 7 axes
-    for r, q in enumerate(range(n - 1, n - 7, -1)):
-        d.axes[r] = q
-    d.nrounds = 1
-    rc = N.lib().dm_apply_pass_tc(vp(t), n, ctypes.byref(d), vp(u), 8192, vp(status), stream(torch))
-    assert rc == N.DM_ERR_PROGRAM
-    d.k = 7
-    for r, q in enumerate(range(n - 1, n - 8, -1)):
-        d.axes[r] = q
-    d.round_axes[0][0], d.round_axes[0][1], d.round_axes[0][2] = 0, 2, 1   # not ascending
-    rc = N.lib().dm_apply_pass_tc(vp(t), n, ctypes.byref(d), vp(u), 8192, vp(status), stream(torch))
-    assert rc == N.DM_ERR_PROGRAM
-    d.round_axes[0][0], d.round_axes[0][1], d.round_axes[0][2] = 0, 1, 2
-    d.round_moff[0] = 4                      # image would overrun the 8192-float buffer
-    rc = N.lib().dm_apply_pass_tc(vp(t), n, ctypes.byref(d), vp(u), 8192, vp(status), stream(torch))
-    assert rc == N.DM_ERR_PROGRAM
+    rng = np.random.default_rng(0)
+    from test_planner import random_ops
+    ops = random_ops(rng, n, 10)
+    good = P.encode_pass_tc(P.plan_passes(ops, n, 7, 2)[0], n, [])
+
+    def rc_of(mutate):
+        d = N.DmTcPass.from_buffer_copy(good)
+        mutate(d)
+        return N.lib().dm_apply_pass_tc(vp(t), n, ctypes.byref(d), vp(u), 8192, vp(status), stream(torch))
+
+    def bad_axes(d):
+        d.axes[1], d.axes[2] = d.axes[2], d.axes[1]           # not decreasing
+    def bad_umoff(d):
+        d.rounds[0].umoff = 4                                 # image overruns the 8192-float buffer
+    def bad_row(d):
+        d.rounds[0].rowc[0] = 3 if d.nrounds > 1 else 20000   # not a power of two / outside the tile
+    def bad_vec(d):
+        d.vec0 = 0
+        d.natk[0], d.natk[1] = 2, 1                           # vector loads need offsets 1, 2
+    for mut in (bad_axes, bad_umoff, bad_row, bad_vec):
+        assert rc_of(mut) == N.DM_ERR_PROGRAM, mut.__name__
+    assert status.item() == 0

@@ -191,28 +191,85 @@ def test_register_rounds_equal_program_order(n, kmax, low, width):
         np.testing.assert_allclose(got, ref, rtol=1e-10, atol=1e-10 * np.abs(ref).max())
 
 
-def test_tensor_core_round_images_equal_program_order():
-    """Composed 64x64 round matrices (as the tensor-core pass applies them) equal program order."""
+def _emulate_tc_pass(st, n, p):
+    """numpy model of dm_apply_pass_tc's data movement (exact arithmetic, no TF32)."""
+    pp, layouts, mats = P.plan_tc_pass(p, n)
+    conv, rounds = P.tc_tables(layouts)
+    k = 7
+    non = [q for q in range(n - 1, -1, -1) if q not in pp.axes]
+    out = st.copy()
+    for t in range(4 ** (n - k)):
+        base = sum(((t >> (2 * u)) & 3) * 4 ** (n - 1 - q) for u, q in enumerate(non))
+        idx = np.array([base + sum(((e >> (2 * r)) & 3) * 4 ** (n - 1 - q) for r, q in enumerate(pp.axes))
+                        for e in range(4 ** k)])
+        nat = np.zeros(4 ** k)
+        nat[[P.nat_swz(e) for e in range(4 ** k)]] = st[idx]          # cp.async landing
+        A = np.zeros(16384)                                            # operand, float index = byte / 4
+
+        def xor_bits(x, c):
+            o = 0
+            for i, ci in enumerate(c):
+                if (x >> i) & 1:
+                    o ^= ci
+            return o
+
+        for row in range(256):                                         # conversion
+            nb = xor_bits(row, conv['natrow'])
+            for j in range(64):
+                A[(P._row_off(row) + P._k_off(j)) // 4] = nat[nb ^ xor_bits(j, conv['natk'])]
+        for r, (rd, U) in enumerate(zip(rounds, mats)):
+            X = np.array([[A[(P._row_off(row) + P._k_off(j)) // 4] for j in range(64)] for row in range(256)])
+            D = X @ U.T
+            last = r + 1 == len(rounds)
+            newA = np.zeros(16384) if not last else None
+            natout = np.zeros(4 ** k) if last else None
+            for row in range(256):
+                b = xor_bits(row, rd['rowc'])
+                for j in range(64):
+                    o = b ^ xor_bits(j, rd['kc'])
+                    if last:
+                        natout[o] = D[row, j]
+                    else:
+                        newA[o // 4] = D[row, j]
+            if not last:
+                A = newA
+        out[idx] = natout[[P.nat_swz(e) for e in range(4 ** k)]]
+    return out
+
+
+def test_tensor_core_tables_emulated():
+    """The tensor-core pass's layouts and tables, replayed in numpy, equal program order."""
     n = 8
     rng = np.random.default_rng(21)
-    ops = random_ops(rng, n, 50)
+    ops = random_ops(rng, n, 40)
     st0 = rng.normal(size=4 ** n)
     ref = st0.copy()
     for op in ops:
         ref = apply_op(ref, n, op)
     got = st0.copy()
     for p in P.plan_passes(ops, n, 7, 2):
-        pp = P.pad_pass(p, n)
-        assert len(pp.axes) == 7 and pp.axes[0] == n - 1
-        for axes3, rops in P.plan_rounds(pp, 3):
-            U = np.eye(64)
-            for op in rops:
-                U = P.op_matrix64(op, axes3) @ U
-            qs = [pp.axes[a] for a in axes3]
-            t = np.moveaxis(got.reshape([4] * n), (qs[2], qs[1], qs[0]), (0, 1, 2)).reshape(64, -1)
-            t = (U @ t).reshape([4, 4, 4] + [4] * (n - 3))
-            got = np.moveaxis(t, (0, 1, 2), (qs[2], qs[1], qs[0])).reshape(-1)
+        got = _emulate_tc_pass(got, n, p)
     np.testing.assert_allclose(got, ref, rtol=0, atol=1e-10 * np.abs(ref).max())
+
+
+def test_tensor_core_tables_are_valid():
+    """Every table entry obeys the kernel's checks (distinct power-of-two operand offsets, alignment)."""
+    n = 16
+    rng = np.random.default_rng(4)
+    ops = random_ops(rng, n, 300)
+    for p in P.plan_passes(ops, n, 7, 2):
+        _, layouts, _ = P.plan_tc_pass(p, n)
+        conv, rounds = P.tc_tables(layouts)
+        for r, rd in enumerate(rounds):
+            c = rd['rowc'] + rd['kc']
+            if r + 1 < len(rounds):
+                assert all(x > 0 and x & (x - 1) == 0 and x < 65536 for x in c)
+                assert len(set(c)) == 14
+                if rd['vec'] >= 0:
+                    v = rd['vec']
+                    assert rd['kc'][2 * v] == 4 and rd['kc'][2 * v + 1] == 8
+            else:
+                assert all(0 < x < 16384 for x in c)
 
 
 def test_tc_image_layout_and_split():
