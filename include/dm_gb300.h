@@ -165,6 +165,49 @@ typedef struct dm_tc_pass {
 int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, const float *umats_dev, size_t umats_count,
                      int *status_dev, void *stream);
 
+/* ------------------------------------------------------------- batched sweeps */
+
+/* One pass of a batched program (the n-independent part of dm_pass). */
+typedef struct dm_batch_pass {
+    int8_t k;                          /* resident axes; axes[0] must be the instance's qubit n-1 */
+    int8_t nrounds;
+    int16_t nops;
+    int8_t axes[DM_MAX_TILE_AXES];     /* resident qubits, strictly decreasing */
+    int8_t pad;
+    int8_t round_axes[DM_MAX_ROUNDS][4];
+    int16_t round_end[DM_MAX_ROUNDS];
+    dm_op ops[DM_MAX_PASS_OPS];        /* moff relative to the instance's coefficient block */
+} dm_batch_pass;
+
+/* One independent circuit instance of a batched program. */
+typedef struct dm_batch_instance {
+    int32_t n;                         /* qubits */
+    int32_t npasses;                   /* passes pass_begin .. pass_begin + npasses - 1 */
+    int32_t pass_begin;
+    int32_t pad;
+    int64_t state_off;                 /* element offset of the instance's 4**n state */
+    int64_t prob_off;                  /* double offset of its 2**n outcome probabilities */
+    int64_t mats_off;                  /* element offset of its coefficient block */
+    int64_t mats_len;                  /* elements in its coefficient block */
+    double meas_err;                   /* polarisation of the final Z measurement of every qubit */
+} dm_batch_instance;
+
+/* Run many independent circuit instances in one persistent launch: every
+ * CTA takes the next instance from a work counter (the caller orders the
+ * instances largest first), prepares |0...0>, applies the instance's passes
+ * with the pipelined register-round kernel and writes the 2**n probabilities
+ * of a Z measurement of every qubit (polarisation meas_err), the read-out of
+ * DmSimulatorPy._add_ensemble_measure (dm_simulator.py:427-481).
+ * The tables are passed twice: host copies (validated here) and the
+ * identical device copies the kernel reads.  counter_dev is reset here
+ * (cudaMemsetAsync), so the call can be captured in a CUDA graph after a
+ * first call.  status_dev is left 0.  dtype F32 (3-axis rounds, passes of
+ * <= 7 axes) or F64 (2-axis rounds, <= 6 axes). */
+int dm_batch_run(int dtype, void *states_dev, size_t states_count, double *probs_dev, size_t probs_count,
+                 const void *mats_dev, size_t mats_count, const dm_batch_instance *insts_host,
+                 const dm_batch_instance *insts_dev, int ninst, const dm_batch_pass *passes_host,
+                 const dm_batch_pass *passes_dev, int npasses, int *counter_dev, int *status_dev, void *stream);
+
 /* ---------------------------------------------------------------- measurement */
 
 /* Probabilities of a measurement along one Pauli axis per qubit.

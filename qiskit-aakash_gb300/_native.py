@@ -106,6 +106,20 @@ class DmTcPass(ctypes.Structure):
                 ('rounds', DmTcRound * DM_MAX_ROUNDS)]
 
 
+class DmBatchPass(ctypes.Structure):
+    _fields_ = [('k', ctypes.c_int8), ('nrounds', ctypes.c_int8), ('nops', ctypes.c_int16),
+                ('axes', ctypes.c_int8 * DM_MAX_TILE_AXES), ('pad', ctypes.c_int8),
+                ('round_axes', (ctypes.c_int8 * 4) * DM_MAX_ROUNDS),
+                ('round_end', ctypes.c_int16 * DM_MAX_ROUNDS),
+                ('ops', DmOp * DM_MAX_PASS_OPS)]
+
+
+class DmBatchInstance(ctypes.Structure):
+    _fields_ = [('n', ctypes.c_int32), ('npasses', ctypes.c_int32), ('pass_begin', ctypes.c_int32),
+                ('pad', ctypes.c_int32), ('state_off', ctypes.c_int64), ('prob_off', ctypes.c_int64),
+                ('mats_off', ctypes.c_int64), ('mats_len', ctypes.c_int64), ('meas_err', ctypes.c_double)]
+
+
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
 _d = ctypes.c_double
@@ -122,6 +136,8 @@ SIGNATURES = {
     'dm_apply_memory_noise': (_i, [_vp, _i, _i, _d, _d, _d, _vp]),
     'dm_apply_pass': (_i, [_vp, _i, _i, ctypes.POINTER(DmPass), _vp, _sz, _vp]),
     'dm_apply_pass_tc': (_i, [_vp, _i, ctypes.POINTER(DmTcPass), _vp, _sz, _vp, _vp]),
+    'dm_batch_run': (_i, [_i, _vp, _sz, _vp, _sz, _vp, _sz, ctypes.POINTER(DmBatchInstance), _vp, _i,
+                          ctypes.POINTER(DmBatchPass), _vp, _i, _vp, _vp, _vp]),
     'dm_axis_probs': (_i, [_vp, _i, _i, _ip, _d, _vp, _vp]),
     'dm_nbasis_probs_scratch_bytes': (_sz, [_i]),
     'dm_nbasis_probs': (_i, [_vp, _i, _i, _dp, _d, _vp, _vp, _vp]),

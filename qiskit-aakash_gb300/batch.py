@@ -1,0 +1,505 @@
+"""Batched noise sweeps: thousands of independent circuit instances, one persistent launch.
+
+Each instance is an ordinary dm_simulator experiment (same merge, levels,
+per-level memory noise and final Z ensemble measurement as
+``DmSimulatorGPU.run_experiment``); the batch runs them all in one
+``dm_batch_run`` launch, where every CTA takes the next instance from a
+work counter and runs it start to finish (state preparation, fused passes,
+read-out).  The launch can be captured in a CUDA graph and replayed.
+
+Host work is kept small by sharing plans: instances with the same
+structure (qubit count and depth of the layered template) share one pass /
+round plan; per instance only the coefficients of the plan's operations are
+rebuilt from the instance's own gate and noise matrices (``Op.src``).  The
+resident-axis count per qubit count is picked by ``autotune``, which times
+each candidate on the device.
+"""
+import ctypes
+import time
+
+import numpy as np
+
+from . import _native as N
+from . import program as P
+from .circuit import noise_options, random_layer_circuit
+from .exceptions import BasicAerError
+
+MAX_QUBITS = 12
+
+
+class HostRecorder:
+    """DeviceState's interface without a device: records one experiment's op stream and read-outs."""
+
+    def __init__(self, n, **_):
+        self.n = n
+        self.init = None
+        self.ops = []
+        self.readouts = []
+        self.passes_run = 0
+        self.h2d_bytes = 0
+        self.d2h_bytes = 0
+
+    def init_product(self, vectors, scale):
+        self.init = (np.asarray(vectors, dtype=float), float(scale))
+        self.ops = []
+
+    def load(self, coeffs):
+        raise BasicAerError('batched programs start from product states')
+
+    def map1(self, q, m):
+        self.ops.append(P.Op('map1', (q,), np.asarray(m, dtype=float)))
+
+    def cx(self, ctl, tgt, tsp):
+        coef, ideal = P.cx_coefficients(tsp)
+        self.ops.append(P.Op('cx', (ctl, tgt), np.array(coef), ideal))
+
+    def diag2(self, qa, qb, d):
+        self.ops.append(P.Op('diag2', (qa, qb), np.asarray(d, dtype=float)))
+
+    def axis_probs(self, mode, err):
+        self.readouts.append(('axis', len(self.ops), list(mode), float(err)))
+        return np.zeros(2 ** sum(1 for m in mode if m))
+
+    def nbasis_probs(self, nvec, err):
+        raise BasicAerError('batched programs read out Z ensemble probabilities only')
+
+    def gather(self, indices):
+        raise BasicAerError('batched programs read out Z ensemble probabilities only')
+
+    def coefficients(self, chop_threshold):
+        return None
+
+    def raw_coefficients(self):
+        return None
+
+    def density_matrix(self):
+        return None
+
+    def overlap(self, other):
+        raise BasicAerError('batched programs do not compare states')
+
+    def synchronize(self):
+        pass
+
+
+def compile_experiment(experiment, options):
+    """Op stream and final Z read-out of one experiment, through the backend's own run loop."""
+    from .dm_simulator import DmSimulatorGPU
+    DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
+    b = DmSimulatorGPU()
+    opts = dict(options)
+    opts['compute_densitymatrix'] = False
+    b._set_options(backend_options=opts)
+    rec = b.compile_experiment(experiment)
+    if len(rec.readouts) != 1 or any(m != 3 for m in rec.readouts[0][2]):
+        raise BasicAerError('a batched instance must end with one Z ensemble measurement of every qubit')
+    # the level's memory noise after the read-out does not change the probabilities
+    del rec.ops[rec.readouts[0][1]:]
+    if rec.init is None or not np.array_equal(rec.init[0], np.tile([1.0, 0.0, 0.0, 1.0], (rec.n, 1))):
+        raise BasicAerError('batched instances start in |0...0>')
+    return rec
+
+
+def _signature(ops):
+    return tuple((op.kind, op.axes, op.ideal) for op in ops)
+
+
+class _Plan:
+    """A pass / round plan shared by instances of one structure."""
+
+    def __init__(self, ops, n, kmax, dtype):
+        self.n = n
+        width = N.DM_ROUND_AXES[N.DM_F64 if dtype == np.float64 else N.DM_F32]
+        self.passes = []     # dm_batch_pass
+        self.slots = []      # (kind, src, ideal) per coefficient block entry, in mats order
+        self.mats_len = 0
+        for p in P.plan_passes(ops, n, kmax, 2):
+            pp = p if len(p.axes) >= width else P.pad_pass(p, n, width)
+            rounds = P.plan_rounds(pp, width)
+            bp = N.DmBatchPass()
+            bp.k = len(pp.axes)
+            for r, q in enumerate(pp.axes):
+                bp.axes[r] = q
+            bp.nrounds = len(rounds)
+            if bp.nrounds > N.DM_MAX_ROUNDS:
+                raise BasicAerError('pass needs too many rounds')
+            o = 0
+            for ri, (axes, rops) in enumerate(rounds):
+                for i, a in enumerate(axes):
+                    bp.round_axes[ri][i] = a
+                for i in range(len(axes), 4):
+                    bp.round_axes[ri][i] = -1
+                for op in rops:
+                    d = bp.ops[o]
+                    d.a = op.axes[0]
+                    d.moff = self.mats_len
+                    flags = axes.index(op.axes[0]) << 8
+                    if op.kind == 'map1':
+                        d.kind = N.DM_OP_MAP1
+                        d.b = 0
+                        m = np.asarray(op.data).reshape(16)
+                        row0 = m[0] == 1.0 and not m[1:4].any()
+                        flags |= N.DM_MAP1_ROW0_IDENTITY if row0 else 0
+                        size = 16
+                    elif op.kind == 'cx':
+                        d.kind = N.DM_OP_CX
+                        d.b = op.axes[1]
+                        flags |= (N.DM_CX_IDEAL if op.ideal else 0) | (axes.index(op.axes[1]) << 12)
+                        size = 5
+                    elif op.kind == 'diag2':
+                        d.kind = N.DM_OP_DIAG2
+                        d.b = op.axes[1]
+                        flags |= axes.index(op.axes[1]) << 12
+                        size = 16
+                    else:
+                        raise BasicAerError('batched programs hold 4x4 maps, CX and diagonal pair maps only')
+                    d.flags = flags
+                    self.slots.append((op.kind, list(op.src), op.ideal,
+                                       (flags & N.DM_MAP1_ROW0_IDENTITY) if op.kind == 'map1' else 0))
+                    self.mats_len += size
+                    o += 1
+                bp.round_end[ri] = o
+            bp.nops = o
+            self.passes.append(bp)
+
+    def coefficients(self, ops, dtype):
+        """The coefficient block of one instance (its own op matrices, composed along the plan)."""
+        out = np.empty(self.mats_len, dtype=np.float64)
+        pos = 0
+        for kind, src, ideal, row0 in self.slots:
+            if kind == 'map1':
+                m = ops[src[0]].data
+                for i in src[1:]:
+                    m = ops[i].data @ m
+                m = m.reshape(16)
+                if row0 and not (m[0] == 1.0 and not m[1:4].any()):
+                    raise BasicAerError('instance does not share the plan (I row)')
+                out[pos:pos + 16] = m
+                pos += 16
+            elif kind == 'cx':
+                out[pos:pos + 5] = ops[src[0]].data
+                pos += 5
+            else:
+                out[pos:pos + 16] = np.asarray(ops[src[0]].data).reshape(16)
+                pos += 16
+        return out.astype(dtype)
+
+
+def sweep_specs(count, seed=0, n_range=(6, 12), depth_range=(10, 50), noise_range=(1e-4, 1e-2)):
+    """The seeded batched noise sweep: qubits, depth, circuit seed and log-uniform noise per instance."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(noise_range[0]), np.log(noise_range[1])
+    specs = []
+    for i in range(count):
+        specs.append({
+            'n': int(rng.integers(n_range[0], n_range[1] + 1)),
+            'depth': int(rng.integers(depth_range[0], depth_range[1] + 1)),
+            'seed': seed * 1000003 + i,
+            'depolarisation': float(np.exp(rng.uniform(lo, hi))),
+            'decoherence': 1.0 - float(np.exp(rng.uniform(lo, hi))),
+            'decay': 1.0 - float(np.exp(rng.uniform(lo, hi))),
+        })
+    return specs
+
+
+def instance_experiment(spec):
+    qc = random_layer_circuit(spec['n'], spec['depth'], spec['seed'])
+    opts = noise_options(depolarisation=spec['depolarisation'], decoherence=spec['decoherence'],
+                         decay=spec['decay'])
+    return qc.to_experiment(), opts
+
+
+def _structure(spec):
+    """Instances with the same key run the same template structure (gate angles and noise aside)."""
+    return (spec['n'], spec['depth'])
+
+
+def compile_group(specs, variants):
+    """Op streams of one structure group, planned for each (precision, resident axes) variant.
+
+    Returns, per variant, the distinct plans (their dm_batch_pass tables as
+    bytes, pass count, coefficient count) and per instance (plan index,
+    FP64 coefficient block, measurement polarisation).
+    """
+    recs = [compile_experiment(*instance_experiment(s)) for s in specs]
+    out = []
+    for precision, k in variants:
+        np_dtype = np.float32 if precision == 'single' else np.float64
+        by_sig, plans, insts = {}, [], []
+        for spec, rec in zip(specs, recs):
+            sig = _signature(rec.ops)
+            if sig not in by_sig:
+                by_sig[sig] = len(plans)
+                plans.append(_Plan(rec.ops, spec['n'], min(k, spec['n']), np_dtype))
+            pi = by_sig[sig]
+            insts.append((pi, plans[pi].coefficients(rec.ops, np.float64), rec.readouts[0][3]))
+        out.append(([(bytes((N.DmBatchPass * len(pl.passes))(*pl.passes)), len(pl.passes), pl.mats_len)
+                     for pl in plans], insts))
+    return out
+
+
+_WORKER = r"""
+import importlib.util, os, pickle, sys
+pkg_dir, task_path, out_path = sys.argv[1:4]
+spec = importlib.util.spec_from_file_location('qiskit_aakash_gb300', os.path.join(pkg_dir, '__init__.py'),
+                                              submodule_search_locations=[pkg_dir])
+mod = importlib.util.module_from_spec(spec)
+sys.modules['qiskit_aakash_gb300'] = mod
+spec.loader.exec_module(mod)
+from qiskit_aakash_gb300 import batch
+with open(task_path, 'rb') as f:
+    groups, variants = pickle.load(f)
+res = [batch.compile_group(g, variants) for g in groups]
+with open(out_path + '.tmp', 'wb') as f:
+    pickle.dump(res, f, protocol=pickle.HIGHEST_PROTOCOL)
+os.replace(out_path + '.tmp', out_path)
+"""
+
+
+def _compile_groups(groups, variants, workers):
+    """compile_group over every group, in ``workers`` host processes (fresh interpreters)."""
+    if workers <= 1 or len(groups) <= 1:
+        return [compile_group(g, variants) for g in groups]
+    import os
+    import pickle
+    import subprocess
+    import sys
+    import tempfile
+    cost = [sum(s['n'] * s['depth'] for s in g) for g in groups]
+    bins = [[] for _ in range(min(workers, len(groups)))]
+    load = [0] * len(bins)
+    for gi in sorted(range(len(groups)), key=lambda g: -cost[g]):     # longest first onto the lightest bin
+        b = load.index(min(load))
+        bins[b].append(gi)
+        load[b] += cost[gi]
+    pkg_dir = os.path.dirname(os.path.abspath(__file__))
+    results = [None] * len(groups)
+    with tempfile.TemporaryDirectory(prefix='dm_batch_') as tmp:
+        procs = []
+        for b, members in enumerate(bins):
+            task = os.path.join(tmp, 'task%d' % b)
+            out = os.path.join(tmp, 'out%d' % b)
+            with open(task, 'wb') as f:
+                pickle.dump(([groups[g] for g in members], variants), f, protocol=pickle.HIGHEST_PROTOCOL)
+            env = dict(os.environ, OMP_NUM_THREADS='1', OPENBLAS_NUM_THREADS='1')
+            procs.append((members, out, subprocess.Popen([sys.executable, '-c', _WORKER, pkg_dir, task, out],
+                                                         env=env, stderr=subprocess.PIPE)))
+        for members, out, proc in procs:
+            _, err = proc.communicate()
+            if proc.returncode != 0:
+                raise BasicAerError('batch compile worker failed:\n' + err.decode(errors='replace')[-2000:])
+            with open(out, 'rb') as f:
+                for g, r in zip(members, pickle.load(f)):
+                    results[g] = r
+    return results
+
+
+def compile_sweep(specs, variants, workers=None, kmax=None):
+    """BatchTables for each variant ('single' or 'double') of one sweep, compiled once.
+
+    ``kmax`` maps a qubit count to resident axes (default 7 for FP32, 6
+    for FP64); ``workers`` host processes share the host-side compile
+    (default: every core for large sweeps, in-process for small ones).
+    """
+    import os
+    kmax = dict(kmax or {})
+    t0 = time.perf_counter()
+    for spec in specs:
+        for precision in variants:
+            lo = N.DM_ROUND_AXES[N.DM_F32 if precision == 'single' else N.DM_F64]
+            if not lo <= spec['n'] <= MAX_QUBITS:
+                raise BasicAerError('batched instances hold %d..%d qubits' % (lo, MAX_QUBITS))
+    if workers is None:
+        workers = (os.cpu_count() or 1) if len(specs) >= 64 else 1
+    keys = {}
+    for i, spec in enumerate(specs):
+        keys.setdefault(_structure(spec), []).append(i)
+    order = list(keys)
+    groups = [[specs[i] for i in keys[key]] for key in order]
+    # one variant list per structure: the resident axes depend on the qubit count
+    by_group = {}
+    for key in order:
+        n = key[0]
+        by_group[key] = [(p, kmax.get(n, 7 if p == 'single' else 6)) for p in variants]
+    # compile_group takes one variant list; groups with equal lists are compiled together
+    results = [None] * len(groups)
+    for vlist in {tuple(v) for v in by_group.values()}:
+        idx = [g for g, key in enumerate(order) if tuple(by_group[key]) == vlist]
+        for g, r in zip(idx, _compile_groups([groups[g] for g in idx], list(vlist), workers)):
+            results[g] = r
+    seconds = time.perf_counter() - t0
+    tables = {}
+    for vi, precision in enumerate(variants):
+        per_instance = [None] * len(specs)
+        plans = []
+        for g, key in enumerate(order):
+            gplans, ginsts = results[g][vi]
+            base = len(plans)
+            plans.extend(gplans)
+            for i, (pi, block, err) in zip(keys[key], ginsts):
+                per_instance[i] = (base + pi, block, err)
+        tables[precision] = BatchTables(specs, precision, plans, per_instance, seconds)
+    return tables
+
+
+class BatchTables:
+    """Host tables of a batch: instance table, shared pass plans and coefficient blocks.
+
+    Instances are laid out largest first (4**n x depth), the order the
+    device's work counter hands them out; ``index[i]`` is the slot of input
+    instance i.  States, outcome probabilities and coefficient blocks are
+    packed back to back in slot order.  Built by ``compile_sweep``; the
+    constructor with ``specs`` only compiles one variant.
+    """
+
+    def __init__(self, specs, precision='single', plans=None, per_instance=None, compile_seconds=None,
+                 kmax=None, workers=None):
+        if plans is None:
+            t = compile_sweep(specs, [precision], workers=workers, kmax=kmax)[precision]
+            self.__dict__.update(t.__dict__)
+            return
+        t0 = time.perf_counter()
+        self.precision = precision
+        self.dtype = N.DM_F32 if precision == 'single' else N.DM_F64
+        self.np_dtype = np.float32 if precision == 'single' else np.float64
+        self.specs = specs
+        order = sorted(range(len(specs)), key=lambda i: -(4 ** specs[i]['n'] * specs[i]['depth']))
+        pass_begin, passes, npass_total = {}, [], 0
+        insts, mats = [], []
+        state_off = prob_off = mats_off = 0
+        self.index = np.empty(len(specs), dtype=np.int64)
+        for slot, i in enumerate(order):
+            pi, block, err = per_instance[i]
+            raw, npasses, mats_len = plans[pi]
+            if pi not in pass_begin:
+                pass_begin[pi] = npass_total
+                passes.append(raw)
+                npass_total += npasses
+            n = specs[i]['n']
+            I = N.DmBatchInstance()
+            I.n = n
+            I.npasses = npasses
+            I.pass_begin = pass_begin[pi]
+            I.state_off, I.prob_off, I.mats_off, I.mats_len = state_off, prob_off, mats_off, mats_len
+            I.meas_err = err
+            insts.append(I)
+            mats.append(block)
+            state_off += 4 ** n
+            prob_off += 2 ** n
+            mats_off += mats_len
+            self.index[i] = slot
+        self.nplans = len(pass_begin)
+        self.insts = (N.DmBatchInstance * len(insts))(*insts)
+        blob = b''.join(passes)
+        self.npasses = len(blob) // ctypes.sizeof(N.DmBatchPass)
+        self.passes = (N.DmBatchPass * self.npasses).from_buffer_copy(blob) if blob else (N.DmBatchPass * 0)()
+        self.ninst = len(insts)
+        self.mats = np.concatenate(mats).astype(self.np_dtype)
+        self.states_count = state_off
+        self.probs_count = prob_off
+        self.compile_seconds = compile_seconds
+        self.layout_seconds = time.perf_counter() - t0
+
+    def instance(self, i):
+        """The instance table entry of input instance i."""
+        return self.insts[int(self.index[i])]
+
+    def split(self, probs):
+        """Per-instance outcome probabilities (input order) from the packed output."""
+        out = []
+        for i in range(len(self.specs)):
+            I = self.instance(i)
+            out.append(np.asarray(probs[I.prob_off:I.prob_off + 2 ** I.n]))
+        return out
+
+
+class BatchProgram:
+    """A batch on the device: uploaded tables, resident states and outputs, optional CUDA graph."""
+
+    def __init__(self, tables, device=None):
+        import torch
+        if not torch.cuda.is_available():
+            raise BasicAerError('batched sweeps need a CUDA device')
+        N.lib()
+        self.t = tables
+        self.dtype = tables.dtype
+        self.device = torch.device(device or 'cuda')
+        dev = self.device
+
+        def to_dev(buf):
+            raw = np.frombuffer(bytes(buf), dtype=np.uint8)
+            return torch.from_numpy(raw.copy()).to(dev)
+
+        self.insts_dev = to_dev(tables.insts)
+        self.passes_dev = to_dev(tables.passes)
+        self.mats_dev = torch.from_numpy(tables.mats).to(dev)
+        tdt = torch.float32 if self.dtype == N.DM_F32 else torch.float64
+        self.states = torch.empty(tables.states_count, dtype=tdt, device=dev)
+        self.probs = torch.zeros(tables.probs_count, dtype=torch.float64, device=dev)
+        self.counter = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.h2d_bytes = ctypes.sizeof(tables.insts) + ctypes.sizeof(tables.passes) + tables.mats.nbytes
+        self.graph = None
+
+    def launch(self, stream=None):
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        vp = ctypes.c_void_p
+        t = self.t
+        N.call('dm_batch_run', self.dtype, vp(self.states.data_ptr()), ctypes.c_size_t(t.states_count),
+               vp(self.probs.data_ptr()), ctypes.c_size_t(t.probs_count), vp(self.mats_dev.data_ptr()),
+               ctypes.c_size_t(t.mats.size), t.insts, vp(self.insts_dev.data_ptr()), t.ninst,
+               t.passes, vp(self.passes_dev.data_ptr()), t.npasses, vp(self.counter.data_ptr()),
+               vp(self.status.data_ptr()), vp(s.cuda_stream))
+
+    def capture(self):
+        """Capture one launch in a CUDA graph (after a first, uncaptured launch)."""
+        import torch
+        self.launch()
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.launch(torch.cuda.current_stream(self.device))
+        self.graph = g
+        return g
+
+    def run(self):
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self.launch()
+
+    def results(self):
+        """Outcome probabilities per instance (input order; qubit 0 is the most significant bit)."""
+        return self.t.split(self.probs.cpu().numpy())
+
+
+def autotune(specs, precision='single', candidates=None, reps=2):
+    """Pick the resident-axis count per qubit count by timing each candidate on the device."""
+    import torch
+    candidates = candidates or ([5, 6, 7] if precision == 'single' else [4, 5, 6])
+    by_n = {}
+    for s in specs:
+        by_n.setdefault(s['n'], []).append(s)
+    choice, timings = {}, {}
+    for n, group in sorted(by_n.items()):
+        sample = group[:8]
+        best = None
+        for k in candidates:
+            if k > n or k < N.DM_ROUND_AXES[N.DM_F32 if precision == 'single' else N.DM_F64]:
+                continue
+            prog = BatchProgram(BatchTables(sample, precision, kmax={n: k}, workers=1))
+            prog.launch()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(reps):
+                prog.launch()
+            b.record()
+            torch.cuda.synchronize()
+            ms = a.elapsed_time(b) / reps
+            timings[(n, k)] = ms
+            if best is None or ms < best[0]:
+                best = (ms, k)
+        choice[n] = best[1]
+    return choice, timings

@@ -448,19 +448,17 @@ constexpr int kPipeThreads = 256;
 template <typename T>
 __host__ __device__ constexpr int pipe_tile_axes() { return sizeof(T) == 4 ? 7 : 6; }
 
-// One persistent CTA per SM streams the pass's tiles through kPipeBuffers
-// shared-memory buffers: while the rounds of tile i run, the 16-byte
-// cp.async copies of the next tiles are in flight; each finished tile is
-// written back with 128-bit stores.
+// Stream tiles t0, t0 + dt, ... of one pass through kPipeBuffers shared
+// buffers: while the rounds of tile i run, the 16-byte cp.async copies of
+// the next tiles are in flight; each finished tile is written back with
+// 128-bit stores.  Called by all threads of the CTA; bufs holds
+// kPipeBuffers tiles of the dtype's largest pipelined tile, hi_off 64 int64.
 template <typename T, int R>
-__global__ void __launch_bounds__(kPipeThreads, 1) pass_pipe_kernel(T *__restrict__ st, const __grid_constant__ PassRounds p,
-                                                                    const T *__restrict__ mats) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void pipe_tiles(T *__restrict__ st, const PassRounds &p, const T *__restrict__ mats,
+                                           int64_t t0, int64_t dt, T *bufs, int64_t *hi_off) {
     constexpr int G = 1 << (2 * R);
     constexpr int CE = 16 / sizeof(T);                       // elements per 16-byte chunk
     constexpr int TMAX = 1 << (2 * pipe_tile_axes<T>());
-    __shared__ int64_t hi_off[64];                           // offsets of chunk-index digits above the thread's
-    T *bufs = reinterpret_cast<T *>(smem_raw);
     const int tsize = 1 << (2 * p.k);
     const int nchunks = tsize / CE;
     const int ngroups = 1 << (2 * (p.k - R));
@@ -468,6 +466,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) pass_pipe_kernel(T *__restric
     const int tid = threadIdx.x;
     // chunk c = tid + kPipeThreads * i covers elements e = CE * c ...: offset(e) = offset(CE*tid) + offset(CE*kPipeThreads*i)
     const int64_t off_tid = rounds_offset(p, (CE * tid) & (tsize - 1));
+    __syncthreads();   // previous users of hi_off are done
     for (int i = tid; i < 64; i += kPipeThreads) {
         const int e = CE * kPipeThreads * i;
         hi_off[i] = e < tsize ? rounds_offset(p, e) : 0;
@@ -494,7 +493,6 @@ __global__ void __launch_bounds__(kPipeThreads, 1) pass_pipe_kernel(T *__restric
         cp_async_commit();
     };
 
-    const int64_t t0 = blockIdx.x, dt = gridDim.x;
 #pragma unroll
     for (int s = 0; s < kPipeBuffers - 1; ++s) issue_load(t0 + s * dt, s);
     int b = 0;
@@ -541,6 +539,16 @@ __global__ void __launch_bounds__(kPipeThreads, 1) pass_pipe_kernel(T *__restric
         b = (b + 1) % kPipeBuffers;
     }
     cp_async_wait<0>();
+    __syncthreads();
+}
+
+// One persistent CTA per SM streams the pass's tiles.
+template <typename T, int R>
+__global__ void __launch_bounds__(kPipeThreads, 1) pass_pipe_kernel(T *__restrict__ st, const __grid_constant__ PassRounds p,
+                                                                    const T *__restrict__ mats) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int64_t hi_off[64];
+    pipe_tiles<T, R>(st, p, mats, blockIdx.x, gridDim.x, reinterpret_cast<T *>(smem_raw), hi_off);
 }
 
 // ---------------------------------------------------------------------------
@@ -761,4 +769,198 @@ extern "C" int dm_apply_memory_noise(void *state_dev, int n, int dtype, double f
         if (rc) return rc;
     }
     return DM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batched sweeps: one persistent CTA per SM runs whole instances
+// ---------------------------------------------------------------------------
+
+namespace dmg {
+
+constexpr int kBatchMaxQubits = 12;   // the Z read-out's 2**n doubles fit one tile buffer
+
+template <typename T, int R>
+__global__ void __launch_bounds__(kPipeThreads, 1)
+    batch_kernel(T *__restrict__ states, double *__restrict__ probs, const T *__restrict__ mats,
+                 const dm_batch_instance *__restrict__ insts, int ninst, const dm_batch_pass *__restrict__ passes,
+                 int *counter) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int64_t hi_off[64];
+    __shared__ PassRounds ps;
+    __shared__ int inst_s;
+    T *bufs = reinterpret_cast<T *>(smem_raw);
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) inst_s = atomicAdd(counter, 1);
+        __syncthreads();
+        const int ii = inst_s;
+        if (ii >= ninst) break;
+        const dm_batch_instance I = insts[ii];
+        const int n = I.n;
+        T *st = states + I.state_off;
+        const int64_t total = int64_t(1) << (2 * n);
+        // |0...0>: a = 2**-n on the {I, Z}**n sub-lattice, 0 elsewhere
+        for (int64_t e = int64_t(tid) * 4; e < total; e += 4 * kPipeThreads) {
+            st[e] = T(0);
+            st[e + 1] = T(0);
+            st[e + 2] = T(0);
+            st[e + 3] = T(0);
+        }
+        __syncthreads();
+        const T amp = T(ldexp(1.0, -n));
+        for (int i = tid; i < (1 << n); i += kPipeThreads) {
+            int64_t idx = 0;
+            for (int q = 0; q < n; ++q)
+                if ((i >> q) & 1) idx += int64_t(3) << (2 * q);
+            st[idx] = amp;
+        }
+        __syncthreads();
+        for (int pi = 0; pi < I.npasses; ++pi) {
+            const dm_batch_pass &bp = passes[I.pass_begin + pi];
+            if (tid == 0) {
+                ps.n = n;
+                ps.k = bp.k;
+                ps.m = n - bp.k;
+                ps.nops = bp.nops;
+                ps.nrounds = bp.nrounds;
+                int low = 0;
+                while (low < bp.k && bp.axes[low] == n - 1 - low) ++low;
+                ps.low = low;
+                bool resident[DM_MAX_QUBITS] = {false};
+                for (int r = 0; r < bp.k; ++r) {
+                    resident[bp.axes[r]] = true;
+                    ps.res_stride[r] = int64_t(1) << (2 * (n - 1 - bp.axes[r]));
+                }
+                int m = 0;
+                for (int q = n - 1; q >= 0; --q)
+                    if (!resident[q]) ps.nonres_stride[m++] = int64_t(1) << (2 * (n - 1 - q));
+            }
+            for (int r = tid; r < bp.nrounds; r += kPipeThreads) {
+                for (int i = 0; i < 4; ++i) ps.rax[r][i] = bp.round_axes[r][i];
+                ps.rend[r] = bp.round_end[r];
+            }
+            for (int o = tid; o < bp.nops; o += kPipeThreads) ps.ops[o] = bp.ops[o];
+            __syncthreads();
+            pipe_tiles<T, R>(st, ps, mats + I.mats_off, 0, 1, bufs, hi_off);
+        }
+        // Z read-out: gather the 2**n sub-lattice coefficients, scale by err**popcount,
+        // Walsh-Hadamard transform in shared memory (outcome bit of qubit 0 is the MSB)
+        double *wv = reinterpret_cast<double *>(smem_raw);
+        const int np = 1 << n;
+        for (int i = tid; i < np; i += kPipeThreads) {
+            int64_t idx = 0;
+            double w = 1.0;
+            for (int j = 0; j < n; ++j)
+                if ((i >> (n - 1 - j)) & 1) {
+                    idx += int64_t(3) << (2 * (n - 1 - j));
+                    w *= I.meas_err;
+                }
+            wv[i] = double(st[idx]) * w;
+        }
+        __syncthreads();
+        for (int b = 0; b < n; ++b) {
+            for (int pidx = tid; pidx < np / 2; pidx += kPipeThreads) {
+                const int i0 = ((pidx >> b) << (b + 1)) | (pidx & ((1 << b) - 1));
+                const int i1 = i0 | (1 << b);
+                const double x = wv[i0], y = wv[i1];
+                wv[i0] = x + y;
+                wv[i1] = x - y;
+            }
+            __syncthreads();
+        }
+        for (int i = tid; i < np; i += kPipeThreads) probs[I.prob_off + i] = wv[i];
+        __syncthreads();
+    }
+}
+
+template <typename T, int R>
+static int launch_batch(T *states, double *probs, const T *mats, const dm_batch_instance *insts, int ninst,
+                        const dm_batch_pass *passes, int *counter, cudaStream_t s) {
+    const size_t smem = size_t(kPipeBuffers) * (size_t(1) << (2 * pipe_tile_axes<T>())) * sizeof(T);
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [smem] {
+        attr_err = cudaFuncSetAttribute(batch_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    });
+    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    DM_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), s));
+    int grid = sm_count();
+    if (grid > ninst) grid = ninst;
+    batch_kernel<T, R><<<grid, kPipeThreads, smem, s>>>(states, probs, mats, insts, ninst, passes, counter);
+    count_launch();
+    return launch_status();
+}
+
+static int validate_batch_pass(const dm_batch_pass &bp, int n, int R, int kmax, int64_t mats_len) {
+    const int k = bp.k;
+    if (k < R || k > kmax || k > n) return DM_ERR_PROGRAM;
+    if (bp.nops < 0 || bp.nops > DM_MAX_PASS_OPS || bp.nrounds < 1 || bp.nrounds > DM_MAX_ROUNDS) return DM_ERR_PROGRAM;
+    if (bp.axes[0] != n - 1) return DM_ERR_PROGRAM;   // the lowest axis streams in 16-byte chunks
+    for (int r = 0; r < k; ++r)
+        if (bp.axes[r] < 0 || bp.axes[r] >= n || (r > 0 && bp.axes[r] >= bp.axes[r - 1])) return DM_ERR_PROGRAM;
+    int prev_end = 0;
+    for (int r = 0; r < bp.nrounds; ++r) {
+        int last = -1;
+        for (int i = 0; i < R; ++i) {
+            const int a = bp.round_axes[r][i];
+            if (a <= last || a >= k) return DM_ERR_PROGRAM;
+            last = a;
+        }
+        const int end = bp.round_end[r];
+        if (end < prev_end || end > bp.nops) return DM_ERR_PROGRAM;
+        for (int o = prev_end; o < end; ++o) {
+            const dm_op &op = bp.ops[o];
+            int64_t need = 0;
+            switch (op.kind) {
+                case DM_OP_MAP1: need = 16; break;
+                case DM_OP_DIAG2: need = 16; break;
+                case DM_OP_CX: need = 5; break;
+                default: return DM_ERR_PROGRAM;   // general 16x16 maps are not held in registers
+            }
+            if (op.moff < 0 || op.moff + need > mats_len) return DM_ERR_PROGRAM;
+            const int da = (op.flags >> 8) & 3, db = (op.flags >> 12) & 3;
+            if (op.a < 0 || op.a >= k || da >= R || bp.round_axes[r][da] != op.a) return DM_ERR_PROGRAM;
+            if (op.kind != DM_OP_MAP1 &&
+                (op.b < 0 || op.b >= k || op.b == op.a || db >= R || db == da || bp.round_axes[r][db] != op.b))
+                return DM_ERR_PROGRAM;
+        }
+        prev_end = end;
+    }
+    return prev_end == bp.nops ? DM_OK : DM_ERR_PROGRAM;
+}
+
+}  // namespace dmg
+
+extern "C" int dm_batch_run(int dtype, void *states_dev, size_t states_count, double *probs_dev, size_t probs_count,
+                            const void *mats_dev, size_t mats_count, const dm_batch_instance *insts_host,
+                            const dm_batch_instance *insts_dev, int ninst, const dm_batch_pass *passes_host,
+                            const dm_batch_pass *passes_dev, int npasses, int *counter_dev, int *status_dev,
+                            void *stream) {
+    DM_CHECK_ARG(valid_dtype(dtype) && states_dev && probs_dev && mats_dev && insts_host && insts_dev &&
+                 passes_host && passes_dev && counter_dev && ninst >= 1 && npasses >= 1);
+    (void)status_dev;
+    if (reinterpret_cast<uintptr_t>(states_dev) & 15) return DM_ERR_ARG;
+    const int R = dtype == DM_F64 ? DM_ROUND_AXES_F64 : DM_ROUND_AXES_F32;
+    const int kmax = dtype == DM_F64 ? 6 : 7;
+    for (int i = 0; i < ninst; ++i) {
+        const dm_batch_instance &I = insts_host[i];
+        if (I.n < R || I.n > kBatchMaxQubits) return DM_ERR_RANGE;
+        const int64_t total = int64_t(1) << (2 * I.n);
+        if (I.state_off < 0 || (I.state_off & 3) || size_t(I.state_off + total) > states_count) return DM_ERR_ARG;
+        if (I.prob_off < 0 || size_t(I.prob_off + (int64_t(1) << I.n)) > probs_count) return DM_ERR_ARG;
+        if (I.mats_off < 0 || I.mats_len < 0 || size_t(I.mats_off + I.mats_len) > mats_count) return DM_ERR_ARG;
+        if (I.npasses < 0 || I.pass_begin < 0 || I.pass_begin + I.npasses > npasses) return DM_ERR_PROGRAM;
+        for (int p = 0; p < I.npasses; ++p) {
+            const int rc = validate_batch_pass(passes_host[I.pass_begin + p], I.n, R, kmax, I.mats_len);
+            if (rc) return rc;
+        }
+    }
+    cudaStream_t s = as_stream(stream);
+    if (dtype == DM_F64)
+        return launch_batch<double, DM_ROUND_AXES_F64>(static_cast<double *>(states_dev), probs_dev,
+                                                       static_cast<const double *>(mats_dev), insts_dev, ninst,
+                                                       passes_dev, counter_dev, s);
+    return launch_batch<float, DM_ROUND_AXES_F32>(static_cast<float *>(states_dev), probs_dev,
+                                                  static_cast<const float *>(mats_dev), insts_dev, ninst, passes_dev,
+                                                  counter_dev, s);
 }

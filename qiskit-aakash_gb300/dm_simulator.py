@@ -230,6 +230,7 @@ class DmSimulatorGPU(_Base):
         self.last_run_stats = {}
         self._record_next = False
         self.recorded_state = None
+        self._state_factory = DeviceState
 
     def record_experiment(self, experiment):
         """Run one experiment and keep its device state with a replayable call tape.
@@ -244,6 +245,29 @@ class DmSimulatorGPU(_Base):
             return self.run_experiment(experiment)
         finally:
             self._record_next = False
+
+    def compile_experiment(self, experiment):
+        """Run one experiment's host logic against a recorder instead of a device state.
+
+        Returns the recorder (``batch.HostRecorder``) holding the initial
+        product state, the op stream (merged gates, levelled noise,
+        measurement updates) and the read-outs the experiment asks for; the
+        batched sweep runner executes such streams for many instances in
+        one launch.  Read-out values seen by the host logic are zeros.
+        """
+        from .batch import HostRecorder
+        holder = {}
+
+        def keep(n, **kw):
+            holder['rec'] = HostRecorder(n, **kw)
+            return holder['rec']
+
+        self._state_factory = keep
+        try:
+            self.run_experiment(experiment)
+        finally:
+            self._state_factory = DeviceState
+        return holder['rec']
 
     # ------------------------------------------------------------------ options
     def _set_options(self, qobj_config=None, backend_options=None):
@@ -554,8 +578,9 @@ class DmSimulatorGPU(_Base):
         data = {}
         if any(op.name == 'bfunc' for op in experiment.instructions):
             raise BasicAerError('dm_simulator does not support conditional (bfunc) operations')
-        self._dev = DeviceState(n, precision=self._precision, fusion=self._fusion, tile_axes=self._tile_axes,
-                                rounds=self._register_rounds, tensor_cores=self._tensor_cores)
+        self._dev = self._state_factory(n, precision=self._precision, fusion=self._fusion,
+                                        tile_axes=self._tile_axes, rounds=self._register_rounds,
+                                        tensor_cores=self._tensor_cores)
         if self._record_next:
             self._dev.record()
         launches0 = N.lib().dm_kernel_launch_count()

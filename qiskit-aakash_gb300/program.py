@@ -136,14 +136,21 @@ def bell_projection_diag(err):
 # ---------------------------------------------------------------------------
 
 class Op:
-    """One pending operation: kind in {'map1', 'cx', 'diag2', 'map2'}; axes are qubits."""
-    __slots__ = ('kind', 'axes', 'data', 'ideal')
+    """One pending operation: kind in {'map1', 'cx', 'diag2', 'map2'}; axes are qubits.
 
-    def __init__(self, kind, axes, data, ideal=False):
+    ``src`` lists the indices (in the planner's input) of the operations this
+    one stands for: a composed 4x4 map lists the maps it multiplies, in
+    application order.  Batched programs use it to rebuild the coefficients
+    of a shared plan for each instance.
+    """
+    __slots__ = ('kind', 'axes', 'data', 'ideal', 'src')
+
+    def __init__(self, kind, axes, data, ideal=False, src=None):
         self.kind = kind
         self.axes = tuple(axes)
         self.data = data
         self.ideal = ideal
+        self.src = src
 
     def __repr__(self):
         return 'Op(%s, %s)' % (self.kind, self.axes)
@@ -173,6 +180,7 @@ def plan_passes(ops, n, kmax, low):
     low = min(low, kmax)
     base = tuple(range(n - 1, n - 1 - low, -1))
     pending = list(ops)
+    index_of = {id(op): i for i, op in enumerate(pending)}
     passes = []
     while pending:
         resident = set(base)
@@ -195,15 +203,16 @@ def plan_passes(ops, n, kmax, low):
             grow = [a for a in axes if a not in resident]
             resident.update(grow)
             taken_idx.append(i)
+            src = op.src if op.src is not None else [index_of[id(op)]]
             if op.kind == 'map1':
                 a = axes[0]
                 j = last_on_axis.get(a)
                 if j is not None and body[j].kind == 'map1':
-                    body[j] = Op('map1', (a,), op.data @ body[j].data)
+                    body[j] = Op('map1', (a,), op.data @ body[j].data, src=body[j].src + src)
                     continue
-                body.append(Op('map1', axes, op.data))
+                body.append(Op('map1', axes, op.data, src=src))
             else:
-                body.append(op)
+                body.append(Op(op.kind, axes, op.data, op.ideal, src=src))
             for a in axes:
                 last_on_axis[a] = len(body) - 1
             if len(resident) >= kmax:
@@ -227,7 +236,7 @@ def plan_rounds(p, width):
     local axes with no mandatory axes.
     """
     k = len(p.axes)
-    local = [Op(op.kind, tuple(p.local(a) for a in op.axes), op.data, op.ideal) for op in p.ops]
+    local = [Op(op.kind, tuple(p.local(a) for a in op.axes), op.data, op.ideal, src=op.src) for op in p.ops]
     rounds = []
     for r in plan_passes(local, k, width, 0):
         axes = sorted(r.axes)

@@ -1,0 +1,127 @@
+"""Host side of the batched noise sweep (no GPU).
+
+The instance table, shared pass plans and per-instance coefficient blocks
+are replayed with numpy, exactly as the batch kernel reads them (local axis
+digits, coefficient offsets, CX flags), and the resulting Z ensemble
+probabilities must equal the oracle's for every instance.
+"""
+import numpy as np
+import pytest
+
+from oracle import dm_oracle as O
+from qiskit_aakash_gb300 import _native as N
+from qiskit_aakash_gb300 import batch as B
+
+from test_planner import apply_map1, apply_pair, cx_matrix
+
+
+def emulate_instance(T, i):
+    I = T.instance(i)
+    n = I.n
+    st = np.zeros(4 ** n)
+    # |0...0>: 2**-n on every string of I and Z
+    for m in range(2 ** n):
+        idx = sum((3 if (m >> (n - 1 - q)) & 1 else 0) * 4 ** (n - 1 - q) for q in range(n))
+        st[idx] = 2.0 ** -n
+    mats = T.mats[I.mats_off:I.mats_off + I.mats_len].astype(np.float64)
+    for p in range(I.pass_begin, I.pass_begin + I.npasses):
+        bp = T.passes[p]
+        axes = [bp.axes[r] for r in range(bp.k)]
+        assert axes[0] == n - 1 and axes == sorted(axes, reverse=True)
+        o = 0
+        for r in range(bp.nrounds):
+            rax = [bp.round_axes[r][j] for j in range(4)]
+            for o in range(o, bp.round_end[r]):
+                d = bp.ops[o]
+                da, db = (d.flags >> 8) & 3, (d.flags >> 12) & 3
+                assert rax[da] == d.a
+                qa = axes[d.a]
+                if d.kind == N.DM_OP_MAP1:
+                    st = apply_map1(st, n, qa, mats[d.moff:d.moff + 16].reshape(4, 4))
+                    continue
+                assert rax[db] == d.b
+                qb = axes[d.b]
+                if d.kind == N.DM_OP_CX:
+                    st = apply_pair(st, n, qa, qb, cx_matrix(mats[d.moff:d.moff + 5], d.flags & N.DM_CX_IDEAL))
+                elif d.kind == N.DM_OP_DIAG2:
+                    st = apply_pair(st, n, qa, qb, np.diag(mats[d.moff:d.moff + 16]))
+                else:
+                    raise AssertionError(d.kind)
+            o = bp.round_end[r]
+        assert o == bp.nops
+    return O.ensemble_probabilities(st, n, 'Z', None, I.meas_err)
+
+
+def oracle_probs(spec):
+    exp, opts = B.instance_experiment(spec)
+    res = O.OracleDmSimulator(dict(opts, compute_densitymatrix=False)).run_experiment(exp)
+    p = res['data']['ensemble_probability']
+    return np.array([p[k] for k in O.bitstring_keys(spec['n'])])
+
+
+@pytest.mark.parametrize('precision', ['double', 'single'])
+def test_batch_tables_replay_equals_oracle(precision):
+    specs = B.sweep_specs(12, seed=3, n_range=(3, 6), depth_range=(2, 9))
+    T = B.BatchTables(specs, precision)
+    tol = 1e-12 if precision == 'double' else 2e-5
+    for i, spec in enumerate(specs):
+        got = emulate_instance(T, i)
+        assert np.max(np.abs(got - oracle_probs(spec))) < tol, (i, spec)
+
+
+def test_batch_layout_is_largest_first_and_packed():
+    specs = B.sweep_specs(30, seed=5, n_range=(3, 7), depth_range=(1, 6))
+    T = B.BatchTables(specs, 'single', kmax={7: 5, 6: 4})
+    work = [4 ** T.insts[s].n for s in range(T.ninst)]
+    sizes = [4 ** specs[i]['n'] * specs[i]['depth'] for i in sorted(range(30), key=lambda i: T.index[i])]
+    assert sizes == sorted(sizes, reverse=True)
+    s_off = p_off = m_off = 0
+    for s in range(T.ninst):
+        I = T.insts[s]
+        assert (I.state_off, I.prob_off, I.mats_off) == (s_off, p_off, m_off)
+        s_off += 4 ** I.n
+        p_off += 2 ** I.n
+        m_off += I.mats_len
+        for p in range(I.pass_begin, I.pass_begin + I.npasses):
+            assert T.passes[p].k <= {7: 5, 6: 4}.get(I.n, 7)
+    assert (s_off, p_off, m_off) == (T.states_count, T.probs_count, T.mats.size) and sum(work) == s_off
+
+
+def test_plans_are_shared_by_instances_of_one_structure():
+    base = B.sweep_specs(1, seed=9, n_range=(5, 5), depth_range=(6, 6))[0]
+    specs = [dict(base, seed=base['seed'] + j, depolarisation=d, decoherence=1 - d, decay=1 - 2 * d)
+             for j, d in enumerate((1e-4, 1e-3, 1e-2))]
+    T = B.BatchTables(specs, 'double')
+    assert T.nplans == 1 and T.npasses == T.insts[0].npasses
+    assert len({T.insts[s].pass_begin for s in range(3)}) == 1
+    blocks = [T.mats[T.insts[s].mats_off:T.insts[s].mats_off + T.insts[s].mats_len] for s in range(3)]
+    assert not np.array_equal(blocks[0], blocks[1])
+    for i, spec in enumerate(specs):
+        assert np.max(np.abs(emulate_instance(T, i) - oracle_probs(spec))) < 1e-12
+
+
+def test_batch_rejects_unsupported_instances():
+    with pytest.raises(Exception):
+        B.BatchTables([dict(B.sweep_specs(1, seed=1)[0], n=13)])
+    with pytest.raises(Exception):
+        B.BatchTables([dict(B.sweep_specs(1, seed=1)[0], n=2)], 'single')
+
+
+def test_sweep_specs_ranges():
+    specs = B.sweep_specs(500, seed=0)
+    ns = [s['n'] for s in specs]
+    ds = [s['depth'] for s in specs]
+    assert min(ns) == 6 and max(ns) == 12 and min(ds) >= 10 and max(ds) <= 50
+    for s in specs:
+        assert 1e-4 <= s['depolarisation'] <= 1e-2
+        assert 1e-4 <= 1 - s['decoherence'] <= 1e-2 and 1e-4 <= 1 - s['decay'] <= 1e-2
+
+
+def test_worker_processes_compile_the_same_tables():
+    specs = B.sweep_specs(24, seed=11, n_range=(3, 6), depth_range=(2, 6))
+    a = B.compile_sweep(specs, ['single', 'double'], workers=1)
+    b = B.compile_sweep(specs, ['single', 'double'], workers=3)
+    for prec in ('single', 'double'):
+        assert bytes(a[prec].insts) == bytes(b[prec].insts)
+        assert bytes(a[prec].passes) == bytes(b[prec].passes)
+        assert np.array_equal(a[prec].mats, b[prec].mats)

@@ -40,14 +40,21 @@ def test_struct_layout_matches_header(tmp_path):
     src = tmp_path / 'layout.c'
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "dm_gb300.h"\n'
-        'int main(void) { printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(dm_op), sizeof(dm_pass), '
+        'int main(void) { printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", '
+        'sizeof(dm_op), sizeof(dm_pass), '
         'offsetof(dm_pass, nops), offsetof(dm_pass, nrounds), offsetof(dm_pass, round_axes), '
-        'offsetof(dm_pass, round_end), offsetof(dm_pass, ops), sizeof(dm_tc_pass)); return 0; }\n')
+        'offsetof(dm_pass, round_end), offsetof(dm_pass, ops), sizeof(dm_tc_pass), '
+        'sizeof(dm_batch_pass), offsetof(dm_batch_pass, axes), offsetof(dm_batch_pass, round_axes), '
+        'offsetof(dm_batch_pass, round_end), offsetof(dm_batch_pass, ops), sizeof(dm_batch_instance), '
+        'offsetof(dm_batch_instance, meas_err)); return 0; }\n')
     exe = tmp_path / 'layout'
     subprocess.run(['gcc', '-I', os.path.dirname(HEADER), str(src), '-o', str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     want = [ctypes.sizeof(N.DmOp), ctypes.sizeof(N.DmPass), N.DmPass.nops.offset, N.DmPass.nrounds.offset,
-            N.DmPass.round_axes.offset, N.DmPass.round_end.offset, N.DmPass.ops.offset, ctypes.sizeof(N.DmTcPass)]
+            N.DmPass.round_axes.offset, N.DmPass.round_end.offset, N.DmPass.ops.offset, ctypes.sizeof(N.DmTcPass),
+            ctypes.sizeof(N.DmBatchPass), N.DmBatchPass.axes.offset, N.DmBatchPass.round_axes.offset,
+            N.DmBatchPass.round_end.offset, N.DmBatchPass.ops.offset, ctypes.sizeof(N.DmBatchInstance),
+            N.DmBatchInstance.meas_err.offset]
     assert got == want
     text = open(HEADER).read()
     assert int(re.search(r'#define DM_MAX_TILE_AXES (\d+)', text).group(1)) == N.DM_MAX_TILE_AXES
