@@ -63,6 +63,12 @@ def parse():
     ap.add_argument('--e2e-steps', type=int, default=2)
     ap.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline sample')
     ap.add_argument('--no-gate-kinds', action='store_true', help='skip the per-gate-kind bandwidth table')
+    ap.add_argument('--batch', type=int, default=4096,
+                    help='instances of the batched noise sweep (0 skips the sweep leg)')
+    ap.add_argument('--surrogate-train', type=int, default=131072,
+                    help='training points of the noise surrogate (0 skips the surrogate leg)')
+    ap.add_argument('--surrogate-test', type=int, default=16384, help='held-out points of the noise surrogate')
+    ap.add_argument('--surrogate-epochs', type=int, default=8)
     return ap.parse_args()
 
 
@@ -329,6 +335,166 @@ def per_gate_kind(torch, N, n=14, reps=3):
     return {'n_qubits': n, 'dtype': 'f64', 'bytes_per_sweep': 2 * 4 ** n * 8, 'kinds': res}
 
 
+def batch_cpu_sample(pkg, specs, budget_s=8.0):
+    """Oracle seconds per instance cost unit (4**n x n x depth) on a few small instances of the sweep."""
+    from oracle import dm_oracle as O
+    from qiskit_aakash_gb300 import batch as B
+    units = secs = 0.0
+    used = []
+    t_all = time.perf_counter()
+    for spec in sorted((s for s in specs if s['n'] <= 9), key=lambda s: -s['n']):
+        exp, opts = B.instance_experiment(spec)
+        t0 = time.perf_counter()
+        O.OracleDmSimulator(dict(opts, compute_densitymatrix=False)).run_experiment(exp)
+        secs += time.perf_counter() - t0
+        units += 4.0 ** spec['n'] * spec['n'] * spec['depth']
+        used.append((spec['n'], spec['depth']))
+        if time.perf_counter() - t_all > budget_s:
+            break
+    total_units = sum(4.0 ** s['n'] * s['n'] * s['depth'] for s in specs)
+    est = secs / units * total_units
+    return {'value': len(specs) / est, 'unit': 'instances/s', 'cores': 1, 'kind': 'port',
+            'sample': '%d sweep instances (n, depth) %s through the oracle (%.1f s), extrapolated to the whole '
+                      'sweep by 4**n * n * depth' % (len(used), used, secs)}
+
+
+def batch_leg(args, pkg, torch, N):
+    """Batched noise sweep: all instances in one persistent launch, replayed from a CUDA graph."""
+    from qiskit_aakash_gb300 import batch as B
+    specs = B.sweep_specs(args.batch, seed=args.seed)
+    t0 = time.perf_counter()
+    choice, tune_ms = B.autotune(specs, 'single')
+    tune_s = time.perf_counter() - t0
+    tables = B.compile_sweep(specs, ['single', 'double'], kmax={'single': choice})
+    t32, t64 = tables['single'], tables['double']
+
+    def algorithmic_bytes(t, esize):
+        return sum(2 * 4 ** t.insts[s].n * esize * t.insts[s].npasses for s in range(t.ninst))
+
+    prog = B.BatchProgram(t32)
+    prog.capture()
+    for _ in range(args.warmup):
+        prog.run()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.steps):
+        prog.run()
+    b.record()
+    torch.cuda.synchronize()
+    ms32 = a.elapsed_time(b) / args.steps
+    p32 = prog.results()
+    del prog
+    torch.cuda.empty_cache()
+    prog = B.BatchProgram(t64)
+    prog.launch()
+    torch.cuda.synchronize()
+    a.record()
+    prog.launch()
+    b.record()
+    torch.cuda.synchronize()
+    ms64 = a.elapsed_time(b)
+    p64 = prog.results()
+    del prog
+    torch.cuda.empty_cache()
+    tv = np.array([0.5 * np.abs(x - y).sum() for x, y in zip(p32, p64)])
+    mx = max(float(np.max(np.abs(x - y))) for x, y in zip(p32, p64))
+    # end to end: host compile of the sweep, upload, one launch, outcome distributions back
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    te = B.compile_sweep(specs, ['single'], kmax={'single': choice})['single']
+    pe = B.BatchProgram(te)
+    pe.launch()
+    res = pe.results()
+    e2e_s = time.perf_counter() - e0
+    h2d, d2h = pe.h2d_bytes, int(te.probs_count * 8)
+    del pe, res
+    torch.cuda.empty_cache()
+    hbm, peak_kind = measured_peaks()
+    by32 = algorithmic_bytes(t32, 4)
+    out = {
+        'metric': 'instances/s, batched noise sweep (4096 random-layer instances, n~U{6..12}, depth~U{10..50})',
+        'value': t32.ninst / (ms32 / 1e3), 'unit': 'instances/s', 'ms_per_step': ms32, 'steps': args.steps,
+        'dtype': 'f32', 'gpu_launches_per_step': 1,
+        'config': {'instances': t32.ninst, 'seed': args.seed, 'n_range': [6, 12], 'depth_range': [10, 50],
+                   'noise': 'log-uniform depolarisation, 1-decoherence, 1-decay in [1e-4, 1e-2]',
+                   'state_bytes_fp32': int(t32.states_count * 4), 'passes': t32.npasses, 'plans': t32.nplans,
+                   'l2': 'inputs larger than L2: %.1f GB of states' % (t32.states_count * 4 / 1e9),
+                   'launch': 'one persistent dm_batch_run launch per step, CUDA graph replay'},
+        'autotune': {'k_by_n': {str(k): v for k, v in choice.items()},
+                     'ms': {'%d/%d' % nk: v for nk, v in tune_ms.items()}, 'seconds': tune_s},
+        'accuracy_vs_fp64': {'max_tv': float(tv.max()), 'median_tv': float(np.median(tv)), 'max_abs_prob': mx,
+                             'against': 'the same sweep in the batched FP64 form'},
+        'fp64': {'value': t64.ninst / (ms64 / 1e3), 'unit': 'instances/s', 'ms_per_step': ms64,
+                 'passes': t64.npasses},
+        'roofline': {'bound': 'hbm', 'achieved': by32 / (ms32 / 1e3) / 1e9, 'peak': hbm, 'unit': 'GB/s',
+                     'frac': by32 / (ms32 / 1e3) / 1e9 / hbm, 'kernel': 'batch_kernel<float,3>',
+                     'algorithmic_bytes_per_launch': by32, 'peak_kind': peak_kind},
+        'host_compile_s': t32.compile_seconds,
+        'e2e': {'value': t32.ninst / e2e_s, 'unit': 'instances/s', 'seconds_per_step': e2e_s,
+                'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': d2h,
+                'api': 'batch.compile_sweep + BatchProgram.launch + results (host compile included)'},
+    }
+    if not args.no_cpu:
+        out['cpu_baseline'] = batch_cpu_sample(pkg, specs)
+    return out
+
+
+def surrogate_leg(args, torch):
+    """Noise surrogate on a fixed 10-qubit, 30-layer template: data generation, training, held-out TV."""
+    from qiskit_aakash_gb300 import surrogate as S
+    tmpl = S.Template(n=10, layers=30, seed=args.seed)
+    raw_tr = S.sample_noise(args.surrogate_train, seed=args.seed + 101)
+    raw_te = S.sample_noise(args.surrogate_test, seed=args.seed + 202)
+    tmpl.simulate(raw_te[:256])       # warm-up (tables, states)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    y_tr = tmpl.simulate(raw_tr).float()
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    y_te = tmpl.simulate(raw_te).float()
+    torch.cuda.synchronize()
+    sim_te_s = time.perf_counter() - t0
+    f_tr = torch.from_numpy(S.features(raw_tr)).cuda()
+    f_te = torch.from_numpy(S.features(raw_te)).cuda()
+    ens = S.MLPEnsemble(members=5, batch=1024, seed=args.seed)
+    fit = ens.fit(f_tr, y_tr, epochs=args.surrogate_epochs)
+    ens.predict(f_te[:1024])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    qs = ens.predict(f_te)
+    mean, spread, tv = ens.ensemble(qs, y_te)
+    torch.cuda.synchronize()
+    inf_s = time.perf_counter() - t0
+    tv_np, spread_np = tv.cpu().numpy(), spread.cpu().numpy()
+    blind = y_tr.mean(dim=0, keepdim=True)
+    tv_blind = (0.5 * (y_te - blind).abs().sum(dim=1)).cpu().numpy()
+    sim_rate = len(raw_te) / sim_te_s
+    fallback = {}
+    for tau in (0.01, 0.02, 0.05):
+        fb = spread_np > tau
+        hybrid_tv = np.where(fb, 0.0, tv_np)
+        t_h = inf_s + fb.sum() / sim_rate
+        fallback['%g' % tau] = {'fallback_fraction': float(fb.mean()), 'hybrid_mean_tv': float(hybrid_tv.mean()),
+                                'hybrid_max_tv': float(hybrid_tv.max()), 'points_per_s': len(raw_te) / t_h}
+    return {
+        'template': 'random brick layers n=10, 30 layers, Z ensemble; 6 noise inputs',
+        'train_points': len(raw_tr), 'test_points': len(raw_te), 'members': 5, 'epochs': args.surrogate_epochs,
+        'data_generation': {'instances_per_s': len(raw_tr) / gen_s, 'seconds': gen_s,
+                            'kernel': 'batch_param_kernel<float,3> (FP64 recipe composition per pass)'},
+        'training': {'steps': fit['steps'], 'seconds': fit['seconds'],
+                     'samples_per_s': fit['steps'] * 1024 * 5 / fit['seconds']},
+        'inference': {'points_per_s': len(raw_te) / inf_s, 'seconds': inf_s},
+        'plain_simulation_points_per_s': sim_rate,
+        'held_out_tv': {'mean': float(tv_np.mean()), 'median': float(np.median(tv_np)),
+                        'p99': float(np.quantile(tv_np, 0.99)), 'max': float(tv_np.max())},
+        'parameter_blind_baseline_tv': {'mean': float(tv_blind.mean()), 'max': float(tv_blind.max())},
+        'spread': {'mean': float(spread_np.mean()), 'corr_with_tv': float(np.corrcoef(spread_np, tv_np)[0, 1])},
+        'fallback_by_spread_threshold': fallback,
+    }
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_setup(args)
@@ -464,6 +630,10 @@ def run_ours(args):
     }
     if not args.no_gate_kinds:
         line['per_gate_kind_fp64'] = per_gate_kind(torch, N)
+    if args.batch > 0:
+        line['batched_sweep'] = batch_leg(args, pkg, torch, N)
+    if args.surrogate_train > 0:
+        line['noise_surrogate'] = surrogate_leg(args, torch)
     if not args.no_cpu:
         line['cpu_baseline'] = cpu_sample(pkg, n, args.seed)
     return line

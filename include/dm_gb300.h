@@ -208,6 +208,137 @@ int dm_batch_run(int dtype, void *states_dev, size_t states_count, double *probs
                  const dm_batch_instance *insts_dev, int ninst, const dm_batch_pass *passes_host,
                  const dm_batch_pass *passes_dev, int npasses, int *counter_dev, int *status_dev, void *stream);
 
+/* Parametric batched programs: every instance runs the same circuit
+ * template (one plan) and differs only in its noise parameters.  Each
+ * operation of the template is a recipe; a slot of a pass composes a chain
+ * of recipes (application order) in FP64 on the GPU, per instance and per
+ * pass, from the instance's parameter vector:
+ *   params[0..2]  decoherence f, thermal p, decay g   (memory noise, dm_simulator.py:397-425)
+ *   params[3..8]  rotation error (<cos>, mean) of rx, ry, rz   (basicaertools.py:93-126)
+ *   params[9..10] CX transition model error (<cos>, mean)      (basicaertools.py:329-336)
+ *   params[11]    measurement polarisation of the final Z read-out */
+#define DM_PARAMS_MIN_STRIDE 12
+#define DM_RECIPE_ROT 1     /* up to 3 rotations (axis 0 rx, 1 ry, 2 rz) by fixed angles, instance errors */
+#define DM_RECIPE_NOISE 2   /* memory noise of the instance's f, p, g */
+#define DM_RECIPE_CX 3      /* CX coefficients of the instance's transition model error */
+#define DM_RECIPE_CONST 4   /* a fixed 4x4 map (or 16-entry diagonal pair map): 16 values in consts */
+
+typedef struct dm_recipe {
+    int8_t kind;
+    int8_t nrot;
+    int8_t axis[3];
+    int8_t pad[3];
+    int32_t const_off;
+    int32_t pad2;
+    double angle[3];
+} dm_recipe;
+
+typedef struct dm_param_slot {
+    int32_t begin, len;                /* recipe indices chain[begin .. begin + len - 1] */
+} dm_param_slot;
+
+/* One template program.  The passes are dm_batch_pass tables (op moff is
+ * ignored: a pass's coefficients are composed into shared memory); slot s
+ * of the program is op s of the concatenated passes. */
+typedef struct dm_param_program {
+    int32_t n, npasses, nslots, nchain, nrecipes, nconsts;
+    const dm_batch_pass *passes;
+    const dm_param_slot *slots;
+    const int32_t *chain;
+    const dm_recipe *recipes;
+    const double *consts;
+} dm_param_program;
+
+/* Run ninst instances of one template in one persistent launch: instance i
+ * starts in |0...0>, runs the passes with its own parameters
+ * (params_dev + i * params_stride) and writes the 2**n probabilities of a
+ * Z measurement of every qubit to probs_dev + i * 2**n; its state lives at
+ * states_dev + i * 4**n.  host holds host copies of the tables (validated
+ * here), dev the identical device copies the kernel reads.  The call resets
+ * counter_dev and can be captured in a CUDA graph after a first call. */
+int dm_batch_run_params(int dtype, const dm_param_program *host, const dm_param_program *dev,
+                        const double *params_dev, int params_stride, int ninst, void *states_dev,
+                        size_t states_count, double *probs_dev, size_t probs_count, int *counter_dev, void *stream);
+
+/* ---------------------------------------------------------- noise surrogate
+ *
+ * No counterpart in the reference.  A small MLP ensemble learns the map from
+ * noise parameters to a fixed circuit's Z outcome distribution from data
+ * that the batched sweep generates; the plain simulation stays the fallback
+ * wherever the ensemble disagrees with itself.  These entry points are the
+ * network's kernels: a tcgen05 BF16 GEMM with fused epilogues, softmax with
+ * the KL loss and its gradient, bias gradients, Adam, the minibatch gather
+ * and the ensemble statistics.  BF16 values travel as uint16_t bit patterns.
+ * Every call works on `members` independent networks at once (member i adds
+ * i times the *_ms stride, in elements, to each of its pointers). */
+
+#define DM_MLP_EPI_GELU_FWD 0   /* u = acc + bias: out_f32 = u (optional), out_bf16 / out_t = gelu(u) */
+#define DM_MLP_EPI_BIAS_F32 1   /* out_f32 = acc + bias */
+#define DM_MLP_EPI_GELU_BWD 2   /* d = acc * gelu'(pre): out_bf16 / out_t = d */
+#define DM_MLP_EPI_F32 3        /* out_f32 = acc */
+
+/* C[M x N] = A[M x K] * B[N x K]^T, BF16 operands (row-major, K contiguous),
+ * FP32 accumulation in tensor memory, then the epilogue.  M % 128 == 0,
+ * N % 64 == 0, K % 64 == 0; leading dimensions and member strides are
+ * multiples of 8 elements and every pointer is 16-byte aligned.  out_t is
+ * the transposed [N x M] copy (optional). */
+typedef struct dm_mlp_gemm {
+    int32_t epi, M, N, K, members, pad;
+    const uint16_t *A;
+    int64_t lda, a_ms;
+    const uint16_t *B;
+    int64_t ldb, b_ms;
+    const float *bias;
+    int64_t bias_ms;
+    const float *pre;
+    int64_t ld_pre, pre_ms;
+    float *out_f32;
+    int64_t ld_f32, f32_ms;
+    uint16_t *out_bf16;
+    int64_t ld_bf16, bf16_ms;
+    uint16_t *out_t;
+    int64_t ld_t, t_ms;
+} dm_mlp_gemm;
+
+/* status_dev is set to 1 if a bounded wait for the tensor cores gave up. */
+int dm_mlp_gemm_run(const dm_mlp_gemm *g, int *status_dev, void *stream);
+
+/* Row softmax of logits [members][rows][nout]; with targets (same shape),
+ * loss_rows[members][rows] = KL(t || q) per row and the gradient
+ * d = (q - t) * grad_scale as BF16 dz [members][rows][nout] and its
+ * transpose dzt [members][nout][rows].  probs (optional) receives q.
+ * nout % 256 == 0, nout <= 4096. */
+int dm_mlp_softmax_xent(const float *logits, const float *targets, int rows, int members, int nout,
+                        float grad_scale, float *probs, uint16_t *dz, uint16_t *dzt, float *loss_rows, void *stream);
+
+/* db[n] = sum over b < rows of d_t[n * ld + b] (BF16 in, FP32 out), n < N. */
+int dm_mlp_bias_grad(const uint16_t *d_t, int64_t ld, int64_t d_ms, int N, int rows, int members, float *db,
+                     int64_t db_ms, void *stream);
+
+/* One Adam step over every parameter of `members` networks laid out as
+ * W1 b1 W2 b2 ... (W row-major [out x in]); shapes holds (out, in) per layer
+ * (host array, nlayers <= 8).  step <= 0 only refreshes the BF16 copies:
+ * w_bf16 (same layout) and wt_bf16 (each W transposed [in x out] at the
+ * same offset). */
+int dm_mlp_adam(float *params, const float *grads, float *m, float *v, int64_t count_per_member, int members,
+                const int32_t *shapes, int nlayers, float lr, float beta1, float beta2, float eps, int step,
+                uint16_t *w_bf16, uint16_t *wt_bf16, void *stream);
+
+/* Minibatch gather: for member z and row r, sample s = index[z * rows + r]:
+ * x[z][r][f] and xt[z][f][r] = features[s][f] (BF16, zero for
+ * nfeat <= f < width) and, unless targets is NULL, t[z][r][:] = targets[s][:]
+ * (nout FP32 values).  An index outside [0, samples) reads sample 0.
+ * width % 8 == 0, nout % 4 == 0. */
+int dm_mlp_gather(const float *features, int nfeat, const float *targets, int nout, int64_t samples,
+                  const int32_t *index, int rows, int members, int width, uint16_t *x, uint16_t *xt, float *t,
+                  void *stream);
+
+/* Ensemble statistics of probs [members][rows][nout]: mean [rows][nout],
+ * spread[r] = mean over members of TV(q_member, mean) and, with ref
+ * [rows][nout], tv_ref[r] = TV(mean, ref).  members <= 8. */
+int dm_mlp_ensemble(const float *probs, int rows, int members, int nout, const float *ref, float *mean,
+                    float *spread, float *tv_ref, void *stream);
+
 /* ---------------------------------------------------------------- measurement */
 
 /* Probabilities of a measurement along one Pauli axis per qubit.

@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG_DIR, 'csrc')
 INCLUDE = os.path.join(REPO_DIR, 'include')
 BUILD_DIR = os.path.join(PKG_DIR, '_build')
 LIB_PATH = os.path.join(PKG_DIR, 'libdmgb300.so')
-SOURCES = ['dm_misc.cu', 'dm_pass.cu', 'dm_state.cu', 'dm_measure.cu', 'dm_tc.cu']
+SOURCES = ['dm_misc.cu', 'dm_pass.cu', 'dm_state.cu', 'dm_measure.cu', 'dm_tc.cu', 'dm_mlp.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '-Xptxas', '-warn-spills',
               '--expt-relaxed-constexpr']
@@ -120,6 +120,41 @@ class DmBatchInstance(ctypes.Structure):
                 ('mats_off', ctypes.c_int64), ('mats_len', ctypes.c_int64), ('meas_err', ctypes.c_double)]
 
 
+class DmRecipe(ctypes.Structure):
+    _fields_ = [('kind', ctypes.c_int8), ('nrot', ctypes.c_int8), ('axis', ctypes.c_int8 * 3),
+                ('pad', ctypes.c_int8 * 3), ('const_off', ctypes.c_int32), ('pad2', ctypes.c_int32),
+                ('angle', ctypes.c_double * 3)]
+
+
+class DmParamSlot(ctypes.Structure):
+    _fields_ = [('begin', ctypes.c_int32), ('len', ctypes.c_int32)]
+
+
+class DmParamProgram(ctypes.Structure):
+    _fields_ = [('n', ctypes.c_int32), ('npasses', ctypes.c_int32), ('nslots', ctypes.c_int32),
+                ('nchain', ctypes.c_int32), ('nrecipes', ctypes.c_int32), ('nconsts', ctypes.c_int32),
+                ('passes', ctypes.c_void_p), ('slots', ctypes.c_void_p), ('chain', ctypes.c_void_p),
+                ('recipes', ctypes.c_void_p), ('consts', ctypes.c_void_p)]
+
+
+DM_PARAMS_MIN_STRIDE = 12
+DM_RECIPE_ROT, DM_RECIPE_NOISE, DM_RECIPE_CX, DM_RECIPE_CONST = 1, 2, 3, 4
+
+
+class DmMlpGemm(ctypes.Structure):
+    _fields_ = [('epi', ctypes.c_int32), ('M', ctypes.c_int32), ('N', ctypes.c_int32), ('K', ctypes.c_int32),
+                ('members', ctypes.c_int32), ('pad', ctypes.c_int32),
+                ('A', ctypes.c_void_p), ('lda', ctypes.c_int64), ('a_ms', ctypes.c_int64),
+                ('B', ctypes.c_void_p), ('ldb', ctypes.c_int64), ('b_ms', ctypes.c_int64),
+                ('bias', ctypes.c_void_p), ('bias_ms', ctypes.c_int64),
+                ('pre', ctypes.c_void_p), ('ld_pre', ctypes.c_int64), ('pre_ms', ctypes.c_int64),
+                ('out_f32', ctypes.c_void_p), ('ld_f32', ctypes.c_int64), ('f32_ms', ctypes.c_int64),
+                ('out_bf16', ctypes.c_void_p), ('ld_bf16', ctypes.c_int64), ('bf16_ms', ctypes.c_int64),
+                ('out_t', ctypes.c_void_p), ('ld_t', ctypes.c_int64), ('t_ms', ctypes.c_int64)]
+
+
+DM_MLP_EPI_GELU_FWD, DM_MLP_EPI_BIAS_F32, DM_MLP_EPI_GELU_BWD, DM_MLP_EPI_F32 = 0, 1, 2, 3
+
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
 _d = ctypes.c_double
@@ -138,6 +173,15 @@ SIGNATURES = {
     'dm_apply_pass_tc': (_i, [_vp, _i, ctypes.POINTER(DmTcPass), _vp, _sz, _vp, _vp]),
     'dm_batch_run': (_i, [_i, _vp, _sz, _vp, _sz, _vp, _sz, ctypes.POINTER(DmBatchInstance), _vp, _i,
                           ctypes.POINTER(DmBatchPass), _vp, _i, _vp, _vp, _vp]),
+    'dm_batch_run_params': (_i, [_i, ctypes.POINTER(DmParamProgram), ctypes.POINTER(DmParamProgram), _vp, _i, _i,
+                                 _vp, _sz, _vp, _sz, _vp, _vp]),
+    'dm_mlp_gemm_run': (_i, [ctypes.POINTER(DmMlpGemm), _vp, _vp]),
+    'dm_mlp_softmax_xent': (_i, [_vp, _vp, _i, _i, _i, ctypes.c_float, _vp, _vp, _vp, _vp, _vp]),
+    'dm_mlp_bias_grad': (_i, [_vp, ctypes.c_int64, ctypes.c_int64, _i, _i, _i, _vp, ctypes.c_int64, _vp]),
+    'dm_mlp_adam': (_i, [_vp, _vp, _vp, _vp, ctypes.c_int64, _i, ctypes.POINTER(ctypes.c_int32), _i, ctypes.c_float,
+                         ctypes.c_float, ctypes.c_float, ctypes.c_float, _i, _vp, _vp, _vp]),
+    'dm_mlp_gather': (_i, [_vp, _i, _vp, _i, ctypes.c_int64, _vp, _i, _i, _i, _vp, _vp, _vp, _vp]),
+    'dm_mlp_ensemble': (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     'dm_axis_probs': (_i, [_vp, _i, _i, _ip, _d, _vp, _vp]),
     'dm_nbasis_probs_scratch_bytes': (_sz, [_i]),
     'dm_nbasis_probs': (_i, [_vp, _i, _i, _dp, _d, _vp, _vp, _vp]),

@@ -46,12 +46,12 @@ class HostRecorder:
     def load(self, coeffs):
         raise BasicAerError('batched programs start from product states')
 
-    def map1(self, q, m):
-        self.ops.append(P.Op('map1', (q,), np.asarray(m, dtype=float)))
+    def map1(self, q, m, tag=None):
+        self.ops.append(P.Op('map1', (q,), np.asarray(m, dtype=float), tag=tag))
 
     def cx(self, ctl, tgt, tsp):
         coef, ideal = P.cx_coefficients(tsp)
-        self.ops.append(P.Op('cx', (ctl, tgt), np.array(coef), ideal))
+        self.ops.append(P.Op('cx', (ctl, tgt), np.array(coef), ideal, tag=('cx',)))
 
     def diag2(self, qa, qb, d):
         self.ops.append(P.Op('diag2', (qa, qb), np.asarray(d, dtype=float)))
@@ -85,12 +85,18 @@ class HostRecorder:
 def compile_experiment(experiment, options):
     """Op stream and final Z read-out of one experiment, through the backend's own run loop."""
     from .dm_simulator import DmSimulatorGPU
+    # the backend mirrors the reference's class-level rotation_error leak; an
+    # instance compile starts from the pristine default and leaves the class as it was
+    saved = DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error']
     DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
-    b = DmSimulatorGPU()
-    opts = dict(options)
-    opts['compute_densitymatrix'] = False
-    b._set_options(backend_options=opts)
-    rec = b.compile_experiment(experiment)
+    try:
+        b = DmSimulatorGPU()
+        opts = dict(options)
+        opts['compute_densitymatrix'] = False
+        b._set_options(backend_options=opts)
+        rec = b.compile_experiment(experiment)
+    finally:
+        DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = saved
     if len(rec.readouts) != 1 or any(m != 3 for m in rec.readouts[0][2]):
         raise BasicAerError('a batched instance must end with one Z ensemble measurement of every qubit')
     # the level's memory noise after the read-out does not change the probabilities
@@ -298,17 +304,25 @@ def compile_sweep(specs, variants, workers=None, kmax=None):
     """BatchTables for each variant ('single' or 'double') of one sweep, compiled once.
 
     ``kmax`` maps a qubit count to resident axes (default 7 for FP32, 6
-    for FP64); ``workers`` host processes share the host-side compile
-    (default: every core for large sweeps, in-process for small ones).
+    for FP64), or a precision name to such a map; ``workers`` host
+    processes share the host-side compile (default: every core for large
+    sweeps, in-process for small ones).
     """
     import os
     kmax = dict(kmax or {})
+    if not any(p in kmax for p in ('single', 'double')):
+        kmax = {p: kmax for p in variants}
     t0 = time.perf_counter()
     for spec in specs:
         for precision in variants:
             lo = N.DM_ROUND_AXES[N.DM_F32 if precision == 'single' else N.DM_F64]
             if not lo <= spec['n'] <= MAX_QUBITS:
                 raise BasicAerError('batched instances hold %d..%d qubits' % (lo, MAX_QUBITS))
+    for per_n in kmax.values():
+        for n, k in per_n.items():
+            if k < min(4, n):
+                # the two lowest qubits are always resident: a CX elsewhere needs two more axes
+                raise BasicAerError('a pass of %d-qubit instances needs at least %d resident axes' % (n, min(4, n)))
     if workers is None:
         workers = (os.cpu_count() or 1) if len(specs) >= 64 else 1
     keys = {}
@@ -320,7 +334,7 @@ def compile_sweep(specs, variants, workers=None, kmax=None):
     by_group = {}
     for key in order:
         n = key[0]
-        by_group[key] = [(p, kmax.get(n, 7 if p == 'single' else 6)) for p in variants]
+        by_group[key] = [(p, kmax.get(p, {}).get(n, 7 if p == 'single' else 6)) for p in variants]
     # compile_group takes one variant list; groups with equal lists are compiled together
     results = [None] * len(groups)
     for vlist in {tuple(v) for v in by_group.values()}:
@@ -474,32 +488,61 @@ class BatchProgram:
         return self.t.split(self.probs.cpu().numpy())
 
 
-def autotune(specs, precision='single', candidates=None, reps=2):
-    """Pick the resident-axis count per qubit count by timing each candidate on the device."""
+def autotune(specs, precision='single', candidates=None, sample=8, fill=None, reps=2):
+    """Pick the resident axes (pass width k) per qubit count by timing each candidate on the device.
+
+    For every qubit count in ``specs``, up to ``sample`` of its instances are
+    recorded once and planned for every candidate k; each plan runs as a
+    batch of ``fill`` instances (the sample repeated; default one per SM, so
+    the timing sees a full GPU's memory traffic) and the fastest k wins.
+    Returns ({n: k}, {(n, k): ms per launch}).
+    """
     import torch
-    candidates = candidates or ([5, 6, 7] if precision == 'single' else [4, 5, 6])
+    lo = N.DM_ROUND_AXES[N.DM_F32 if precision == 'single' else N.DM_F64]
+    hi = 7 if precision == 'single' else 6
+    candidates = candidates or list(range(max(lo, hi - 2), hi + 1))
+    if fill is None:
+        fill = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     by_n = {}
     for s in specs:
         by_n.setdefault(s['n'], []).append(s)
     choice, timings = {}, {}
     for n, group in sorted(by_n.items()):
-        sample = group[:8]
+        ks = [k for k in candidates if lo <= k <= min(n, hi)]
+        if len(ks) <= 1:
+            choice[n] = ks[0] if ks else min(n, hi)
+            continue
+        # a short prefix of each sampled instance is enough to rank pass widths
+        smp = [dict(sp, depth=min(sp['depth'], 12)) for sp in group[:sample]]
+        # one recording per instance, one plan per candidate (instances may differ in depth)
+        per_spec = [compile_group([sp], [(precision, k) for k in ks]) for sp in smp]
+        reps_specs = [smp[j % len(smp)] for j in range(max(fill, len(smp)))]
         best = None
-        for k in candidates:
-            if k > n or k < N.DM_ROUND_AXES[N.DM_F32 if precision == 'single' else N.DM_F64]:
-                continue
-            prog = BatchProgram(BatchTables(sample, precision, kmax={n: k}, workers=1))
-            prog.launch()
-            torch.cuda.synchronize()
+        for vi, k in sorted(enumerate(ks), key=lambda t: -t[1]):    # widest first: usually the fastest
+            plans, per_instance = [], []
+            for j in range(len(reps_specs)):
+                gplans, ginsts = per_spec[j % len(smp)][vi]
+                if j < len(smp):
+                    plans.extend(gplans)
+                _, block, err = ginsts[0]
+                per_instance.append((j % len(smp), block, err))    # plan j % len(smp): one per sample
+            prog = BatchProgram(BatchTables(reps_specs, precision, plans, per_instance, 0.0))
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record()
-            for _ in range(reps):
-                prog.launch()
+            prog.launch()
             b.record()
             torch.cuda.synchronize()
-            ms = a.elapsed_time(b) / reps
+            ms = a.elapsed_time(b)
+            if best is None or ms < 1.5 * best[0]:     # a clear loser is not timed again
+                a.record()
+                for _ in range(reps):
+                    prog.launch()
+                b.record()
+                torch.cuda.synchronize()
+                ms = a.elapsed_time(b) / reps
             timings[(n, k)] = ms
             if best is None or ms < best[0]:
                 best = (ms, k)
+            del prog
         choice[n] = best[1]
     return choice, timings

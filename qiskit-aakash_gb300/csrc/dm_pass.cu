@@ -779,6 +779,88 @@ namespace dmg {
 
 constexpr int kBatchMaxQubits = 12;   // the Z read-out's 2**n doubles fit one tile buffer
 
+// |0...0>: a = 2**-n on the {I, Z}**n sub-lattice, 0 elsewhere.  Called by all threads.
+template <typename T>
+__device__ void batch_init_zero(T *st, int n) {
+    const int tid = threadIdx.x;
+    const int64_t total = int64_t(1) << (2 * n);
+    for (int64_t e = int64_t(tid) * 4; e < total; e += 4 * kPipeThreads) {
+        st[e] = T(0);
+        st[e + 1] = T(0);
+        st[e + 2] = T(0);
+        st[e + 3] = T(0);
+    }
+    __syncthreads();
+    const T amp = T(ldexp(1.0, -n));
+    for (int i = tid; i < (1 << n); i += kPipeThreads) {
+        int64_t idx = 0;
+        for (int q = 0; q < n; ++q)
+            if ((i >> q) & 1) idx += int64_t(3) << (2 * q);
+        st[idx] = amp;
+    }
+    __syncthreads();
+}
+
+// Kernel parameters of one batched pass (the resident axes' strides from the pass table).
+template <int UNUSED = 0>
+__device__ void batch_pass_setup(PassRounds &ps, const dm_batch_pass &bp, int n) {
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        ps.n = n;
+        ps.k = bp.k;
+        ps.m = n - bp.k;
+        ps.nops = bp.nops;
+        ps.nrounds = bp.nrounds;
+        int low = 0;
+        while (low < bp.k && bp.axes[low] == n - 1 - low) ++low;
+        ps.low = low;
+        bool resident[DM_MAX_QUBITS] = {false};
+        for (int r = 0; r < bp.k; ++r) {
+            resident[bp.axes[r]] = true;
+            ps.res_stride[r] = int64_t(1) << (2 * (n - 1 - bp.axes[r]));
+        }
+        int m = 0;
+        for (int q = n - 1; q >= 0; --q)
+            if (!resident[q]) ps.nonres_stride[m++] = int64_t(1) << (2 * (n - 1 - q));
+    }
+    for (int r = tid; r < bp.nrounds; r += kPipeThreads) {
+        for (int i = 0; i < 4; ++i) ps.rax[r][i] = bp.round_axes[r][i];
+        ps.rend[r] = bp.round_end[r];
+    }
+    for (int o = tid; o < bp.nops; o += kPipeThreads) ps.ops[o] = bp.ops[o];
+}
+
+// Z read-out: gather the 2**n sub-lattice coefficients, scale by err**popcount,
+// Walsh-Hadamard transform in shared memory (outcome bit of qubit 0 is the MSB).
+template <typename T>
+__device__ void batch_z_readout(const T *st, int n, double err, double *out, double *wv) {
+    const int tid = threadIdx.x;
+    const int np = 1 << n;
+    for (int i = tid; i < np; i += kPipeThreads) {
+        int64_t idx = 0;
+        double w = 1.0;
+        for (int j = 0; j < n; ++j)
+            if ((i >> (n - 1 - j)) & 1) {
+                idx += int64_t(3) << (2 * (n - 1 - j));
+                w *= err;
+            }
+        wv[i] = double(st[idx]) * w;
+    }
+    __syncthreads();
+    for (int b = 0; b < n; ++b) {
+        for (int pidx = tid; pidx < np / 2; pidx += kPipeThreads) {
+            const int i0 = ((pidx >> b) << (b + 1)) | (pidx & ((1 << b) - 1));
+            const int i1 = i0 | (1 << b);
+            const double x = wv[i0], y = wv[i1];
+            wv[i0] = x + y;
+            wv[i1] = x - y;
+        }
+        __syncthreads();
+    }
+    for (int i = tid; i < np; i += kPipeThreads) out[i] = wv[i];
+    __syncthreads();
+}
+
 template <typename T, int R>
 __global__ void __launch_bounds__(kPipeThreads, 1)
     batch_kernel(T *__restrict__ states, double *__restrict__ probs, const T *__restrict__ mats,
@@ -796,80 +878,135 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
         const int ii = inst_s;
         if (ii >= ninst) break;
         const dm_batch_instance I = insts[ii];
-        const int n = I.n;
         T *st = states + I.state_off;
-        const int64_t total = int64_t(1) << (2 * n);
-        // |0...0>: a = 2**-n on the {I, Z}**n sub-lattice, 0 elsewhere
-        for (int64_t e = int64_t(tid) * 4; e < total; e += 4 * kPipeThreads) {
-            st[e] = T(0);
-            st[e + 1] = T(0);
-            st[e + 2] = T(0);
-            st[e + 3] = T(0);
-        }
-        __syncthreads();
-        const T amp = T(ldexp(1.0, -n));
-        for (int i = tid; i < (1 << n); i += kPipeThreads) {
-            int64_t idx = 0;
-            for (int q = 0; q < n; ++q)
-                if ((i >> q) & 1) idx += int64_t(3) << (2 * q);
-            st[idx] = amp;
-        }
-        __syncthreads();
+        batch_init_zero(st, I.n);
         for (int pi = 0; pi < I.npasses; ++pi) {
-            const dm_batch_pass &bp = passes[I.pass_begin + pi];
-            if (tid == 0) {
-                ps.n = n;
-                ps.k = bp.k;
-                ps.m = n - bp.k;
-                ps.nops = bp.nops;
-                ps.nrounds = bp.nrounds;
-                int low = 0;
-                while (low < bp.k && bp.axes[low] == n - 1 - low) ++low;
-                ps.low = low;
-                bool resident[DM_MAX_QUBITS] = {false};
-                for (int r = 0; r < bp.k; ++r) {
-                    resident[bp.axes[r]] = true;
-                    ps.res_stride[r] = int64_t(1) << (2 * (n - 1 - bp.axes[r]));
-                }
-                int m = 0;
-                for (int q = n - 1; q >= 0; --q)
-                    if (!resident[q]) ps.nonres_stride[m++] = int64_t(1) << (2 * (n - 1 - q));
-            }
-            for (int r = tid; r < bp.nrounds; r += kPipeThreads) {
-                for (int i = 0; i < 4; ++i) ps.rax[r][i] = bp.round_axes[r][i];
-                ps.rend[r] = bp.round_end[r];
-            }
-            for (int o = tid; o < bp.nops; o += kPipeThreads) ps.ops[o] = bp.ops[o];
+            batch_pass_setup(ps, passes[I.pass_begin + pi], I.n);
             __syncthreads();
             pipe_tiles<T, R>(st, ps, mats + I.mats_off, 0, 1, bufs, hi_off);
         }
-        // Z read-out: gather the 2**n sub-lattice coefficients, scale by err**popcount,
-        // Walsh-Hadamard transform in shared memory (outcome bit of qubit 0 is the MSB)
-        double *wv = reinterpret_cast<double *>(smem_raw);
-        const int np = 1 << n;
-        for (int i = tid; i < np; i += kPipeThreads) {
-            int64_t idx = 0;
-            double w = 1.0;
-            for (int j = 0; j < n; ++j)
-                if ((i >> (n - 1 - j)) & 1) {
-                    idx += int64_t(3) << (2 * (n - 1 - j));
-                    w *= I.meas_err;
-                }
-            wv[i] = double(st[idx]) * w;
+        batch_z_readout(st, I.n, I.meas_err, probs + I.prob_off, reinterpret_cast<double *>(smem_raw));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// parametric programs: coefficients composed per instance and per pass
+// ---------------------------------------------------------------------------
+
+constexpr int kCoefStride = 16;   // shared-memory coefficients per slot
+
+// m <- (rotation about `axis` by angle, error (e0, e1)) * m, rows k0 / k1 only.
+__device__ __forceinline__ void rot_apply(double (&m)[16], int axis, double angle, double e0, double e1) {
+    // planes of rx, ry, rz: (Y, Z), (Z, X), (X, Y)  (basicaertools.py:106-124)
+    const int k0 = axis == 0 ? 2 : axis == 1 ? 3 : 1;
+    const int k1 = axis == 0 ? 3 : axis == 1 ? 1 : 2;
+    double sn, cs;
+    sincos(angle + e1, &sn, &cs);
+    const double c = e0 * cs, s = e0 * sn;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const double a = m[4 * k0 + j], b = m[4 * k1 + j];
+        m[4 * k0 + j] = c * a - s * b;
+        m[4 * k1 + j] = s * a + c * b;
+    }
+}
+
+// m <- memory noise (f, p, g) * m: X, Y rows scaled by sqrt(g) f; Z <- g Z + (1 - g)(2p - 1) I.
+__device__ __forceinline__ void noise_apply(double (&m)[16], double f, double p, double g) {
+    const double k = sqrt(g) * f, d = (1 - g) * (2 * p - 1);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        m[4 + j] *= k;
+        m[8 + j] *= k;
+        m[12 + j] = g * m[12 + j] + d * m[j];
+    }
+}
+
+template <typename T>
+__device__ void compose_slot(const dm_param_program &P, int slot, const double *prm, T *out) {
+    const dm_param_slot sl = P.slots[slot];
+    const dm_recipe &first = P.recipes[P.chain[sl.begin]];
+    if (first.kind == DM_RECIPE_CX) {
+        const double cav = prm[9], mean = prm[10];
+        const double c2av = 4 * cav - 3;
+        double sn, cs, sn2, cs2;
+        sincos(mean, &sn, &cs);
+        sincos(2 * mean, &sn2, &cs2);
+        out[0] = T(cav * cs);
+        out[1] = T(cav * sn);
+        out[2] = T(0.5 * (1 + c2av * cs2));
+        out[3] = T(0.5 * (1 - c2av * cs2));
+        out[4] = T(c2av * sn * cs);
+        return;
+    }
+    double m[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) m[i] = (i % 5 == 0) ? 1.0 : 0.0;
+    for (int c = 0; c < sl.len; ++c) {
+        const dm_recipe &rc = P.recipes[P.chain[sl.begin + c]];
+        if (rc.kind == DM_RECIPE_ROT) {
+            for (int k = 0; k < rc.nrot; ++k) {
+                const int ax = rc.axis[k];
+                rot_apply(m, ax, rc.angle[k], prm[3 + 2 * ax], prm[4 + 2 * ax]);
+            }
+        } else if (rc.kind == DM_RECIPE_NOISE) {
+            noise_apply(m, prm[0], prm[1], prm[2]);
+        } else {   // DM_RECIPE_CONST: m <- C m (a diagonal pair map is a chain of one)
+            const double *cm = P.consts + rc.const_off;
+            if (sl.len == 1) {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) m[i] = cm[i];
+            } else {
+                double t[16];
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        t[4 * i + j] = cm[4 * i] * m[j] + cm[4 * i + 1] * m[4 + j] + cm[4 * i + 2] * m[8 + j] +
+                                       cm[4 * i + 3] * m[12 + j];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) m[i] = t[i];
+            }
         }
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) out[i] = T(m[i]);
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(kPipeThreads, 1)
+    batch_param_kernel(T *__restrict__ states, double *__restrict__ probs, const dm_param_program P,
+                       const double *__restrict__ params, int params_stride, int ninst, int *counter) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int64_t hi_off[64];
+    __shared__ PassRounds ps;
+    __shared__ __align__(16) T coef[DM_MAX_PASS_OPS * kCoefStride];
+    __shared__ double prm[DM_PARAMS_MIN_STRIDE];
+    __shared__ int inst_s;
+    T *bufs = reinterpret_cast<T *>(smem_raw);
+    const int tid = threadIdx.x;
+    const int n = P.n;
+    for (;;) {
+        if (tid == 0) inst_s = atomicAdd(counter, 1);
         __syncthreads();
-        for (int b = 0; b < n; ++b) {
-            for (int pidx = tid; pidx < np / 2; pidx += kPipeThreads) {
-                const int i0 = ((pidx >> b) << (b + 1)) | (pidx & ((1 << b) - 1));
-                const int i1 = i0 | (1 << b);
-                const double x = wv[i0], y = wv[i1];
-                wv[i0] = x + y;
-                wv[i1] = x - y;
+        const int ii = inst_s;
+        if (ii >= ninst) break;
+        if (tid < DM_PARAMS_MIN_STRIDE) prm[tid] = params[int64_t(ii) * params_stride + tid];
+        T *st = states + (int64_t(ii) << (2 * n));
+        batch_init_zero(st, n);     // its barriers also publish prm
+        int slot_base = 0;
+        for (int pi = 0; pi < P.npasses; ++pi) {
+            const dm_batch_pass &bp = P.passes[pi];
+            batch_pass_setup(ps, bp, n);
+            for (int o = tid; o < bp.nops; o += kPipeThreads) {
+                ps.ops[o].moff = o * kCoefStride;
+                compose_slot(P, slot_base + o, prm, coef + o * kCoefStride);
             }
             __syncthreads();
+            pipe_tiles<T, R>(st, ps, coef, 0, 1, bufs, hi_off);
+            slot_base += bp.nops;
         }
-        for (int i = tid; i < np; i += kPipeThreads) probs[I.prob_off + i] = wv[i];
-        __syncthreads();
+        batch_z_readout(st, n, prm[11], probs + (int64_t(ii) << n), reinterpret_cast<double *>(smem_raw));
     }
 }
 
@@ -891,6 +1028,7 @@ static int launch_batch(T *states, double *probs, const T *mats, const dm_batch_
     return launch_status();
 }
 
+// mats_len < 0: the pass's coefficients are composed on the device (moff is not read)
 static int validate_batch_pass(const dm_batch_pass &bp, int n, int R, int kmax, int64_t mats_len) {
     const int k = bp.k;
     if (k < R || k > kmax || k > n) return DM_ERR_PROGRAM;
@@ -917,7 +1055,7 @@ static int validate_batch_pass(const dm_batch_pass &bp, int n, int R, int kmax, 
                 case DM_OP_CX: need = 5; break;
                 default: return DM_ERR_PROGRAM;   // general 16x16 maps are not held in registers
             }
-            if (op.moff < 0 || op.moff + need > mats_len) return DM_ERR_PROGRAM;
+            if (mats_len >= 0 && (op.moff < 0 || op.moff + need > mats_len)) return DM_ERR_PROGRAM;
             const int da = (op.flags >> 8) & 3, db = (op.flags >> 12) & 3;
             if (op.a < 0 || op.a >= k || da >= R || bp.round_axes[r][da] != op.a) return DM_ERR_PROGRAM;
             if (op.kind != DM_OP_MAP1 &&
@@ -927,6 +1065,69 @@ static int validate_batch_pass(const dm_batch_pass &bp, int n, int R, int kmax, 
         prev_end = end;
     }
     return prev_end == bp.nops ? DM_OK : DM_ERR_PROGRAM;
+}
+
+template <typename T, int R>
+static int launch_batch_params(T *states, double *probs, const dm_param_program &P, const double *params,
+                               int params_stride, int ninst, int *counter, cudaStream_t s) {
+    const size_t smem = size_t(kPipeBuffers) * (size_t(1) << (2 * pipe_tile_axes<T>())) * sizeof(T);
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [smem] {
+        attr_err = cudaFuncSetAttribute(batch_param_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int(smem));
+    });
+    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    DM_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), s));
+    int grid = sm_count();
+    if (grid > ninst) grid = ninst;
+    batch_param_kernel<T, R><<<grid, kPipeThreads, smem, s>>>(states, probs, P, params, params_stride, ninst, counter);
+    count_launch();
+    return launch_status();
+}
+
+// Every table of a parametric program: passes as for dm_batch_run, slots and
+// recipe chains in range, and each slot's chain of a kind its op can take.
+static int validate_param_program(const dm_param_program &P, int R, int kmax) {
+    if (P.n < R || P.n > kBatchMaxQubits) return DM_ERR_RANGE;
+    if (P.npasses < 0 || P.nslots < 0 || P.nchain < 0 || P.nrecipes < 0 || P.nconsts < 0) return DM_ERR_PROGRAM;
+    if ((P.npasses && !P.passes) || (P.nslots && !P.slots) || (P.nchain && !P.chain) ||
+        (P.nrecipes && !P.recipes) || (P.nconsts && !P.consts))
+        return DM_ERR_ARG;
+    for (int r = 0; r < P.nrecipes; ++r) {
+        const dm_recipe &rc = P.recipes[r];
+        if (rc.kind == DM_RECIPE_ROT) {
+            if (rc.nrot < 1 || rc.nrot > 3) return DM_ERR_PROGRAM;
+            for (int k = 0; k < rc.nrot; ++k)
+                if (rc.axis[k] < 0 || rc.axis[k] > 2) return DM_ERR_PROGRAM;
+        } else if (rc.kind == DM_RECIPE_CONST) {
+            if (rc.const_off < 0 || int64_t(rc.const_off) + 16 > P.nconsts) return DM_ERR_PROGRAM;
+        } else if (rc.kind != DM_RECIPE_NOISE && rc.kind != DM_RECIPE_CX) {
+            return DM_ERR_PROGRAM;
+        }
+    }
+    for (int c = 0; c < P.nchain; ++c)
+        if (P.chain[c] < 0 || P.chain[c] >= P.nrecipes) return DM_ERR_PROGRAM;
+    int slot = 0;
+    for (int p = 0; p < P.npasses; ++p) {
+        const dm_batch_pass &bp = P.passes[p];
+        const int rc = validate_batch_pass(bp, P.n, R, kmax, -1);
+        if (rc) return rc;
+        for (int o = 0; o < bp.nops; ++o, ++slot) {
+            if (slot >= P.nslots) return DM_ERR_PROGRAM;
+            const dm_param_slot sl = P.slots[slot];
+            if (sl.len < 1 || sl.begin < 0 || int64_t(sl.begin) + sl.len > P.nchain) return DM_ERR_PROGRAM;
+            const int kind = bp.ops[o].kind;
+            for (int c = 0; c < sl.len; ++c) {
+                const int rk = P.recipes[P.chain[sl.begin + c]].kind;
+                const bool ok = kind == DM_OP_MAP1 ? (rk != DM_RECIPE_CX)
+                                                   : (sl.len == 1 && rk == (kind == DM_OP_CX ? DM_RECIPE_CX
+                                                                                             : DM_RECIPE_CONST));
+                if (!ok) return DM_ERR_PROGRAM;
+            }
+        }
+    }
+    return slot == P.nslots ? DM_OK : DM_ERR_PROGRAM;
 }
 
 }  // namespace dmg
@@ -963,4 +1164,26 @@ extern "C" int dm_batch_run(int dtype, void *states_dev, size_t states_count, do
     return launch_batch<float, DM_ROUND_AXES_F32>(static_cast<float *>(states_dev), probs_dev,
                                                   static_cast<const float *>(mats_dev), insts_dev, ninst, passes_dev,
                                                   counter_dev, s);
+}
+
+extern "C" int dm_batch_run_params(int dtype, const dm_param_program *host, const dm_param_program *dev,
+                                   const double *params_dev, int params_stride, int ninst, void *states_dev,
+                                   size_t states_count, double *probs_dev, size_t probs_count, int *counter_dev,
+                                   void *stream) {
+    DM_CHECK_ARG(valid_dtype(dtype) && host && dev && params_dev && states_dev && probs_dev && counter_dev);
+    DM_CHECK_ARG(ninst >= 1 && params_stride >= DM_PARAMS_MIN_STRIDE);
+    if (reinterpret_cast<uintptr_t>(states_dev) & 15) return DM_ERR_ARG;
+    const int R = dtype == DM_F64 ? DM_ROUND_AXES_F64 : DM_ROUND_AXES_F32;
+    const int kmax = dtype == DM_F64 ? 6 : 7;
+    const int rc = validate_param_program(*host, R, kmax);
+    if (rc) return rc;
+    if (host->n != dev->n || host->npasses != dev->npasses || host->nslots != dev->nslots) return DM_ERR_ARG;
+    if (size_t(ninst) * (size_t(1) << (2 * host->n)) > states_count) return DM_ERR_ARG;
+    if (size_t(ninst) * (size_t(1) << host->n) > probs_count) return DM_ERR_ARG;
+    cudaStream_t s = as_stream(stream);
+    if (dtype == DM_F64)
+        return launch_batch_params<double, DM_ROUND_AXES_F64>(static_cast<double *>(states_dev), probs_dev, *dev,
+                                                              params_dev, params_stride, ninst, counter_dev, s);
+    return launch_batch_params<float, DM_ROUND_AXES_F32>(static_cast<float *>(states_dev), probs_dev, *dev, params_dev,
+                                                         params_stride, ninst, counter_dev, s);
 }

@@ -23,6 +23,7 @@
 #include <mutex>
 
 #include "dm_common.cuh"
+#include "dm_tcgen05.cuh"
 
 namespace dmg {
 
@@ -37,7 +38,6 @@ constexpr uint32_t kABytes = kGroups * 64 * 4; // 64 KB
 constexpr uint32_t kBBytes = 64 * 64 * 4;      // 16 KB
 constexpr uint32_t kSmemBytes = kNatBytes + 2 * kABytes + 2 * kBBytes;   // 224 KB
 constexpr uint32_t kTmemCols = 128;            // two M = 128 blocks x N = 64
-constexpr int kSpinLimit = 1 << 24;            // bounded waits (about a second)
 
 // K-major core-matrix layout (no swizzle) of a rows x 64 operand: element
 // (row, k) lives at byte (row%8)*16 + (k%4)*4 + (k/4)*128 + (row/8)*2048.
@@ -47,17 +47,14 @@ constexpr uint32_t kLBO = 128, kSBO = 2048;
 __device__ __forceinline__ uint32_t row_off(int row) { return (row & 7) * 16 + (row >> 3) * kSBO; }
 __device__ __forceinline__ uint32_t k_off(int k) { return (k & 3) * 4 + (k >> 2) * kLBO; }
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
+using tcg::cp_async16;
+using tcg::cp_async_commit;
+using tcg::cp_async_wait_all;
+using tcg::mbar_wait;
+using tcg::smem_u32;
+using tcg::tmem_ld64;
 
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
-    uint64_t d = uint64_t((saddr >> 4) & 0x3FFF);
-    d |= uint64_t((kLBO >> 4) & 0x3FFF) << 16;
-    d |= uint64_t((kSBO >> 4) & 0x3FFF) << 32;
-    d |= uint64_t(1) << 46;   // sm_100 descriptor version; base offset 0, no swizzle
-    return d;
-}
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) { return tcg::smem_desc(saddr, kLBO, kSBO); }
 
 // kind::tf32, D = F32, A = B = TF32, both K-major, M = 128, N = 64.
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
@@ -66,27 +63,8 @@ __device__ __forceinline__ float tf32_rn(float x) {
     return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
 // Natural-layout swizzle of the tile (16-byte chunks intact), as in dm_pass.cu.
 __device__ __forceinline__ int nat_swz(int e) { return e ^ ((((e >> 5) ^ (e >> 8)) & 7) << 2); }
-
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-    for (int it = 0; it < kSpinLimit; ++it) {
-        uint32_t ok;
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(ok)
-            : "r"(mbar), "r"(parity)
-            : "memory");
-        if (ok) return true;
-    }
-    return false;
-}
 
 struct Round {
     int8_t digits[3];
@@ -130,27 +108,6 @@ __device__ __forceinline__ void digit_tables(const uint32_t *kc, uint32_t (&t)[3
         t[d][2] = kc[2 * d + 1];
         t[d][3] = kc[2 * d] ^ kc[2 * d + 1];
     }
-}
-
-__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
-    uint32_t r[64];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x64.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,"
-        "%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,"
-        "%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
-          "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
-          "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
-          "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
-          "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int j = 0; j < 64; ++j) v[j] = __uint_as_float(r[j]);
 }
 
 __device__ __forceinline__ void put_split(unsigned char *AH, unsigned char *AL, uint32_t o, float x) {

@@ -404,7 +404,7 @@ class DmSimulatorGPU(_Base):
         m = np.eye(4)
         for axis, angle in gate:
             m = P.rotation_ptm(axis, angle, self._error_params['one_qubit_gates'][axis]) @ m
-        self._dev.map1(qubit, m)
+        self._dev.map1(qubit, m, tag=('rot', tuple((axis, float(angle)) for axis, angle in gate)))
 
     def _add_unitary_two(self, qubit0, qubit1):
         """dm_simulator.py:386-395 (cx_gate_dm_matrix, basicaertools.py:310-392)."""
@@ -419,7 +419,7 @@ class DmSimulatorGPU(_Base):
         if np.array_equal(m, np.eye(4)):
             return
         for q in range(self._number_of_qubits):
-            self._dev.map1(q, m)
+            self._dev.map1(q, m, tag=('noise',))
 
     def _add_qasm_measure(self, basis, qubit, err_param, nvec=None):
         self._dev.map1(qubit, P.measure_ptm(basis, err_param, nvec))

@@ -116,7 +116,7 @@ class DeviceState:
                a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), self.stream)
 
     # -- queued operations ---------------------------------------------------
-    def map1(self, q, m):
+    def map1(self, q, m, tag=None):
         self.pending.append(Op('map1', (q,), np.asarray(m, dtype=np.float64)))
 
     def cx(self, ctl, tgt, tsp):

@@ -141,16 +141,19 @@ class Op:
     ``src`` lists the indices (in the planner's input) of the operations this
     one stands for: a composed 4x4 map lists the maps it multiplies, in
     application order.  Batched programs use it to rebuild the coefficients
-    of a shared plan for each instance.
+    of a shared plan for each instance.  ``tag`` names where a 4x4 map came
+    from (('rot', rotations) for a gate, ('noise',) for memory noise), so a
+    template program can recompute it from an instance's noise parameters.
     """
-    __slots__ = ('kind', 'axes', 'data', 'ideal', 'src')
+    __slots__ = ('kind', 'axes', 'data', 'ideal', 'src', 'tag')
 
-    def __init__(self, kind, axes, data, ideal=False, src=None):
+    def __init__(self, kind, axes, data, ideal=False, src=None, tag=None):
         self.kind = kind
         self.axes = tuple(axes)
         self.data = data
         self.ideal = ideal
         self.src = src
+        self.tag = tag
 
     def __repr__(self):
         return 'Op(%s, %s)' % (self.kind, self.axes)

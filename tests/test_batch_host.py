@@ -105,6 +105,8 @@ def test_batch_rejects_unsupported_instances():
         B.BatchTables([dict(B.sweep_specs(1, seed=1)[0], n=13)])
     with pytest.raises(Exception):
         B.BatchTables([dict(B.sweep_specs(1, seed=1)[0], n=2)], 'single')
+    with pytest.raises(Exception):
+        B.BatchTables(B.sweep_specs(2, seed=1, n_range=(6, 6)), 'single', kmax={6: 3})
 
 
 def test_sweep_specs_ranges():

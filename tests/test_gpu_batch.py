@@ -1,0 +1,113 @@
+"""Batched noise sweep on the GPU: every instance of one dm_batch_run launch
+against the oracle (small instances) and against the single-experiment
+backend (larger ones), graph replay, and table rejection on the host."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import dm_oracle as O
+from qiskit_aakash_gb300 import _native as N
+from qiskit_aakash_gb300 import batch as B
+
+pytestmark = pytest.mark.gpu
+
+TOL = {'double': 1e-12, 'single': 2e-5}
+
+
+def oracle_probs(spec):
+    exp, opts = B.instance_experiment(spec)
+    res = O.OracleDmSimulator(dict(opts, compute_densitymatrix=False)).run_experiment(exp)
+    p = res['data']['ensemble_probability']
+    return np.array([p[k] for k in O.bitstring_keys(spec['n'])])
+
+
+@pytest.fixture(scope='module')
+def small_sweep():
+    specs = B.sweep_specs(40, seed=21, n_range=(3, 8), depth_range=(2, 12))
+    return specs, [oracle_probs(s) for s in specs]
+
+
+@pytest.mark.parametrize('precision', ['double', 'single'])
+def test_batch_matches_oracle(small_sweep, precision):
+    specs, want = small_sweep
+    prog = B.BatchProgram(B.BatchTables(specs, precision))
+    prog.launch()
+    got = prog.results()
+    for i, spec in enumerate(specs):
+        assert np.max(np.abs(got[i] - want[i])) < TOL[precision], (i, spec)
+        assert abs(got[i].sum() - 1.0) < TOL[precision]
+
+
+@pytest.mark.parametrize('precision,kmax', [('single', {8: 5, 7: 4, 6: 4}), ('double', {8: 4, 7: 4, 6: 5})])
+def test_batch_resident_axes_do_not_change_results(small_sweep, precision, kmax):
+    specs, want = small_sweep
+    prog = B.BatchProgram(B.BatchTables(specs, precision, kmax=kmax))
+    prog.launch()
+    for i, g in enumerate(prog.results()):
+        assert np.max(np.abs(g - want[i])) < TOL[precision]
+
+
+def test_batch_large_instances_match_backend():
+    from qiskit_aakash_gb300.dm_simulator import DmSimulatorGPU
+    specs = B.sweep_specs(6, seed=4, n_range=(10, 12), depth_range=(8, 20))
+    for precision in ('double', 'single'):
+        prog = B.BatchProgram(B.BatchTables(specs, precision))
+        prog.launch()
+        got = prog.results()
+        for i, spec in enumerate(specs):
+            exp, opts = B.instance_experiment(spec)
+            DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
+            be = DmSimulatorGPU()
+            be._set_options(backend_options=dict(opts, compute_densitymatrix=False, precision='double'))
+            res = be.run_experiment(exp)
+            p = res['data']['ensemble_probability']
+            ref = np.array([p[k] for k in O.bitstring_keys(spec['n'])])
+            assert np.max(np.abs(got[i] - ref)) < TOL[precision] * 10, (precision, i)
+
+
+def test_batch_graph_replay_and_rerun():
+    import torch
+    specs = B.sweep_specs(30, seed=8, n_range=(3, 9), depth_range=(2, 10))
+    prog = B.BatchProgram(B.BatchTables(specs, 'single'))
+    prog.capture()
+    torch.cuda.synchronize()
+    first = [r.copy() for r in prog.results()]
+    prog.probs.zero_()
+    prog.states.fill_(float('nan'))
+    for _ in range(3):
+        prog.run()
+    torch.cuda.synchronize()
+    for a, b in zip(first, prog.results()):
+        assert np.array_equal(a, b)
+
+
+def test_batch_rejects_bad_tables():
+    specs = B.sweep_specs(3, seed=2, n_range=(4, 5), depth_range=(2, 4))
+    prog = B.BatchProgram(B.BatchTables(specs, 'single'))
+    t = prog.t
+    bad = (N.DmBatchPass * t.npasses).from_buffer_copy(bytes(t.passes))
+    bad[0].axes[0] -= 1
+    vp = ctypes.c_void_p
+    args = lambda insts, passes, npasses: (  # noqa: E731
+        N.DM_F32, vp(prog.states.data_ptr()), ctypes.c_size_t(t.states_count), vp(prog.probs.data_ptr()),
+        ctypes.c_size_t(t.probs_count), vp(prog.mats_dev.data_ptr()), ctypes.c_size_t(t.mats.size), insts,
+        vp(prog.insts_dev.data_ptr()), t.ninst, passes, vp(prog.passes_dev.data_ptr()), npasses,
+        vp(prog.counter.data_ptr()), vp(prog.status.data_ptr()), None)
+    with pytest.raises(N.NativeError) as e:
+        N.call('dm_batch_run', *args(t.insts, bad, t.npasses))
+    assert e.value.code == N.DM_ERR_PROGRAM
+    insts = (N.DmBatchInstance * t.ninst).from_buffer_copy(bytes(t.insts))
+    insts[0].state_off = t.states_count
+    with pytest.raises(N.NativeError) as e:
+        N.call('dm_batch_run', *args(insts, t.passes, t.npasses))
+    assert e.value.code == N.DM_ERR_ARG
+    insts = (N.DmBatchInstance * t.ninst).from_buffer_copy(bytes(t.insts))
+    insts[0].n = 13
+    with pytest.raises(N.NativeError) as e:
+        N.call('dm_batch_run', *args(insts, t.passes, t.npasses))
+    assert e.value.code == N.DM_ERR_RANGE
+    insts = (N.DmBatchInstance * t.ninst).from_buffer_copy(bytes(t.insts))
+    insts[0].mats_len = 1
+    with pytest.raises(N.NativeError):
+        N.call('dm_batch_run', *args(insts, t.passes, t.npasses))
