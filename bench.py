@@ -68,7 +68,10 @@ def parse():
     ap.add_argument('--surrogate-train', type=int, default=131072,
                     help='training points of the noise surrogate (0 skips the surrogate leg)')
     ap.add_argument('--surrogate-test', type=int, default=16384, help='held-out points of the noise surrogate')
-    ap.add_argument('--surrogate-epochs', type=int, default=8)
+    ap.add_argument('--surrogate-epochs', type=int, default=40)
+    ap.add_argument('--legs', default='headline,batch,surrogate',
+                    help='comma list of legs to run (the JSON line keeps only what ran)')
+    ap.add_argument('--no-autotune', action='store_true', help='batched sweep with the widest passes, untuned')
     return ap.parse_args()
 
 
@@ -363,7 +366,10 @@ def batch_leg(args, pkg, torch, N):
     from qiskit_aakash_gb300 import batch as B
     specs = B.sweep_specs(args.batch, seed=args.seed)
     t0 = time.perf_counter()
-    choice, tune_ms = B.autotune(specs, 'single')
+    if args.no_autotune:
+        choice, tune_ms = {n: min(7, n) for n in range(6, 13)}, {}
+    else:
+        choice, tune_ms = B.autotune(specs, 'single')
     tune_s = time.perf_counter() - t0
     tables = B.compile_sweep(specs, ['single', 'double'], kmax={'single': choice})
     t32, t64 = tables['single'], tables['double']
@@ -495,16 +501,8 @@ def surrogate_leg(args, torch):
     }
 
 
-def run_ours(args):
-    import torch
-    world, rank, local = dist_setup(args)
-    if world > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group('nccl')
-    pkg = __graft_entry__.build()
-    from qiskit_aakash_gb300 import _native as N
-    from qiskit_aakash_gb300.dm_simulator import DmSimulatorGPU
+def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
+    """The n=16 layered workload: TC FP32 (value), CUDA-core FP32, FP64, e2e; None on ranks != 0."""
     n, layers = args.n, args.layers
     seed = args.seed + rank
     qc, opts = workload(pkg, n, layers, seed)
@@ -628,14 +626,33 @@ def run_ours(args):
         'gpu_launches': int(launches),
         'clocks': clocks.summary(),
     }
-    if not args.no_gate_kinds:
+    return line
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup(args)
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    pkg = __graft_entry__.build()
+    from qiskit_aakash_gb300 import _native as N
+    from qiskit_aakash_gb300.dm_simulator import DmSimulatorGPU
+    legs = set(args.legs.split(','))
+    line = headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank) if 'headline' in legs else None
+    if rank != 0:
+        return None
+    if line is None:
+        line = {'metric': METRIC, 'legs': sorted(legs), 'note': 'headline leg not run'}
+    if 'headline' in legs and not args.no_gate_kinds:
         line['per_gate_kind_fp64'] = per_gate_kind(torch, N)
-    if args.batch > 0:
+    if 'batch' in legs and args.batch > 0:
         line['batched_sweep'] = batch_leg(args, pkg, torch, N)
-    if args.surrogate_train > 0:
+    if 'surrogate' in legs and args.surrogate_train > 0:
         line['noise_surrogate'] = surrogate_leg(args, torch)
-    if not args.no_cpu:
-        line['cpu_baseline'] = cpu_sample(pkg, n, args.seed)
+    if 'headline' in legs and not args.no_cpu:
+        line['cpu_baseline'] = cpu_sample(pkg, args.n, args.seed)
     return line
 
 
