@@ -391,6 +391,11 @@ int dm_gather(const void *state_dev, int n, int dtype, const int64_t *idx, int c
  * Replaces DmSimulatorPy._get_densitymatrix's chop, dm_simulator.py:1257-1269. */
 int dm_chop_copy(const void *state_dev, int n, int dtype, double threshold, double *out_dev, void *stream);
 
+/* dm_chop_copy of coefficients offset .. offset + count - 1 only (out_dev holds count
+ * values), so a large state can be copied out in chunks that overlap the host copies. */
+int dm_chop_copy_range(const void *state_dev, int n, int dtype, int64_t offset, int64_t count, double threshold,
+                       double *out_dev, void *stream);
+
 /* Pauli basis -> 2**n x 2**n complex128 matrix (interleaved re/im, row-major).
  * Replaces DmSimulatorPy._compute_densitymatrix, dm_simulator.py:1198-1255.
  * scratch_dev: dm_pauli_to_matrix_scratch_bytes(n) bytes. */

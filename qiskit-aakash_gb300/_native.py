@@ -188,6 +188,7 @@ SIGNATURES = {
     'dm_nbasis_probs_noalloc': (_i, [_vp, _i, _i, _dp, _d, _vp, _vp]),
     'dm_gather': (_i, [_vp, _i, _i, _i64p, _i, _vp, _vp]),
     'dm_chop_copy': (_i, [_vp, _i, _i, _d, _vp, _vp]),
+    'dm_chop_copy_range': (_i, [_vp, _i, _i, ctypes.c_int64, ctypes.c_int64, _d, _vp, _vp]),
     'dm_pauli_to_matrix_scratch_bytes': (_sz, [_i]),
     'dm_pauli_to_matrix': (_i, [_vp, _i, _i, _vp, _vp, _vp]),
     'dm_overlap_scratch_bytes': (_sz, [_i]),

@@ -207,8 +207,19 @@ extern "C" int dm_load_state(void *state_dev, int n, int dtype, const double *ho
 
 extern "C" int dm_chop_copy(const void *state_dev, int n, int dtype, double threshold, double *out_dev,
                             void *stream) {
+    DM_CHECK_ARG(valid_n(n));
+    return dm_chop_copy_range(state_dev, n, dtype, 0, pow4(n), threshold, out_dev, stream);
+}
+
+extern "C" int dm_chop_copy_range(const void *state_dev, int n, int dtype, int64_t offset, int64_t count,
+                                  double threshold, double *out_dev, void *stream) {
     DM_CHECK_ARG(state_dev && out_dev && valid_n(n) && valid_dtype(dtype));
-    const int64_t total = pow4(n);
+    DM_CHECK_ARG(offset >= 0 && count > 0 && offset + count <= pow4(n));
+    const int64_t total = count;
+    if (dtype == DM_F64)
+        state_dev = static_cast<const double *>(state_dev) + offset;
+    else
+        state_dev = static_cast<const float *>(state_dev) + offset;
     cudaStream_t s = as_stream(stream);
     if (dtype == DM_F64)
         chop_kernel<double><<<grid_for(total, 256), 256, 0, s>>>(static_cast<const double *>(state_dev), total,

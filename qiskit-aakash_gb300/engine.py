@@ -21,6 +21,31 @@ from .program import TC_AXES, Op, cx_coefficients, encode_pass, encode_pass_tc, 
 DEFAULT_TILE_AXES = {'double': 6, 'single': 7}
 DEFAULT_LOW_AXES = 2
 
+# Copy-out of large states: 32 Mi coefficients (256 MB FP64) per chunk, two
+# device and two pinned host buffers per device, host copies in 16 MB slices.
+_COPY_CHUNK = 1 << 25
+_HOST_SLICE = 1 << 21
+_COPY_BUFFERS = {}
+_POOL = []
+
+
+def _copy_buffers(device):
+    torch = _torch()
+    key = (str(device), _COPY_CHUNK)
+    if key not in _COPY_BUFFERS:
+        dev = [torch.empty(_COPY_CHUNK, dtype=torch.float64, device=device) for _ in range(2)]
+        pinned = [torch.empty(_COPY_CHUNK, dtype=torch.float64).pin_memory() for _ in range(2)]
+        _COPY_BUFFERS[key] = (dev, pinned)
+    return _COPY_BUFFERS[key]
+
+
+def _host_pool():
+    if not _POOL:
+        import os
+        from concurrent.futures import ThreadPoolExecutor
+        _POOL.append(ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1))))
+    return _POOL[0]
+
 
 def _torch():
     import torch
@@ -228,13 +253,49 @@ class DeviceState:
         return np.concatenate(out)
 
     def coefficients(self, chop_threshold):
-        """FP64 copy of the coefficients with |a| < chop_threshold set to 0."""
+        """FP64 copy of the coefficients with |a| < chop_threshold set to 0.
+
+        Large states stream out in chunks: the chop kernel fills one of two
+        device buffers, an async copy moves it to one of two pinned host
+        buffers, and host threads copy the previous chunk into the result
+        while the GPU works on the next one.
+        """
         self.flush()
         torch = _torch()
-        out = torch.empty(4 ** self.n, dtype=torch.float64, device=self.device)
-        N.call('dm_chop_copy', self.ptr, self.n, self.dtype, float(chop_threshold),
-               ctypes.c_void_p(out.data_ptr()), self.stream)
-        return self._to_host(out)
+        total = 4 ** self.n
+        if total <= _COPY_CHUNK:
+            out = torch.empty(total, dtype=torch.float64, device=self.device)
+            N.call('dm_chop_copy', self.ptr, self.n, self.dtype, float(chop_threshold),
+                   ctypes.c_void_p(out.data_ptr()), self.stream)
+            return self._to_host(out)
+        result = np.empty(total, dtype=np.float64)
+        dev, pinned = _copy_buffers(self.device)
+        stream = torch.cuda.current_stream(self.device)
+        events = [None, None]
+        pending = None
+        pool = _host_pool()
+
+        def drain(item):
+            b, off, cnt = item
+            events[b].synchronize()
+            src = pinned[b].numpy()
+            parts = [(s0, min(cnt, s0 + _HOST_SLICE)) for s0 in range(0, cnt, _HOST_SLICE)]
+            list(pool.map(lambda r: np.copyto(result[off + r[0]:off + r[1]], src[r[0]:r[1]]), parts))
+
+        for i, off in enumerate(range(0, total, _COPY_CHUNK)):
+            b = i % 2
+            cnt = min(_COPY_CHUNK, total - off)
+            N.call('dm_chop_copy_range', self.ptr, self.n, self.dtype, ctypes.c_int64(off), ctypes.c_int64(cnt),
+                   float(chop_threshold), ctypes.c_void_p(dev[b].data_ptr()), self.stream)
+            pinned[b][:cnt].copy_(dev[b][:cnt], non_blocking=True)
+            events[b] = torch.cuda.Event()
+            events[b].record(stream)
+            if pending is not None:
+                drain(pending)      # the other buffer pair: its host copy overlaps this chunk's GPU work
+            pending = (b, off, cnt)
+        drain(pending)
+        self.d2h_bytes += total * 8
+        return result
 
     def raw_coefficients(self):
         """FP64 copy of the unchopped coefficients."""

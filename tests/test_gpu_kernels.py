@@ -243,3 +243,24 @@ def test_tensor_core_pass_rejects_bad_programs(torch):
     for mut in (bad_axes, bad_umoff, bad_row, bad_vec):
         assert rc_of(mut) == N.DM_ERR_PROGRAM, mut.__name__
     assert status.item() == 0
+
+
+@pytest.mark.parametrize('dtype', [N.DM_F64, N.DM_F32])
+def test_chunked_copy_out_equals_one_shot(torch, dtype, monkeypatch):
+    """DeviceState.coefficients in chunks (chop range kernel, pinned double buffers) = dm_chop_copy."""
+    from qiskit_aakash_gb300 import engine
+    n = 7
+    rng = np.random.default_rng(5)
+    st = rng.normal(size=4 ** n) * 2.0 ** -n
+    st[rng.random(4 ** n) < 0.3] *= 1e-17
+    ds = engine.DeviceState(n, precision='double' if dtype == N.DM_F64 else 'single')
+    ds.load(st)
+    one = ds.coefficients(1e-15)
+    monkeypatch.setattr(engine, '_COPY_CHUNK', 1000)     # 17 chunks, the last one ragged
+    monkeypatch.setattr(engine, '_HOST_SLICE', 96)
+    chunked = ds.coefficients(1e-15)
+    assert np.array_equal(one, chunked)
+    with pytest.raises(N.NativeError):
+        out = torch.empty(10, dtype=torch.float64, device='cuda')
+        N.call('dm_chop_copy_range', ds.ptr, n, dtype, ctypes.c_int64(4 ** n - 5), ctypes.c_int64(10), 0.0,
+               vp(out), stream(torch))
