@@ -130,18 +130,19 @@ int dm_apply_pass(void *state_dev, int n, int dtype, const dm_pass *pass, const 
                   size_t mats_count, void *stream);
 
 /* A tensor-core pass.  Every tile of 4**7 coefficients (the 7 resident
- * axes) is viewed, round by round, as a 256 x 64 operand: rows are groups,
- * K the 64 coefficients of the round's 3 axes, stored in the K-major
- * core-matrix layout byte(row, k) = (row%8)*16 + (k%4)*4 + (k/4)*128 +
- * (row/8)*2048.  A round is D = X U^T with U the 64x64 transfer matrix of
+ * axes) is viewed, round by round, as a 256 x 64 FP16 operand: rows are
+ * groups, K the 64 coefficients of the round's 3 axes, stored in the K-major
+ * core-matrix layout byte(row, k) = (row%8)*16 + (k%8)*2 + (k/8)*128 +
+ * (row/8)*1024.  A round is D = X U^T with U the 64x64 transfer matrix of
  * its composed operations.  Layout offsets are XOR-combinations of one
  * offset per index bit (every operand-layout bit contributes a distinct
  * power of two, and the natural tile layout is XOR-linear). */
 typedef struct dm_tc_round {
     int8_t digits[3];     /* local axes of K digits 0, 1, 2 (j = d0 + 4 d1 + 16 d2) */
-    int8_t vec;           /* digit whose 4 values this round's epilogue stores as one 128-bit vector, or -1 */
-    int32_t umoff;        /* float offset of the round's matrix image: 4096 TF32-rounded hi floats then 4096
-                             lo remainders, float (n%8)*4 + k%4 + (k/4)*32 + (n/8)*512 for output n, input k */
+    int8_t vec;           /* digit whose 4 values the epilogue stores as one vector (8 bytes of FP16 into
+                             the next operand, 16 bytes of FP32 into the natural tile), or -1 */
+    int32_t umoff;        /* FP16-value offset of the round's matrix images: 2**11 Uh, Uh, Ul (4096 each),
+                             value (n%8)*8 + k%8 + (k/8)*64 + (n/8)*512 for output n, input k */
     uint32_t rowc[8];     /* destination offset of row bit i of this round: bytes into the next round's
                              operand, or, after the last round, elements of the natural tile */
     uint32_t kc[6];       /* destination offset of K bit i of this round */
@@ -158,11 +159,14 @@ typedef struct dm_tc_pass {
 } dm_tc_pass;
 
 /* The fused pass on the tensor cores (FP32 state only, n >= 7): the rounds
- * run as tcgen05.mma kind::tf32 in 3xTF32 (hi/lo split of state and matrix,
- * FP32 accumulation in tensor memory).  umats_dev holds umats_count floats.
- * status_dev (device int, 0 before the first call) is set to 1 if the kernel
- * abandons a bounded wait.  Same role as dm_apply_pass (dm_simulator.py:1005-1177). */
-int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, const float *umats_dev, size_t umats_count,
+ * run as tcgen05.mma kind::f16 on a 3-way FP16 split (the tile in units of
+ * 2**-n, x = h + 2**-11 l; U = Uh + 2**-11 Ul; one FP32 accumulator in
+ * tensor memory collects h (2**11 Uh)^T + l Uh^T + h Ul^T).  The state must
+ * be physical enough that |2**n a| < 65504.  umats_dev holds umats_count
+ * FP16 values (uint16_t bits).  status_dev (device int, 0 before the first
+ * call) is set to 1 if the kernel abandons a bounded wait.  Same role as
+ * dm_apply_pass (dm_simulator.py:1005-1177). */
+int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, const uint16_t *umats_dev, size_t umats_count,
                      int *status_dev, void *stream);
 
 /* ------------------------------------------------------------- batched sweeps */

@@ -513,18 +513,39 @@ __device__ __forceinline__ void pipe_tiles(T *__restrict__ st, const PassRounds 
                 t2s[d] = R > 2 ? swz16<T>(d << (2 * a2)) : 0;
             }
             const int ope = p.rend[r];
+            // With local axis 0 (the tile's fastest, 16-byte-chunk axis) as round digit 0, a
+            // group's four values along it are one aligned 16-byte vector (FP32) or two (FP64).
+            const bool vec = sizeof(T) == 4 && a0 == 0;
             for (int g = tid; g < ngroups; g += kPipeThreads) {
                 int gb = insert_zero_digit32(g, a0);
                 gb = insert_zero_digit32(gb, a1);
                 if (R > 2) gb = insert_zero_digit32(gb, a2);
                 int pb = swz16<T>(gb);
                 T v[G];
+                if (vec) {
 #pragma unroll
-                for (int j = 0; j < G; ++j) v[j] = tile[pb ^ t0s[j & 3] ^ t1s[(j >> 2) & 3] ^ t2s[(j >> 4) & 3]];
+                    for (int m = 0; m < G / 4; ++m) {
+                        const float4 q = *reinterpret_cast<const float4 *>(tile + (pb ^ t1s[m & 3] ^ t2s[(m >> 2) & 3]));
+                        v[4 * m] = q.x;
+                        v[4 * m + 1] = q.y;
+                        v[4 * m + 2] = q.z;
+                        v[4 * m + 3] = q.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < G; ++j) v[j] = tile[pb ^ t0s[j & 3] ^ t1s[(j >> 2) & 3] ^ t2s[(j >> 4) & 3]];
+                }
                 for (int i = opb; i < ope; ++i) reg_apply<T, R>(v, p.ops[i], mats);
                 asm volatile("" : "+r"(pb));   // recompute the addresses instead of keeping them live
+                if (vec) {
 #pragma unroll
-                for (int j = 0; j < G; ++j) tile[pb ^ t0s[j & 3] ^ t1s[(j >> 2) & 3] ^ t2s[(j >> 4) & 3]] = v[j];
+                    for (int m = 0; m < G / 4; ++m)
+                        *reinterpret_cast<float4 *>(tile + (pb ^ t1s[m & 3] ^ t2s[(m >> 2) & 3])) =
+                            make_float4(v[4 * m], v[4 * m + 1], v[4 * m + 2], v[4 * m + 3]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < G; ++j) tile[pb ^ t0s[j & 3] ^ t1s[(j >> 2) & 3] ^ t2s[(j >> 4) & 3]] = v[j];
+                }
             }
             opb = ope;
             __syncthreads();

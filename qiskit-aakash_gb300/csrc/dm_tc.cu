@@ -1,4 +1,4 @@
-// Tensor-core fused pass (FP32 state, 3xTF32 on tcgen05).
+// Tensor-core fused pass (FP32 state, 3-way FP16 split on tcgen05).
 //
 // A pass holds 7 resident qubit axes: every tile of 4**7 = 16,384
 // coefficients is streamed into shared memory (cp.async, 16-byte chunks),
@@ -8,19 +8,25 @@
 // on the 64 coefficients that differ only in those axes.  With the tile
 // viewed as 256 groups x 64 (one row per group), the round is
 //     D[g][j'] = sum_j X[g][j] * U[j'][j]           (M = 256, N = 64, K = 64)
-// issued as two M = 128 tcgen05.mma.kind::tf32 chains into TMEM.  FP32
-// accuracy comes from the 3xTF32 split X = Xh + Xl, U = Uh + Ul:
-//     D = Xh Uh^T + Xl Uh^T + Xh Ul^T             (the Xl Ul term is below FP32)
-// The epilogue reads D from TMEM (tcgen05.ld, one group per thread) and
-// writes the hi/lo split directly in the operand layout of the next round;
-// after the last round it writes the tile back in its natural layout for
-// 128-bit stores.  Every wait on an mbarrier is bounded: a wait that gives up
-// records an error in *status and the kernel drains and returns.
+// issued as two M = 128 tcgen05.mma.kind::f16 chains into TMEM.  FP32
+// accuracy comes from a 3-way FP16 split: inside the pass the tile is held
+// in units of 2**-n (x = 2**n a, |x| <= 1), x = h + 2**-11 l with
+// h = fp16(x), l = fp16(2**11 (x - h)), and U = Uh + 2**-11 Ul likewise;
+//     D = h (2**11 Uh)^T + l Uh^T + h Ul^T = 2**11 x U^T + O(2**-22 |x|)
+// (the l Ul term is below FP32), and the epilogue scales D by 2**-11.
+// FP16 runs at twice the TF32 rate and halves the operand bytes.  The
+// epilogue reads D from TMEM (tcgen05.ld, one group per thread) and writes
+// the h / l split directly in the operand layout of the next round; after
+// the last round it writes the tile back in its natural FP32 layout for
+// 128-bit stores.  Every wait on an mbarrier is bounded: a wait that gives
+// up records an error in *status and the kernel drains and returns.
 //
-// Shared memory (dynamic, 224 KB): NAT 64 KB (cp.async landing buffer of
-// the next tile), AH / AL 64 KB each (round operand hi / lo, K-major
-// core-matrix layout, 256 rows x 64), BH / BL 16 KB each (U hi / lo).
+// Shared memory (dynamic, 152 KB): NAT 64 KB (cp.async landing buffer of
+// the next tile), AH / AL 32 KB each (round operand h / l, K-major
+// core-matrix FP16 layout, 256 rows x 64), B 24 KB (2**11 Uh, Uh, Ul).
 #include <mutex>
+
+#include <cuda_fp16.h>
 
 #include "dm_common.cuh"
 #include "dm_tcgen05.cuh"
@@ -34,18 +40,21 @@ constexpr int kAxes = 7;                       // resident axes per tile
 constexpr int kTile = 1 << (2 * kAxes);        // 16384 coefficients
 constexpr int kGroups = kTile / 64;            // 256 rows per round
 constexpr uint32_t kNatBytes = kTile * 4;      // 64 KB
-constexpr uint32_t kABytes = kGroups * 64 * 4; // 64 KB
-constexpr uint32_t kBBytes = 64 * 64 * 4;      // 16 KB
-constexpr uint32_t kSmemBytes = kNatBytes + 2 * kABytes + 2 * kBBytes;   // 224 KB
+constexpr uint32_t kABytes = kGroups * 64 * 2; // 32 KB per FP16 operand image
+constexpr uint32_t kBImage = 64 * 64 * 2;      // 8 KB per FP16 matrix image
+constexpr uint32_t kBBytes = 3 * kBImage;      // 24 KB
+constexpr uint32_t kSmemBytes = kNatBytes + 2 * kABytes + kBBytes;   // 152 KB
+constexpr int kUHalves = 3 * 64 * 64;          // FP16 values per round image
+constexpr float kLoScale = 2048.0f, kLoUnscale = 1.0f / 2048.0f;
 constexpr uint32_t kTmemCols = 128;            // two M = 128 blocks x N = 64
 
-// K-major core-matrix layout (no swizzle) of a rows x 64 operand: element
-// (row, k) lives at byte (row%8)*16 + (k%4)*4 + (k/4)*128 + (row/8)*2048.
-// LBO (next 16-byte core matrix along K) = 128 B, SBO (next 8 rows) = 2048 B.
-constexpr uint32_t kLBO = 128, kSBO = 2048;
+// K-major core-matrix layout (no swizzle) of a rows x 64 FP16 operand: element
+// (row, k) lives at byte (row%8)*16 + (k%8)*2 + (k/8)*128 + (row/8)*1024.
+// LBO (next 16-byte core matrix along K) = 128 B, SBO (next 8 rows) = 1024 B.
+constexpr uint32_t kLBO = 128, kSBO = 1024;
 
 __device__ __forceinline__ uint32_t row_off(int row) { return (row & 7) * 16 + (row >> 3) * kSBO; }
-__device__ __forceinline__ uint32_t k_off(int k) { return (k & 3) * 4 + (k >> 2) * kLBO; }
+__device__ __forceinline__ uint32_t k_off(int k) { return (k & 7) * 2 + (k >> 3) * kLBO; }
 
 using tcg::cp_async16;
 using tcg::cp_async_commit;
@@ -56,12 +65,8 @@ using tcg::tmem_ld64;
 
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) { return tcg::smem_desc(saddr, kLBO, kSBO); }
 
-// kind::tf32, D = F32, A = B = TF32, both K-major, M = 128, N = 64.
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
-
-__device__ __forceinline__ float tf32_rn(float x) {
-    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
-}
+// kind::f16, D = F32 (bits 4-5 = 1), A = B = F16 (bits 7-9, 10-12 = 0), both K-major, M = 128, N = 64.
+constexpr uint32_t kIdesc = (1u << 4) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
 
 // Natural-layout swizzle of the tile (16-byte chunks intact), as in dm_pass.cu.
 __device__ __forceinline__ int nat_swz(int e) { return e ^ ((((e >> 5) ^ (e >> 8)) & 7) << 2); }
@@ -77,6 +82,7 @@ struct Round {
 struct Pass {
     int n, m, low, nrounds;
     int vec0;
+    float up, down;                  // 2**n, 2**-n
     int64_t res_stride[kAxes];
     int64_t nonres_stride[DM_MAX_QUBITS];
     uint32_t natrow[8], natk[6];
@@ -110,22 +116,36 @@ __device__ __forceinline__ void digit_tables(const uint32_t *kc, uint32_t (&t)[3
     }
 }
 
-__device__ __forceinline__ void put_split(unsigned char *AH, unsigned char *AL, uint32_t o, float x) {
-    const float h = tf32_rn(x);
-    *reinterpret_cast<float *>(AH + o) = h;
-    *reinterpret_cast<float *>(AL + o) = x - h;
+// x -> (h, l): h = fp16(x), l = fp16(2**11 (x - h)), as FP16 bit patterns.
+__device__ __forceinline__ void split_h(float x, unsigned short &h, unsigned short &l) {
+    const __half hh = __float2half_rn(x);
+    h = __half_as_ushort(hh);
+    l = __half_as_ushort(__float2half_rn((x - __half2float(hh)) * kLoScale));
 }
 
+__device__ __forceinline__ void put_split(unsigned char *AH, unsigned char *AL, uint32_t o, float x) {
+    unsigned short h, l;
+    split_h(x, h, l);
+    *reinterpret_cast<unsigned short *>(AH + o) = h;
+    *reinterpret_cast<unsigned short *>(AL + o) = l;
+}
+
+// four values adjacent in K: one 64-bit store into each image
 __device__ __forceinline__ void put_split4(unsigned char *AH, unsigned char *AL, uint32_t o, float a, float b,
                                            float c, float d) {
-    const float ha = tf32_rn(a), hb = tf32_rn(b), hc = tf32_rn(c), hd = tf32_rn(d);
-    *reinterpret_cast<float4 *>(AH + o) = make_float4(ha, hb, hc, hd);
-    *reinterpret_cast<float4 *>(AL + o) = make_float4(a - ha, b - hb, c - hc, d - hd);
+    unsigned short ha, la, hb, lb, hc, lc, hd, ld;
+    split_h(a, ha, la);
+    split_h(b, hb, lb);
+    split_h(c, hc, lc);
+    split_h(d, hd, ld);
+    *reinterpret_cast<uint2 *>(AH + o) = make_uint2(uint32_t(ha) | (uint32_t(hb) << 16), uint32_t(hc) | (uint32_t(hd) << 16));
+    *reinterpret_cast<uint2 *>(AL + o) = make_uint2(uint32_t(la) | (uint32_t(lb) << 16), uint32_t(lc) | (uint32_t(ld) << 16));
 }
 
 // Epilogue stores of one thread's 64 values (K index j = d0 + 4 d1 + 16 d2)
 // at base ^ t[0][d0] ^ t[1][d1] ^ t[2][d2].  With a vector digit D the four
-// values along D are adjacent in the destination: one 128-bit store.
+// values along D are adjacent in the destination: one 64-bit store per
+// FP16 image (SPLIT), or one 128-bit FP32 store into the natural tile.
 template <int D, bool SPLIT>
 __device__ __forceinline__ void store_vec(const float (&v)[64], uint32_t base, const uint32_t (&t)[3][4],
                                           unsigned char *AH, unsigned char *AL) {
@@ -166,12 +186,12 @@ __device__ __forceinline__ void store_all(const float (&v)[64], int vec, uint32_
 }
 
 __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict__ st, const __grid_constant__ Pass p,
-                                                              const float *__restrict__ umats, int *status) {
+                                                              const uint16_t *__restrict__ umats, int *status) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *NAT = smem;
     unsigned char *AH = smem + kNatBytes;
     unsigned char *AL = AH + kABytes;
-    unsigned char *BH = AL + kABytes;
+    unsigned char *B = AL + kABytes;
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base_s;
     __shared__ int64_t hi_off[16];
@@ -217,12 +237,12 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
         }
         cp_async_commit();
     };
-    auto load_u = [&](int r) {          // round r's U images into BH / BL (contiguous)
-        const float *src = umats + p.rounds[r].umoff;
+    auto load_u = [&](int r) {          // round r's three U images into B (contiguous)
+        const uint16_t *src = umats + p.rounds[r].umoff;
 #pragma unroll
-        for (int i = 0; i < 2 * 64 * 64 / 4 / kThreads; ++i) {
+        for (int i = 0; i < int(kBBytes) / 16 / kThreads; ++i) {
             const int c = tid + kThreads * i;
-            cp_async16(BH + 16 * c, src + 4 * c);
+            cp_async16(B + 16 * c, src + 8 * c);
         }
         cp_async_commit();
     };
@@ -240,6 +260,7 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
             uint32_t tn[3][4], tk[3][4];
             digit_tables(p.natk, tn);
             const float *nat = reinterpret_cast<const float *>(NAT);
+            const float up = p.up;      // 2**n: the tile in units of 2**-n
             if (p.vec0 == 0) {
                 // digit 0 is local axis 0: four adjacent natural elements = four adjacent K
 #pragma unroll
@@ -247,12 +268,14 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
 #pragma unroll
                     for (int y = 0; y < 4; ++y) {
                         const float4 q = *reinterpret_cast<const float4 *>(nat + (nb ^ tn[1][x] ^ tn[2][y]));
-                        put_split4(AH, AL, row_bytes + k_off(4 * x + 16 * y), q.x, q.y, q.z, q.w);
+                        put_split4(AH, AL, row_bytes + k_off(4 * x + 16 * y), q.x * up, q.y * up, q.z * up,
+                                   q.w * up);
                     }
             } else {
 #pragma unroll
                 for (int j = 0; j < 64; ++j)
-                    put_split(AH, AL, row_bytes + k_off(j), nat[nb ^ tn[0][j & 3] ^ tn[1][(j >> 2) & 3] ^ tn[2][j >> 4]]);
+                    put_split(AH, AL, row_bytes + k_off(j),
+                              up * nat[nb ^ tn[0][j & 3] ^ tn[1][(j >> 2) & 3] ^ tn[2][j >> 4]]);
             }
             (void)tk;
         }
@@ -267,7 +290,8 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (tid == 0) {
-                const uint32_t ah = smem_u32(AH), al = smem_u32(AL), bh = smem_u32(BH), bl = bh + kBBytes;
+                // terms: h x (2**11 Uh), l x Uh, h x Ul
+                const uint32_t ah = smem_u32(AH), al = smem_u32(AL), b0 = smem_u32(B);
 #pragma unroll
                 for (int mb = 0; mb < 2; ++mb) {
                     const uint32_t d = tmem + mb * 64;
@@ -275,15 +299,15 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
 #pragma unroll
                     for (int term = 0; term < 3; ++term) {
                         const uint32_t a = (term == 1 ? al : ah) + aoff;
-                        const uint32_t b = term == 2 ? bl : bh;
+                        const uint32_t b = b0 + term * kBImage;
 #pragma unroll
-                        for (int ks = 0; ks < 8; ++ks) {
+                        for (int ks = 0; ks < 4; ++ks) {      // K = 16 per MMA: two core matrices
                             const uint64_t da = smem_desc(a + ks * 2 * kLBO);
                             const uint64_t db = smem_desc(b + ks * 2 * kLBO);
                             const uint32_t acc = (term | ks) ? 1u : 0u;
                             asm volatile(
                                 "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                                "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+                                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
                                 "l"(da), "l"(db), "r"(kIdesc), "r"(acc));
                         }
                     }
@@ -312,10 +336,15 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
             digit_tables(R.kc, tk);
             const uint32_t base = xor_bits<8>(row, R.rowc);
             if (r + 1 < p.nrounds) {
+#pragma unroll
+                for (int j = 0; j < 64; ++j) v[j] *= kLoUnscale;
                 store_all<true>(v, R.vec, base, tk, AH, AL);
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             } else {
-                store_all<false>(v, R.vec, base, tk, AH, AL);   // natural layout into AH
+                const float down = p.down * kLoUnscale;   // back to coefficients
+#pragma unroll
+                for (int j = 0; j < 64; ++j) v[j] *= down;
+                store_all<false>(v, R.vec, base, tk, AH, AL);   // natural FP32 layout into AH / AL (64 KB)
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         }
@@ -346,7 +375,7 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
 using namespace dmg;
 
 // Offsets must be distinct powers of two (operand) so that their XOR stays inside
-// a 64 KB operand region, or natural-tile element offsets below 4**7.
+// a 32 KB operand image, or natural-tile element offsets below 4**7.
 static bool valid_tables(const uint32_t *rowc, const uint32_t *kc, int vec, bool natural) {
     uint32_t seen = 0;
     for (int i = 0; i < 14; ++i) {
@@ -360,7 +389,8 @@ static bool valid_tables(const uint32_t *rowc, const uint32_t *kc, int vec, bool
     }
     if (vec >= 0) {
         if (vec > 2) return false;
-        const uint32_t lo = natural ? 1 : 4, hi = natural ? 2 : 8, align = natural ? 4 : 16;
+        // natural: four FP32 elements (16 bytes); operand: four FP16 values (8 bytes)
+        const uint32_t lo = natural ? 1 : 2, hi = natural ? 2 : 4, align = natural ? 4 : 8;
         if (kc[2 * vec] != lo || kc[2 * vec + 1] != hi) return false;
         for (int i = 0; i < 14; ++i) {   // the other bits keep 16-byte alignment
             if (i >= 8 && (i - 8) / 2 == vec) continue;
@@ -371,7 +401,7 @@ static bool valid_tables(const uint32_t *rowc, const uint32_t *kc, int vec, bool
     return true;
 }
 
-extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, const float *umats_dev,
+extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, const uint16_t *umats_dev,
                                 size_t umats_count, int *status_dev, void *stream) {
     DM_CHECK_ARG(state_dev && pass && umats_dev && status_dev && valid_n(n));
     if (reinterpret_cast<uintptr_t>(state_dev) & 15 || reinterpret_cast<uintptr_t>(umats_dev) & 15) return DM_ERR_ARG;
@@ -392,6 +422,8 @@ extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, 
     p.low = low;
     p.n = n;
     p.m = n - tc::kAxes;
+    p.up = float(ldexp(1.0, n));
+    p.down = float(ldexp(1.0, -n));
     int m = 0;
     for (int q = n - 1; q >= 0; --q)
         if (!resident[q]) p.nonres_stride[m++] = axis_stride(n, q);
@@ -413,7 +445,7 @@ extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, 
         if (!valid_tables(in.rowc, in.kc, in.vec, r + 1 == nr)) return DM_ERR_PROGRAM;
         for (int i = 0; i < 8; ++i) o.rowc[i] = in.rowc[i];
         for (int i = 0; i < 6; ++i) o.kc[i] = in.kc[i];
-        if (in.umoff < 0 || (in.umoff & 3) || size_t(in.umoff) + 2 * 64 * 64 > umats_count) return DM_ERR_PROGRAM;
+        if (in.umoff < 0 || (in.umoff & 7) || size_t(in.umoff) + tc::kUHalves > umats_count) return DM_ERR_PROGRAM;
         o.umoff = in.umoff;
     }
     static std::once_flag once;

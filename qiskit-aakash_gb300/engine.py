@@ -169,7 +169,7 @@ class DeviceState:
         torch = _torch()
         umats = []
         descs = [encode_pass_tc(p, self.n, umats) for p in passes]
-        host = np.concatenate(umats)
+        host = np.concatenate(umats).view(np.int16)      # FP16 bit patterns
         h = torch.from_numpy(host).pin_memory()
         dev = h.to(self.device, non_blocking=True)
         self.h2d_bytes += host.nbytes

@@ -388,23 +388,29 @@ def cx_matrix16(coef, ideal):
     return M
 
 
-def _tf32_rn(x32):
-    u = np.ascontiguousarray(x32, dtype=np.float32).view(np.uint32)
-    return ((u + np.uint32(0x1000)) & np.uint32(0xFFFFE000)).view(np.float32)
+# FP16 3-split of the tensor-core rounds.  Inside a pass the tile is held in
+# scaled units x' = 2**n a (|x'| <= 1 for a physical state), split as
+# x' = h + 2**-11 l with h = fp16(x'), l = fp16(2**11 (x' - h)); the round
+# matrix likewise U = Uh + 2**-11 Ul.  One FP32 accumulator collects
+#     h (2**11 Uh)^T + l Uh^T + h Ul^T = 2**11 (x' U^T) + O(2**-22)
+# and the epilogue multiplies by 2**-11 (exact).
+TC_LO_SCALE = 2048.0
+TC_IMAGE_HALVES = 3 * 4096          # per round: 2**11 Uh, Uh, Ul (FP16 bits)
 
-
-# float index of B[n][k] in the K-major core-matrix layout (LBO 128 B, SBO 2048 B)
+# half index of B[n][k] in the K-major FP16 core-matrix layout (LBO 128 B, SBO 1024 B)
 _N, _K = np.meshgrid(np.arange(64), np.arange(64), indexing='ij')
-_KMAJOR = ((_N % 8) * 4 + (_K % 4) + (_K // 4) * 32 + (_N // 8) * 512).reshape(-1)
+_KMAJOR = ((_N % 8) * 8 + (_K % 8) + (_K // 8) * 64 + (_N // 8) * 512).reshape(-1)
 
 
 def tc_round_image(U):
-    """8192 float32: TF32-rounded hi image then lo remainder image of U (64x64, FP64)."""
-    hi = _tf32_rn(U.astype(np.float32))
-    lo = (U - hi.astype(np.float64)).astype(np.float32)
-    img = np.zeros(8192, dtype=np.float32)
-    img[_KMAJOR] = hi.reshape(-1)
-    img[4096 + _KMAJOR] = lo.reshape(-1)
+    """12288 uint16 (FP16 bits): 2**11 Uh, Uh and Ul = fp16(2**11 (U - Uh)) of U (64x64, FP64), K-major."""
+    U = np.asarray(U, dtype=np.float64)
+    uh = U.astype(np.float16)
+    parts = [(uh.astype(np.float64) * TC_LO_SCALE).astype(np.float16), uh,
+             ((U - uh.astype(np.float64)) * TC_LO_SCALE).astype(np.float16)]
+    img = np.zeros(TC_IMAGE_HALVES, dtype=np.uint16)
+    for i, part in enumerate(parts):
+        img[4096 * i + _KMAJOR] = part.view(np.uint16).reshape(-1)
     return img
 
 
@@ -421,22 +427,26 @@ def pad_pass(p, n, k=TC_AXES):
 # ---------------------------------------------------------------------------
 # tensor-core round layouts
 #
-# A tensor-core round views the 4**7-coefficient tile as a 256 x 64 operand
-# (rows: groups, K: the round's 64 coefficients) in the K-major core-matrix
-# layout: byte(row, k) = (row%8)*16 + (k%4)*4 + (k/4)*128 + (row/8)*2048.
-# Which tile bits form the row index, and in which order the round's three
-# axes form the K digits, is free: the host picks them so that the epilogue
-# of each round (one row per thread) writes the next round's operand with
-# 128-bit stores whose 8-thread phases hit distinct bank groups.  Tile bit
-# 2a / 2a+1 is the low / high bit of local axis a's digit.
+# A tensor-core round views the 4**7-coefficient tile as a 256 x 64 FP16
+# operand (rows: groups, K: the round's 64 coefficients) in the K-major
+# core-matrix layout: byte(row, k) = (row%8)*16 + (k%8)*2 + (k/8)*128 +
+# (row/8)*1024.  Which tile bits form the row index, and in which order the
+# round's three axes form the K digits, is free: the host picks them so that
+# the epilogue of each round (one row per thread) writes the next round's
+# operand with 64-bit stores (four FP16 values along one axis) whose
+# half-warp phases hit distinct banks.  Tile bit 2a / 2a+1 is the low / high
+# bit of local axis a's digit.
 # ---------------------------------------------------------------------------
 
+TC_A_BYTES = 256 * 64 * 2           # one FP16 operand image (hi or lo)
+
+
 def _row_off(row):
-    return (row & 7) * 16 + (row >> 3) * 2048
+    return (row & 7) * 16 + (row >> 3) * 1024
 
 
 def _k_off(k):
-    return (k & 3) * 4 + (k >> 2) * 128
+    return (k & 7) * 2 + (k >> 3) * 128
 
 
 def nat_swz(e):
@@ -511,16 +521,18 @@ def epilogue_wavefronts(src, dst, natural=False):
 
     vec_axis = 0 if natural else dst.digits[0]
     d = _vec_digit(src, vec_axis)
+    vec_bytes = 16 if natural else 8     # four FP32 natural values / four FP16 operand values
+    phase = 8 if natural else 16          # threads per shared-memory wavefront of that width
     total = 0
     if d >= 0:
         others = [j for j in range(64) if (j >> (2 * d)) & 3 == 0]
         for j in others:
-            chunks = [addr_bytes(int(r), j) // 16 for r in lanes]
-            for ph in range(4):          # 8-thread phases of a 128-bit store
-                grp = chunks[8 * ph:8 * ph + 8]
+            addrs = [addr_bytes(int(r), j) for r in lanes]
+            for ph in range(32 // phase):
                 cnt = {}
-                for c in grp:
-                    cnt.setdefault(c % 8, set()).add(c)
+                for a in addrs[phase * ph:phase * ph + phase]:
+                    for w in range(a // 4, (a + vec_bytes) // 4):
+                        cnt.setdefault(w % 32, set()).add(w)
                 total += max(len(v) for v in cnt.values())
     else:
         for j in range(64):
@@ -567,7 +579,7 @@ def tc_tables(layouts):
 
 
 def encode_pass_tc(p, n, umats):
-    """DmTcPass for dm_apply_pass_tc; appends the rounds' matrix images to ``umats``."""
+    """DmTcPass for dm_apply_pass_tc; appends the rounds' FP16 matrix images (uint16) to ``umats``."""
     pp, layouts, mats = plan_tc_pass(p, n)
     if len(layouts) > N.DM_MAX_ROUNDS:
         raise RuntimeError('pass needs %d rounds (> %d)' % (len(layouts), N.DM_MAX_ROUNDS))
@@ -581,7 +593,7 @@ def encode_pass_tc(p, n, umats):
         dp.natrow[i] = conv['natrow'][i]
     for i in range(6):
         dp.natk[i] = conv['natk'][i]
-    off = sum(m.size for m in umats)
+    off = sum(m.size for m in umats)          # in FP16 values
     for ri, (rd, U) in enumerate(zip(rounds, mats)):
         o = dp.rounds[ri]
         for i in range(3):

@@ -185,7 +185,7 @@ def test_init_product(torch, n):
 
 @pytest.mark.parametrize('n', [7, 8, 10])
 def test_tensor_core_pass_equals_program_order(torch, n):
-    """dm_apply_pass_tc (3xTF32 tcgen05 rounds) against the ops applied one by one in FP64."""
+    """dm_apply_pass_tc (FP16-split tcgen05 rounds) against the ops applied one by one in FP64."""
     from test_planner import apply_op, random_ops
     rng = np.random.default_rng(3000 + n)
     ops = random_ops(rng, n, 60)
@@ -204,7 +204,7 @@ def test_tensor_core_pass_equals_program_order(torch, n):
     umats = []
     descs = [P.encode_pass_tc(p, n, umats) for p in passes]
     m = np.concatenate(umats)
-    md = dev(torch, m, np.float32)
+    md = torch.from_numpy(m.view(np.int16)).cuda()
     t = dev(torch, st, np.float32)
     status = torch.zeros(1, dtype=torch.int32, device='cuda')
     for d in descs:
@@ -219,7 +219,7 @@ def test_tensor_core_pass_rejects_bad_programs(torch):
     """Malformed tensor-core descriptors are refused on the host (no launch)."""
     n = 8
     t = torch.zeros(4 ** n, dtype=torch.float32, device='cuda')
-    u = torch.zeros(8192, dtype=torch.float32, device='cuda')
+    u = torch.zeros(3 * 4096, dtype=torch.int16, device='cuda')
     status = torch.zeros(1, dtype=torch.int32, device='cuda')
     rng = np.random.default_rng(0)
     from test_planner import random_ops
@@ -229,12 +229,12 @@ def test_tensor_core_pass_rejects_bad_programs(torch):
     def rc_of(mutate):
         d = N.DmTcPass.from_buffer_copy(good)
         mutate(d)
-        return N.lib().dm_apply_pass_tc(vp(t), n, ctypes.byref(d), vp(u), 8192, vp(status), stream(torch))
+        return N.lib().dm_apply_pass_tc(vp(t), n, ctypes.byref(d), vp(u), 3 * 4096, vp(status), stream(torch))
 
     def bad_axes(d):
         d.axes[1], d.axes[2] = d.axes[2], d.axes[1]           # not decreasing
     def bad_umoff(d):
-        d.rounds[0].umoff = 4                                 # image overruns the 8192-float buffer
+        d.rounds[0].umoff = 8                                 # images overrun the 12288-value buffer
     def bad_row(d):
         d.rounds[0].rowc[0] = 3 if d.nrounds > 1 else 20000   # not a power of two / outside the tile
     def bad_vec(d):

@@ -192,7 +192,7 @@ def test_register_rounds_equal_program_order(n, kmax, low, width):
 
 
 def _emulate_tc_pass(st, n, p):
-    """numpy model of dm_apply_pass_tc's data movement (exact arithmetic, no TF32)."""
+    """numpy model of dm_apply_pass_tc's data movement (exact arithmetic, no FP16 split)."""
     pp, layouts, mats = P.plan_tc_pass(p, n)
     conv, rounds = P.tc_tables(layouts)
     k = 7
@@ -204,7 +204,7 @@ def _emulate_tc_pass(st, n, p):
                         for e in range(4 ** k)])
         nat = np.zeros(4 ** k)
         nat[[P.nat_swz(e) for e in range(4 ** k)]] = st[idx]          # cp.async landing
-        A = np.zeros(16384)                                            # operand, float index = byte / 4
+        A = np.zeros(16384)                                            # operand, FP16 index = byte / 2
 
         def xor_bits(x, c):
             o = 0
@@ -216,9 +216,9 @@ def _emulate_tc_pass(st, n, p):
         for row in range(256):                                         # conversion
             nb = xor_bits(row, conv['natrow'])
             for j in range(64):
-                A[(P._row_off(row) + P._k_off(j)) // 4] = nat[nb ^ xor_bits(j, conv['natk'])]
+                A[(P._row_off(row) + P._k_off(j)) // 2] = nat[nb ^ xor_bits(j, conv['natk'])]
         for r, (rd, U) in enumerate(zip(rounds, mats)):
-            X = np.array([[A[(P._row_off(row) + P._k_off(j)) // 4] for j in range(64)] for row in range(256)])
+            X = np.array([[A[(P._row_off(row) + P._k_off(j)) // 2] for j in range(64)] for row in range(256)])
             D = X @ U.T
             last = r + 1 == len(rounds)
             newA = np.zeros(16384) if not last else None
@@ -230,7 +230,7 @@ def _emulate_tc_pass(st, n, p):
                     if last:
                         natout[o] = D[row, j]
                     else:
-                        newA[o // 4] = D[row, j]
+                        newA[o // 2] = D[row, j]
             if not last:
                 A = newA
         out[idx] = natout[[P.nat_swz(e) for e in range(4 ** k)]]
@@ -263,23 +263,39 @@ def test_tensor_core_tables_are_valid():
         for r, rd in enumerate(rounds):
             c = rd['rowc'] + rd['kc']
             if r + 1 < len(rounds):
-                assert all(x > 0 and x & (x - 1) == 0 and x < 65536 for x in c)
+                assert all(x > 0 and x & (x - 1) == 0 and x < P.TC_A_BYTES for x in c)
                 assert len(set(c)) == 14
                 if rd['vec'] >= 0:
                     v = rd['vec']
-                    assert rd['kc'][2 * v] == 4 and rd['kc'][2 * v + 1] == 8
+                    assert rd['kc'][2 * v] == 2 and rd['kc'][2 * v + 1] == 4
+                    assert all(x % 8 == 0 for i, x in enumerate(c) if i < 8 or (i - 8) // 2 != v)
             else:
                 assert all(0 < x < 16384 for x in c)
 
 
 def test_tc_image_layout_and_split():
-    U = np.random.default_rng(2).normal(size=(64, 64))
+    U = np.random.default_rng(2).normal(size=(64, 64)) / 8
     img = P.tc_round_image(U)
-    hi = np.zeros((64, 64), np.float32)
-    lo = np.zeros((64, 64), np.float32)
-    hi.reshape(-1)[:] = img[P._KMAJOR]
-    lo.reshape(-1)[:] = img[4096 + P._KMAJOR]
+    assert img.dtype == np.uint16 and img.size == P.TC_IMAGE_HALVES
     assert len(set(P._KMAJOR.tolist())) == 4096
-    assert (hi.view(np.uint32) & 0x1FFF == 0).all()          # TF32: low 13 mantissa bits clear
-    # lo is FP32 of U - hi (|.| <= 2^-11 |U|): hi + lo carries U to ~2^-35 relative
-    np.testing.assert_allclose(hi.astype(np.float64) + lo, U, rtol=0, atol=1e-10 * np.abs(U).max())
+    parts = [np.zeros((64, 64)) for _ in range(3)]
+    for i in range(3):
+        parts[i].reshape(-1)[:] = img[4096 * i + P._KMAJOR].view(np.float16).astype(np.float64)
+    big, uh, ul = parts
+    assert np.array_equal(big, uh * P.TC_LO_SCALE)                  # 2**11 Uh is exact in FP16
+    assert np.array_equal(uh, U.astype(np.float16).astype(np.float64))
+    # Uh + 2**-11 Ul carries U to about 2**-22 relative
+    np.testing.assert_allclose(uh + ul / P.TC_LO_SCALE, U, rtol=0, atol=2.0 ** -21 * np.abs(U).max())
+
+
+def test_fp16_three_way_split_accuracy():
+    """h (2**11 Uh)^T + l Uh^T + h Ul^T, with FP16 operands and exact products, reproduces 2**11 x U^T."""
+    rng = np.random.default_rng(8)
+    U = rng.normal(size=(64, 64)) / 8
+    x = rng.normal(size=(256, 64)) * np.exp(rng.uniform(-12, 0, size=(256, 64)))   # |x| <= ~1, many tiny
+    h = x.astype(np.float16).astype(np.float64)
+    lo = ((x - h) * P.TC_LO_SCALE).astype(np.float16).astype(np.float64)
+    uh = U.astype(np.float16).astype(np.float64)
+    ul = ((U - uh) * P.TC_LO_SCALE).astype(np.float16).astype(np.float64)
+    D = (h @ (uh * P.TC_LO_SCALE).T + lo @ uh.T + h @ ul.T) / P.TC_LO_SCALE
+    assert np.max(np.abs(D - x @ U.T)) < 2e-6 * np.abs(x @ U.T).max()
