@@ -478,7 +478,7 @@ def surrogate_leg(args, torch):
     tv_blind = (0.5 * (y_te - blind).abs().sum(dim=1)).cpu().numpy()
     sim_rate = len(raw_te) / sim_te_s
     fallback = {}
-    for tau in (0.01, 0.02, 0.05):
+    for tau in (0.0005, 0.001, 0.002):
         fb = spread_np > tau
         hybrid_tv = np.where(fb, 0.0, tv_np)
         t_h = inf_s + fb.sum() / sim_rate
