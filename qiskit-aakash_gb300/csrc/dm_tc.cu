@@ -218,7 +218,6 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
     uint32_t phase = 0;
     // this thread's row in every round (warps 0-3: rows 0-127 = M block 0, warps 4-7: M block 1)
     const uint32_t row = uint32_t(tid);
-    const uint32_t row_bytes = row_off(int(row));
 
     auto tile_base = [&](int64_t t) {
         int64_t base = 0;
@@ -254,30 +253,44 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
         cp_async_wait_all();
         __syncthreads();
         if (abort_s) break;
-        // ---- natural tile -> round 0's operand (hi / lo) ----
+        // ---- natural tile -> round 0's operand (h / l) ----
+        // Thread work items are (row, 8-value K chunk) pairs with the row's low three bits on
+        // the lane bits, so each 16-byte chunk store of an 8-lane phase covers the 8 rows of one
+        // core matrix: all 32 banks, no conflict.
         {
-            const uint32_t nb = xor_bits<8>(row, p.natrow);
-            uint32_t tn[3][4], tk[3][4];
-            digit_tables(p.natk, tn);
             const float *nat = reinterpret_cast<const float *>(NAT);
             const float up = p.up;      // 2**n: the tile in units of 2**-n
-            if (p.vec0 == 0) {
-                // digit 0 is local axis 0: four adjacent natural elements = four adjacent K
+#pragma unroll 2
+            for (int q = 0; q < kGroups * 8 / kThreads; ++q) {
+                const int i = tid + kThreads * q;
+                const int crow = ((i >> 6) << 3) | (i & 7), c = (i >> 3) & 7;
+                // chunk c holds K = 8c .. 8c + 7: K bits 3-5 come from c, bits 0-2 from the element
+                const uint32_t nb = xor_bits<8>(uint32_t(crow), p.natrow) ^ ((c & 1) ? p.natk[3] : 0u) ^
+                                    ((c & 2) ? p.natk[4] : 0u) ^ ((c & 4) ? p.natk[5] : 0u);
+                float x[8];
+                if (p.vec0 == 0) {   // digit 0 is local axis 0: four adjacent natural elements
+                    const float4 a = *reinterpret_cast<const float4 *>(nat + nb);
+                    const float4 b = *reinterpret_cast<const float4 *>(nat + (nb ^ p.natk[2]));
+                    x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
+                    x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+                } else {
 #pragma unroll
-                for (int x = 0; x < 4; ++x)
+                    for (int e = 0; e < 8; ++e)
+                        x[e] = nat[nb ^ ((e & 1) ? p.natk[0] : 0u) ^ ((e & 2) ? p.natk[1] : 0u) ^ ((e & 4) ? p.natk[2] : 0u)];
+                }
+                uint32_t hw[4], lw[4];
 #pragma unroll
-                    for (int y = 0; y < 4; ++y) {
-                        const float4 q = *reinterpret_cast<const float4 *>(nat + (nb ^ tn[1][x] ^ tn[2][y]));
-                        put_split4(AH, AL, row_bytes + k_off(4 * x + 16 * y), q.x * up, q.y * up, q.z * up,
-                                   q.w * up);
-                    }
-            } else {
-#pragma unroll
-                for (int j = 0; j < 64; ++j)
-                    put_split(AH, AL, row_bytes + k_off(j),
-                              up * nat[nb ^ tn[0][j & 3] ^ tn[1][(j >> 2) & 3] ^ tn[2][j >> 4]]);
+                for (int e = 0; e < 8; e += 2) {
+                    unsigned short h0, l0, h1, l1;
+                    split_h(x[e] * up, h0, l0);
+                    split_h(x[e + 1] * up, h1, l1);
+                    hw[e >> 1] = uint32_t(h0) | (uint32_t(h1) << 16);
+                    lw[e >> 1] = uint32_t(l0) | (uint32_t(l1) << 16);
+                }
+                const uint32_t o = row_off(crow) + uint32_t(c) * kLBO;
+                *reinterpret_cast<uint4 *>(AH + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(AL + o) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
             }
-            (void)tk;
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();

@@ -471,11 +471,58 @@ class TcLayout:
         return self._byte[tb]
 
 
+def _store_wavefronts(lane_offs, vec_bytes):
+    """Shared-memory wavefronts of one warp store whose lane i writes at XOR of lane_offs[bits of i].
+
+    A per-store constant offset (the non-lane part of the address) XORs
+    every address alike and does not change the count, so a whole epilogue
+    costs (stores per thread) x this.  Phases: 32 lanes for 2/4-byte stores,
+    16 for 8-byte, 8 for 16-byte."""
+    lanes = np.arange(32)
+    addr = np.zeros(32, dtype=np.int64)
+    for i, o in enumerate(lane_offs):
+        addr ^= ((lanes >> i) & 1) * o
+    phase = 32 if vec_bytes <= 4 else 128 // vec_bytes
+    nw = max(1, vec_bytes // 4)
+    total = 0
+    for ph in range(32 // phase):
+        words = np.unique((addr[ph * phase:(ph + 1) * phase, None] // 4 + np.arange(nw)[None, :]).reshape(-1))
+        total += int(np.bincount(words % 32, minlength=32).max())
+    return total
+
+
+def _transition_cost(src, dst_off, vec):
+    """Store wavefronts + issue of one warp's epilogue from layout src into byte offsets dst_off(tile bit)."""
+    lane_offs = [dst_off(tb) for tb in src.rowbits[:5]]
+    if vec:
+        w, n = _store_wavefronts(lane_offs, vec), 16
+    else:
+        w, n = _store_wavefronts(lane_offs, 2 if vec is None else 4), 64
+    return n * w + n // 4
+
+
+def _natural_cost(layout):
+    vec = 16 if _vec_digit(layout, 0) >= 0 else 0
+    return _transition_cost(layout, lambda tb: 4 * nat_swz(1 << tb), vec)
+
+
 def _choose_layouts(rounds_axes):
-    """Pick each round's digit order and row order (greedy along the round sequence)."""
+    """Pick each round's digit order and row-bit order (greedy along the round sequence).
+
+    The epilogue of round r (one source row per thread) writes round r+1's
+    operand; its cost depends only on where the source's five lane bits land
+    in the destination (bank bits 2-6: destination K bits 1-2 and row bits
+    0-2) and on whether the destination's K digit 0 is one of the source's
+    axes (8-byte vector stores).  For every digit order of the destination
+    and every choice of which source lane bits become its row bits 0-2, the
+    cost is evaluated exactly (``_store_wavefronts``); the last round also
+    pays for its stores into the natural tile.
+    """
+    import itertools
     layouts = []
     prev = None
-    for axes in rounds_axes:
+    nlast = len(rounds_axes) - 1
+    for ri, axes in enumerate(rounds_axes):
         axes = sorted(axes)
         nonround = [tb for tb in range(2 * TC_AXES) if tb // 2 not in axes]
         if prev is None:
@@ -483,16 +530,23 @@ def _choose_layouts(rounds_axes):
             layouts.append(TcLayout(digits, nonround))
             prev = layouts[-1]
             continue
-        # rows follow the previous round's row order where possible (lane bits stay lane bits)
+        lanes = [tb for tb in prev.rowbits[:5] if tb in nonround]
         keep = [tb for tb in prev.rowbits if tb in nonround]
-        rowbits = keep + [tb for tb in nonround if tb not in keep]
+        triples = list(itertools.combinations(lanes, 3)) if len(lanes) >= 3 else [tuple(lanes)]
         best = None
-        for first in axes:
-            digits = [first] + [a for a in axes if a != first]
-            cand = TcLayout(digits, rowbits)
-            score = epilogue_wavefronts(prev, cand)
-            if best is None or score < best[0]:
-                best = (score, cand)
+        for digits in itertools.permutations(axes):
+            for tri in triples:
+                rowbits = list(tri)
+                for tb in lanes + keep + nonround:      # remaining lane bits, then the previous order, then new bits
+                    if tb not in rowbits:
+                        rowbits.append(tb)
+                cand = TcLayout(list(digits), rowbits)
+                vec = 8 if _vec_digit(prev, cand.digits[0]) >= 0 else None
+                cost = _transition_cost(prev, cand.byte_of_bit, vec)
+                if ri == nlast:
+                    cost += _natural_cost(cand)
+                if best is None or cost < best[0]:
+                    best = (cost, cand)
         layouts.append(best[1])
         prev = best[1]
     return layouts
