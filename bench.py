@@ -617,7 +617,7 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
                      'against': 'FP64 GPU plain form (itself parity-checked against the reference at n<=14)',
                      'coeff_scale': 'Pauli expectations 2^n * a_s'},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s', 'frac': achieved / hbm,
-                     'traffic': traffic, 'kernel': 'pass_tc_kernel (tcgen05 3xTF32)', 'launches_per_step': len(durs),
+                     'traffic': traffic, 'kernel': 'pass_tc_kernel (tcgen05 kind::f16, 3-way FP16 split)', 'launches_per_step': len(durs),
                      'mean_launch_ms': mean_pass_ms,
                      'algorithmic_bytes_per_launch': 2 * N4 * 4, 'peak_kind': peak_kind},
         'e2e': {'value': world * layers / e2e_s, 'unit': 'gate-layers/s', 'seconds_per_step': e2e_s,

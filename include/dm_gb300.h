@@ -141,7 +141,7 @@ typedef struct dm_tc_round {
     int8_t digits[3];     /* local axes of K digits 0, 1, 2 (j = d0 + 4 d1 + 16 d2) */
     int8_t vec;           /* digit whose 4 values the epilogue stores as one vector (8 bytes of FP16 into
                              the next operand, 16 bytes of FP32 into the natural tile), or -1 */
-    int32_t umoff;        /* FP16-value offset of the round's matrix images: 2**11 Uh, Uh, Ul (4096 each),
+    int32_t umoff;        /* FP16-value offset of the round's matrix images: 2**11 Uh, Ul, Uh (4096 each),
                              value (n%8)*8 + k%8 + (k/8)*64 + (n/8)*512 for output n, input k */
     uint32_t rowc[8];     /* destination offset of row bit i of this round: bytes into the next round's
                              operand, or, after the last round, elements of the natural tile */

@@ -23,7 +23,10 @@
 //
 // Shared memory (dynamic, 152 KB): NAT 64 KB (cp.async landing buffer of
 // the next tile), AH / AL 32 KB each (round operand h / l, K-major
-// core-matrix FP16 layout, 256 rows x 64), B 24 KB (2**11 Uh, Uh, Ul).
+// core-matrix FP16 layout, 256 rows x 64), B 24 KB (2**11 Uh and Ul stacked
+// as one 128-row operand, then Uh).  The h operand is read once per round
+// for both of its terms (N = 128 into two 64-column accumulators that the
+// epilogue adds).
 #include <mutex>
 
 #include <cuda_fp16.h>
@@ -46,7 +49,7 @@ constexpr uint32_t kBBytes = 3 * kBImage;      // 24 KB
 constexpr uint32_t kSmemBytes = kNatBytes + 2 * kABytes + kBBytes;   // 152 KB
 constexpr int kUHalves = 3 * 64 * 64;          // FP16 values per round image
 constexpr float kLoScale = 2048.0f, kLoUnscale = 1.0f / 2048.0f;
-constexpr uint32_t kTmemCols = 128;            // two M = 128 blocks x N = 64
+constexpr uint32_t kTmemCols = 256;            // two M = 128 blocks x N = 128 (D1 | D2)
 
 // K-major core-matrix layout (no swizzle) of a rows x 64 FP16 operand: element
 // (row, k) lives at byte (row%8)*16 + (k%8)*2 + (k/8)*128 + (row/8)*1024.
@@ -61,12 +64,14 @@ using tcg::cp_async_commit;
 using tcg::cp_async_wait_all;
 using tcg::mbar_wait;
 using tcg::smem_u32;
+using tcg::tmem_ld16;
 using tcg::tmem_ld64;
 
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) { return tcg::smem_desc(saddr, kLBO, kSBO); }
 
-// kind::f16, D = F32 (bits 4-5 = 1), A = B = F16 (bits 7-9, 10-12 = 0), both K-major, M = 128, N = 64.
-constexpr uint32_t kIdesc = (1u << 4) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+// kind::f16, D = F32 (bits 4-5 = 1), A = B = F16 (bits 7-9, 10-12 = 0), both K-major, M = 128, N = 128 / 64.
+constexpr uint32_t kIdesc128 = (1u << 4) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr uint32_t kIdesc64 = (1u << 4) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
 
 // Natural-layout swizzle of the tile (16-byte chunks intact), as in dm_pass.cu.
 __device__ __forceinline__ int nat_swz(int e) { return e ^ ((((e >> 5) ^ (e >> 8)) & 7) << 2); }
@@ -303,16 +308,18 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (tid == 0) {
-                // terms: h x (2**11 Uh), l x Uh, h x Ul
+                // D[:, 0:64] = h (2**11 Uh)^T + l Uh^T and D[:, 64:128] = h Ul^T: the h operand is
+                // read once for both of its terms (N = 128 over the stacked images 2**11 Uh | Ul)
                 const uint32_t ah = smem_u32(AH), al = smem_u32(AL), b0 = smem_u32(B);
 #pragma unroll
                 for (int mb = 0; mb < 2; ++mb) {
-                    const uint32_t d = tmem + mb * 64;
+                    const uint32_t d = tmem + mb * 128;
                     const uint32_t aoff = mb * (kABytes / 2);
 #pragma unroll
-                    for (int term = 0; term < 3; ++term) {
-                        const uint32_t a = (term == 1 ? al : ah) + aoff;
-                        const uint32_t b = b0 + term * kBImage;
+                    for (int term = 0; term < 2; ++term) {
+                        const uint32_t a = (term == 0 ? ah : al) + aoff;
+                        const uint32_t b = b0 + term * 2 * kBImage;
+                        const uint32_t idesc = term == 0 ? kIdesc128 : kIdesc64;
 #pragma unroll
                         for (int ks = 0; ks < 4; ++ks) {      // K = 16 per MMA: two core matrices
                             const uint64_t da = smem_desc(a + ks * 2 * kLBO);
@@ -321,7 +328,7 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
                             asm volatile(
                                 "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
                                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
-                                "l"(da), "l"(db), "r"(kIdesc), "r"(acc));
+                                "l"(da), "l"(db), "r"(idesc), "r"(acc));
                         }
                     }
                 }
@@ -343,7 +350,17 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
             load_u(r + 1 < p.nrounds ? r + 1 : 0);
             // ---- epilogue: D -> next operand (hi / lo), or the natural tile after the last round ----
             float v[64];
-            tmem_ld64(tmem + (uint32_t(32 * (warp & 3)) << 16) + uint32_t((warp >> 2) * 64), v);
+            {
+                const uint32_t ta = tmem + (uint32_t(32 * (warp & 3)) << 16) + uint32_t((warp >> 2) * 128);
+                tmem_ld64(ta, v);
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {   // + the h Ul^T half, 16 columns at a time
+                    float w[16];
+                    tmem_ld16(ta + 64 + 16 * c, w);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) v[16 * c + j] += w[j];
+                }
+            }
             const Round &R = p.rounds[r];
             uint32_t tk[3][4];
             digit_tables(R.kc, tk);

@@ -31,7 +31,7 @@ GB300 options (absent from the reference): ``precision`` ('double', the
 default and the parity form, or 'single'), ``fusion`` (fused tile passes,
 default True), ``tile_axes`` (resident axes per tile), ``register_rounds``
 (apply a pass's operations in register rounds, default True), ``tensor_cores``
-(FP32 passes on tcgen05 as 3xTF32 64x64 transfer matrices, default True) and
+(FP32 passes on tcgen05 as 64x64 transfer matrices in a 3-way FP16 split, default True) and
 ``coefficients_to_host`` (default True; False leaves ``coeffmatrix`` /
 ``densitymatrix`` out of the result, for callers that only need the
 measurement data of a large register).

@@ -74,7 +74,7 @@ class DeviceState:
         self.state = torch.empty(4 ** n, dtype=self.torch_dtype, device=self.device)
         self.fusion = fusion
         self.rounds = rounds
-        # FP32 passes of 7 resident axes run on the tensor cores (3xTF32)
+        # FP32 passes of 7 resident axes run on the tensor cores (3-way FP16 split)
         self.tensor_cores = bool(tensor_cores) and precision == 'single' and n >= TC_AXES
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device) if self.tensor_cores else None
         self.kmax = min(tile_axes or DEFAULT_TILE_AXES[precision], N.DM_MAX_TILE_AXES)

@@ -27,6 +27,7 @@ operation whose axes fit in the pass and none of whose axes is held back by
 an earlier operation it could not take.  Consecutive 4x4 maps on one axis
 inside a pass are multiplied together (in FP64) into one map.
 """
+import functools
 import math
 
 import numpy as np
@@ -229,7 +230,7 @@ def plan_passes(ops, n, kmax, low):
     return passes
 
 
-def plan_rounds(p, width):
+def plan_rounds(p, width, pad='low'):
     """Group a pass's ops into register rounds of ``width`` local axes.
 
     Returns a list of (axes, ops): ``axes`` the round's local axes (ascending,
@@ -240,10 +241,17 @@ def plan_rounds(p, width):
     """
     k = len(p.axes)
     local = [Op(op.kind, tuple(p.local(a) for a in op.axes), op.data, op.ideal, src=op.src) for op in p.ops]
+    planned = plan_passes(local, k, width, 0)
     rounds = []
-    for r in plan_passes(local, k, width, 0):
+    for i, r in enumerate(planned):
         axes = sorted(r.axes)
-        for a in range(k):
+        # 'low': pad with the lowest axes (axis 0 in a round lets the CUDA-core kernel move
+        # 16-byte vectors); 'neighbors': first the axes the next round uses (its epilogue input
+        # then shares them, so the tensor-core epilogue stores whole vectors), then the previous
+        # round's
+        nxt = sorted(planned[i + 1].axes) if i + 1 < len(planned) and pad == 'neighbors' else []
+        prv = rounds[-1][0] if rounds and pad == 'neighbors' else []
+        for a in nxt + prv + list(range(k)):
             if len(axes) >= width:
                 break
             if a not in axes:
@@ -395,7 +403,7 @@ def cx_matrix16(coef, ideal):
 #     h (2**11 Uh)^T + l Uh^T + h Ul^T = 2**11 (x' U^T) + O(2**-22)
 # and the epilogue multiplies by 2**-11 (exact).
 TC_LO_SCALE = 2048.0
-TC_IMAGE_HALVES = 3 * 4096          # per round: 2**11 Uh, Uh, Ul (FP16 bits)
+TC_IMAGE_HALVES = 3 * 4096          # per round: 2**11 Uh, Ul (one 128-row operand), Uh (FP16 bits)
 
 # half index of B[n][k] in the K-major FP16 core-matrix layout (LBO 128 B, SBO 1024 B)
 _N, _K = np.meshgrid(np.arange(64), np.arange(64), indexing='ij')
@@ -403,11 +411,13 @@ _KMAJOR = ((_N % 8) * 8 + (_K % 8) + (_K // 8) * 64 + (_N // 8) * 512).reshape(-
 
 
 def tc_round_image(U):
-    """12288 uint16 (FP16 bits): 2**11 Uh, Uh and Ul = fp16(2**11 (U - Uh)) of U (64x64, FP64), K-major."""
+    """12288 uint16 (FP16 bits) of U (64x64, FP64), each K-major: 2**11 Uh, Ul = fp16(2**11 (U - Uh)), Uh.
+
+    The first two images are adjacent so that they form one 128-row operand."""
     U = np.asarray(U, dtype=np.float64)
     uh = U.astype(np.float16)
-    parts = [(uh.astype(np.float64) * TC_LO_SCALE).astype(np.float16), uh,
-             ((U - uh.astype(np.float64)) * TC_LO_SCALE).astype(np.float16)]
+    parts = [(uh.astype(np.float64) * TC_LO_SCALE).astype(np.float16),
+             ((U - uh.astype(np.float64)) * TC_LO_SCALE).astype(np.float16), uh]
     img = np.zeros(TC_IMAGE_HALVES, dtype=np.uint16)
     for i, part in enumerate(parts):
         img[4096 * i + _KMAJOR] = part.view(np.uint16).reshape(-1)
@@ -471,6 +481,7 @@ class TcLayout:
         return self._byte[tb]
 
 
+@functools.lru_cache(maxsize=None)
 def _store_wavefronts(lane_offs, vec_bytes):
     """Shared-memory wavefronts of one warp store whose lane i writes at XOR of lane_offs[bits of i].
 
@@ -493,7 +504,7 @@ def _store_wavefronts(lane_offs, vec_bytes):
 
 def _transition_cost(src, dst_off, vec):
     """Store wavefronts + issue of one warp's epilogue from layout src into byte offsets dst_off(tile bit)."""
-    lane_offs = [dst_off(tb) for tb in src.rowbits[:5]]
+    lane_offs = tuple(dst_off(tb) for tb in src.rowbits[:5])
     if vec:
         w, n = _store_wavefronts(lane_offs, vec), 16
     else:
@@ -506,18 +517,32 @@ def _natural_cost(layout):
     return _transition_cost(layout, lambda tb: 4 * nat_swz(1 << tb), vec)
 
 
-def _choose_layouts(rounds_axes):
-    """Pick each round's digit order and row-bit order (greedy along the round sequence).
+def _fill_rows(first, lanes, keep, nonround):
+    rowbits = list(first)
+    for tb in lanes + keep + nonround:   # remaining lane bits, the previous order, new bits
+        if tb not in rowbits:
+            rowbits.append(tb)
+    return rowbits
 
-    The epilogue of round r (one source row per thread) writes round r+1's
-    operand; its cost depends only on where the source's five lane bits land
-    in the destination (bank bits 2-6: destination K bits 1-2 and row bits
-    0-2) and on whether the destination's K digit 0 is one of the source's
-    axes (8-byte vector stores).  For every digit order of the destination
-    and every choice of which source lane bits become its row bits 0-2, the
-    cost is evaluated exactly (``_store_wavefronts``); the last round also
-    pays for its stores into the natural tile.
-    """
+
+def _best_next_cost(cand, next_axes):
+    """Cheapest epilogue from ``cand`` into a round on next_axes (lookahead of the greedy choice)."""
+    import itertools
+    nonround = [tb for tb in range(2 * TC_AXES) if tb // 2 not in next_axes]
+    lanes = [tb for tb in cand.rowbits[:5] if tb in nonround]
+    keep = [tb for tb in cand.rowbits if tb in nonround]
+    rows = _fill_rows(lanes[:3], lanes, keep, nonround)
+    best = None
+    for digits in itertools.permutations(sorted(next_axes)):
+        nxt = TcLayout(list(digits), rows)
+        vec = 8 if _vec_digit(cand, nxt.digits[0]) >= 0 else None
+        c = _transition_cost(cand, nxt.byte_of_bit, vec)
+        best = c if best is None or c < best else best
+    return best
+
+
+@functools.lru_cache(maxsize=4096)
+def _choose_layouts_cached(rounds_axes):
     import itertools
     layouts = []
     prev = None
@@ -525,31 +550,56 @@ def _choose_layouts(rounds_axes):
     for ri, axes in enumerate(rounds_axes):
         axes = sorted(axes)
         nonround = [tb for tb in range(2 * TC_AXES) if tb // 2 not in axes]
+        nxt_axes = set(rounds_axes[ri + 1]) if ri < nlast else None
         if prev is None:
             digits = ([0] + [a for a in axes if a != 0]) if 0 in axes else axes
-            layouts.append(TcLayout(digits, nonround))
-            prev = layouts[-1]
+            best = None
+            fourth = [None] + ([tb for tb in nonround if tb % 2 == 0 and tb // 2 in nxt_axes] if nxt_axes else [])
+            for f in fourth:
+                cand = TcLayout(digits, _fill_rows([f] if f is not None else [], [], [], nonround))
+                cost = _best_next_cost(cand, nxt_axes) if nxt_axes else _natural_cost(cand)
+                if best is None or cost < best[0]:
+                    best = (cost, cand)
+            layouts.append(best[1])
+            prev = best[1]
             continue
         lanes = [tb for tb in prev.rowbits[:5] if tb in nonround]
         keep = [tb for tb in prev.rowbits if tb in nonround]
         triples = list(itertools.combinations(lanes, 3)) if len(lanes) >= 3 else [tuple(lanes)]
+        # row 3 feeds the next epilogue's 16-lane phases: the low bit of an axis the next round
+        # adds can become its K bit 2 (byte 8), which keeps those 8-byte stores conflict-free
+        fourth = [None] + ([tb for tb in nonround if tb % 2 == 0 and tb // 2 in nxt_axes] if nxt_axes else [])
         best = None
         for digits in itertools.permutations(axes):
             for tri in triples:
-                rowbits = list(tri)
-                for tb in lanes + keep + nonround:      # remaining lane bits, then the previous order, then new bits
-                    if tb not in rowbits:
-                        rowbits.append(tb)
-                cand = TcLayout(list(digits), rowbits)
-                vec = 8 if _vec_digit(prev, cand.digits[0]) >= 0 else None
-                cost = _transition_cost(prev, cand.byte_of_bit, vec)
-                if ri == nlast:
-                    cost += _natural_cost(cand)
-                if best is None or cost < best[0]:
-                    best = (cost, cand)
+                for f in fourth:
+                    if f in tri:
+                        continue
+                    cand = TcLayout(list(digits), _fill_rows(list(tri) + ([f] if f is not None else []),
+                                                             lanes, keep, nonround))
+                    vec = 8 if _vec_digit(prev, cand.digits[0]) >= 0 else None
+                    cost = _transition_cost(prev, cand.byte_of_bit, vec)
+                    cost += _natural_cost(cand) if ri == nlast else _best_next_cost(cand, nxt_axes)
+                    if best is None or cost < best[0]:
+                        best = (cost, cand)
         layouts.append(best[1])
         prev = best[1]
-    return layouts
+    return tuple(layouts)
+
+
+def _choose_layouts(rounds_axes):
+    """Pick each round's digit order and row-bit order (greedy along the rounds, one round of lookahead).
+
+    The epilogue of round r (one source row per thread) writes round r+1's
+    operand; its cost depends only on where the source's five lane bits land
+    in the destination (bank bits 2-6: destination K bits 1-2 and row bits
+    0-2) and on whether the destination's K digit 0 is one of the source's
+    axes (8-byte vector stores).  Each candidate (digit order, which source
+    lane bits become row bits 0-2, which bit becomes row 3) is scored by the
+    exact wavefront count of its incoming epilogue plus the cheapest
+    outgoing one; the last round pays for its stores into the natural tile.
+    """
+    return list(_choose_layouts_cached(tuple(tuple(sorted(a)) for a in rounds_axes)))
 
 
 def _vec_digit(src, dst_first_axis):
@@ -601,7 +651,7 @@ def epilogue_wavefronts(src, dst, natural=False):
 def plan_tc_pass(p, n):
     """Pad a pass to 7 axes, plan its rounds and their layouts, compose each round's U (FP64)."""
     pp = pad_pass(p, n)
-    rounds = plan_rounds(pp, 3)
+    rounds = plan_rounds(pp, 3, pad='neighbors')
     layouts = _choose_layouts([axes for axes, _ in rounds])
     mats = []
     for (axes, rops), lay in zip(rounds, layouts):

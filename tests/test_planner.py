@@ -281,7 +281,7 @@ def test_tc_image_layout_and_split():
     parts = [np.zeros((64, 64)) for _ in range(3)]
     for i in range(3):
         parts[i].reshape(-1)[:] = img[4096 * i + P._KMAJOR].view(np.float16).astype(np.float64)
-    big, uh, ul = parts
+    big, ul, uh = parts
     assert np.array_equal(big, uh * P.TC_LO_SCALE)                  # 2**11 Uh is exact in FP16
     assert np.array_equal(uh, U.astype(np.float16).astype(np.float64))
     # Uh + 2**-11 Ul carries U to about 2**-22 relative
