@@ -21,14 +21,14 @@
 // 128-bit stores.  Every wait on an mbarrier is bounded: a wait that gives
 // up records an error in *status and the kernel drains and returns.
 //
-// Shared memory (dynamic, 152 KB): NAT 64 KB (cp.async landing buffer of
-// the next tile), AH / AL 32 KB each (round operand h / l, K-major
-// core-matrix FP16 layout, 256 rows x 64), B 24 KB (2**11 Uh and Ul stacked
-// as one 128-row operand, then Uh).  The h operand is read once per round
-// for both of its terms (N = 128 into two 64-column accumulators that the
-// epilogue adds).
-#include <mutex>
-
+// Two CTAs of 128 threads share an SM, so one CTA's tile load, barriers
+// and MMA waits overlap the other's work.  Shared memory per CTA (dynamic,
+// 88 KB): AH / AL 32 KB each (round operand h / l, K-major core-matrix FP16
+// layout, 256 rows x 64; together they also hold the natural FP32 tile that
+// cp.async streams in and the last round writes out), B 24 KB (2**11 Uh and
+// Ul stacked as one 128-row operand, then Uh).  The h operand is read once
+// per round for both of its terms (N = 128 into two 64-column accumulators
+// that the epilogue adds); each thread owns one row of each 128-row M block.
 #include <cuda_fp16.h>
 
 #include "dm_common.cuh"
@@ -38,15 +38,15 @@ namespace dmg {
 
 namespace tc {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 128;                  // two CTAs per SM
+constexpr int kCtasPerSm = 2;
 constexpr int kAxes = 7;                       // resident axes per tile
 constexpr int kTile = 1 << (2 * kAxes);        // 16384 coefficients
 constexpr int kGroups = kTile / 64;            // 256 rows per round
-constexpr uint32_t kNatBytes = kTile * 4;      // 64 KB
 constexpr uint32_t kABytes = kGroups * 64 * 2; // 32 KB per FP16 operand image
 constexpr uint32_t kBImage = 64 * 64 * 2;      // 8 KB per FP16 matrix image
 constexpr uint32_t kBBytes = 3 * kBImage;      // 24 KB
-constexpr uint32_t kSmemBytes = kNatBytes + 2 * kABytes + kBBytes;   // 152 KB
+constexpr uint32_t kSmemBytes = 2 * kABytes + kBBytes;   // 88 KB: two CTAs per SM
 constexpr int kUHalves = 3 * 64 * 64;          // FP16 values per round image
 constexpr float kLoScale = 2048.0f, kLoUnscale = 1.0f / 2048.0f;
 constexpr uint32_t kTmemCols = 256;            // two M = 128 blocks x N = 128 (D1 | D2)
@@ -190,22 +190,22 @@ __device__ __forceinline__ void store_all(const float (&v)[64], int vec, uint32_
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict__ st, const __grid_constant__ Pass p,
-                                                              const uint16_t *__restrict__ umats, int *status) {
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
+    pass_tc_kernel(float *__restrict__ st, const __grid_constant__ Pass p, const uint16_t *__restrict__ umats,
+                   int *status) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *NAT = smem;
-    unsigned char *AH = smem + kNatBytes;
+    unsigned char *AH = smem;             // operand h; with AL, the natural tile before and after the rounds
     unsigned char *AL = AH + kABytes;
     unsigned char *B = AL + kABytes;
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base_s;
-    __shared__ int64_t hi_off[16];
+    __shared__ int64_t hi_off[kTile / 4 / kThreads];
     __shared__ int abort_s;
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int64_t ntiles = int64_t(1) << (2 * p.m);
     const int64_t off_tid = tile_offset(p, 4 * tid);
-    if (tid < 16) hi_off[tid] = tile_offset(p, 4 * kThreads * tid);
+    for (int i = tid; i < kTile / 4 / kThreads; i += kThreads) hi_off[i] = tile_offset(p, 4 * kThreads * i);
     if (tid == 0) {
         abort_s = 0;
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
@@ -221,8 +221,7 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_s;
     uint32_t phase = 0;
-    // this thread's row in every round (warps 0-3: rows 0-127 = M block 0, warps 4-7: M block 1)
-    const uint32_t row = uint32_t(tid);
+    bool pending = false;   // an MMA batch committed but not yet waited for
 
     auto tile_base = [&](int64_t t) {
         int64_t base = 0;
@@ -232,13 +231,11 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
         }
         return base;
     };
-    auto load_tile = [&](int64_t t) {   // into NAT
-        if (t < ntiles) {
-            const float *src = st + tile_base(t) + off_tid;
-#pragma unroll
-            for (int i = 0; i < kTile / 4 / kThreads; ++i)
-                cp_async16(NAT + 4 * nat_swz(4 * (tid + kThreads * i)), src + hi_off[i]);
-        }
+    auto load_tile = [&](int64_t t) {   // natural layout into AH / AL (64 KB)
+        const float *src = st + tile_base(t) + off_tid;
+#pragma unroll 8
+        for (int i = 0; i < kTile / 4 / kThreads; ++i)
+            cp_async16(AH + 4 * nat_swz(4 * (tid + kThreads * i)), src + hi_off[i]);
         cp_async_commit();
     };
     auto load_u = [&](int r) {          // round r's three U images into B (contiguous)
@@ -252,43 +249,50 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
     };
 
     const int64_t t0 = blockIdx.x, dt = gridDim.x;
-    load_tile(t0);
     load_u(0);
     for (int64_t t = t0; t < ntiles; t += dt) {
+        load_tile(t);
         cp_async_wait_all();
         __syncthreads();
-        if (abort_s) break;
-        // ---- natural tile -> round 0's operand (h / l) ----
-        // Thread work items are (row, 8-value K chunk) pairs with the row's low three bits on
-        // the lane bits, so each 16-byte chunk store of an 8-lane phase covers the 8 rows of one
-        // core matrix: all 32 banks, no conflict.
+        // ---- natural tile -> round 0's operand (h / l), in place ----
+        // Work items are (row, 8-value K chunk) pairs with the row's low three bits on the lane
+        // bits, so each 16-byte chunk store of an 8-lane phase covers the 8 rows of one core
+        // matrix: all 32 banks.  Every thread reads all of its values before any is written.
         {
-            const float *nat = reinterpret_cast<const float *>(NAT);
+            constexpr int kItems = kGroups * 8 / kThreads;   // 16
+            const float *nat = reinterpret_cast<const float *>(AH);
             const float up = p.up;      // 2**n: the tile in units of 2**-n
-#pragma unroll 2
-            for (int q = 0; q < kGroups * 8 / kThreads; ++q) {
+            float x[kItems][8];
+#pragma unroll
+            for (int q = 0; q < kItems; ++q) {
                 const int i = tid + kThreads * q;
                 const int crow = ((i >> 6) << 3) | (i & 7), c = (i >> 3) & 7;
                 // chunk c holds K = 8c .. 8c + 7: K bits 3-5 come from c, bits 0-2 from the element
                 const uint32_t nb = xor_bits<8>(uint32_t(crow), p.natrow) ^ ((c & 1) ? p.natk[3] : 0u) ^
                                     ((c & 2) ? p.natk[4] : 0u) ^ ((c & 4) ? p.natk[5] : 0u);
-                float x[8];
                 if (p.vec0 == 0) {   // digit 0 is local axis 0: four adjacent natural elements
-                    const float4 a = *reinterpret_cast<const float4 *>(nat + nb);
-                    const float4 b = *reinterpret_cast<const float4 *>(nat + (nb ^ p.natk[2]));
-                    x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
-                    x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+                    const float4 a4 = *reinterpret_cast<const float4 *>(nat + nb);
+                    const float4 b4 = *reinterpret_cast<const float4 *>(nat + (nb ^ p.natk[2]));
+                    x[q][0] = a4.x; x[q][1] = a4.y; x[q][2] = a4.z; x[q][3] = a4.w;
+                    x[q][4] = b4.x; x[q][5] = b4.y; x[q][6] = b4.z; x[q][7] = b4.w;
                 } else {
 #pragma unroll
                     for (int e = 0; e < 8; ++e)
-                        x[e] = nat[nb ^ ((e & 1) ? p.natk[0] : 0u) ^ ((e & 2) ? p.natk[1] : 0u) ^ ((e & 4) ? p.natk[2] : 0u)];
+                        x[q][e] = nat[nb ^ ((e & 1) ? p.natk[0] : 0u) ^ ((e & 2) ? p.natk[1] : 0u) ^
+                                      ((e & 4) ? p.natk[2] : 0u)];
                 }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < kItems; ++q) {
+                const int i = tid + kThreads * q;
+                const int crow = ((i >> 6) << 3) | (i & 7), c = (i >> 3) & 7;
                 uint32_t hw[4], lw[4];
 #pragma unroll
                 for (int e = 0; e < 8; e += 2) {
                     unsigned short h0, l0, h1, l1;
-                    split_h(x[e] * up, h0, l0);
-                    split_h(x[e + 1] * up, h1, l1);
+                    split_h(x[q][e] * up, h0, l0);
+                    split_h(x[q][e + 1] * up, h1, l1);
                     hw[e >> 1] = uint32_t(h0) | (uint32_t(h1) << 16);
                     lw[e >> 1] = uint32_t(l0) | (uint32_t(l1) << 16);
                 }
@@ -297,12 +301,8 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
                 *reinterpret_cast<uint4 *>(AL + o) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
             }
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        load_tile(t + dt);   // NAT is free: stream the next tile during the rounds
         for (int r = 0; r < p.nrounds; ++r) {
             // round 0's U was waited for with the tile; later rounds wait for their U
-            // (which also completes the older next-tile group)
             if (r > 0) cp_async_wait_all();
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncthreads();
@@ -335,8 +335,12 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                     smem_u32(&mbar)));
             }
+            pending = true;
             const bool ok = mbar_wait(smem_u32(&mbar), phase);
-            phase ^= 1;
+            if (ok) {
+                phase ^= 1;
+                pending = false;
+            }
             if (!__all_sync(0xffffffffu, ok)) {
                 if ((tid & 31) == 0) {
                     atomicExch(status, 1);
@@ -348,10 +352,16 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
             if (abort_s) break;
             // B is free: fetch the next round's U (or round 0's, for the next tile)
             load_u(r + 1 < p.nrounds ? r + 1 : 0);
-            // ---- epilogue: D -> next operand (hi / lo), or the natural tile after the last round ----
-            float v[64];
-            {
-                const uint32_t ta = tmem + (uint32_t(32 * (warp & 3)) << 16) + uint32_t((warp >> 2) * 128);
+            // ---- epilogue: D -> next operand (h / l), or the natural tile after the last round ----
+            // thread tid holds row tid of M block 0 (TMEM columns 0-127) and of M block 1 (128-255)
+            const Round &R = p.rounds[r];
+            uint32_t tk[3][4];
+            digit_tables(R.kc, tk);
+            const bool last = r + 1 == p.nrounds;
+#pragma unroll 1
+            for (int mb = 0; mb < 2; ++mb) {
+                float v[64];
+                const uint32_t ta = tmem + (uint32_t(32 * warp) << 16) + uint32_t(mb * 128);
                 tmem_ld64(ta, v);
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {   // + the h Ul^T half, 16 columns at a time
@@ -360,38 +370,36 @@ __global__ void __launch_bounds__(kThreads, 1) pass_tc_kernel(float *__restrict_
 #pragma unroll
                     for (int j = 0; j < 16; ++j) v[16 * c + j] += w[j];
                 }
-            }
-            const Round &R = p.rounds[r];
-            uint32_t tk[3][4];
-            digit_tables(R.kc, tk);
-            const uint32_t base = xor_bits<8>(row, R.rowc);
-            if (r + 1 < p.nrounds) {
+                const uint32_t base = xor_bits<8>(uint32_t(tid + 128 * mb), R.rowc);
+                if (!last) {
 #pragma unroll
-                for (int j = 0; j < 64; ++j) v[j] *= kLoUnscale;
-                store_all<true>(v, R.vec, base, tk, AH, AL);
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            } else {
-                const float down = p.down * kLoUnscale;   // back to coefficients
+                    for (int j = 0; j < 64; ++j) v[j] *= kLoUnscale;
+                    store_all<true>(v, R.vec, base, tk, AH, AL);
+                } else {
+                    const float down = p.down * kLoUnscale;   // back to coefficients
 #pragma unroll
-                for (int j = 0; j < 64; ++j) v[j] *= down;
-                store_all<false>(v, R.vec, base, tk, AH, AL);   // natural FP32 layout into AH / AL (64 KB)
+                    for (int j = 0; j < 64; ++j) v[j] *= down;
+                    store_all<false>(v, R.vec, base, tk, AH, AL);   // natural FP32 layout into AH / AL
+                }
             }
+            if (!last) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         }
         if (abort_s) break;
         __syncthreads();
-        // ---- write the tile back with 128-bit stores ----
+        // ---- write the tile back with 128-bit stores; the next load waits for these reads ----
         {
             float *dst = st + tile_base(t) + off_tid;
             const float *out = reinterpret_cast<const float *>(AH);
-#pragma unroll
+#pragma unroll 8
             for (int i = 0; i < kTile / 4 / kThreads; ++i) {
                 const int e = 4 * (tid + kThreads * i);
                 *reinterpret_cast<float4 *>(dst + hi_off[i]) = *reinterpret_cast<const float4 *>(out + nat_swz(e));
             }
         }
-        // the next iteration's barrier orders these reads before AH is rewritten
+        __syncthreads();
     }
+    if (pending) mbar_wait(smem_u32(&mbar), phase);   // drain before the accumulator is released
     cp_async_wait_all();
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -486,7 +494,7 @@ extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, 
     });
     if (attr_err != cudaSuccess) return DM_ERR_CUDA;
     const int64_t ntiles = int64_t(1) << (2 * p.m);
-    int64_t grid = sm_count();
+    int64_t grid = int64_t(sm_count()) * tc::kCtasPerSm;
     if (grid > ntiles) grid = ntiles;
     tc::pass_tc_kernel<<<int(grid), tc::kThreads, tc::kSmemBytes, as_stream(stream)>>>(
         static_cast<float *>(state_dev), p, umats_dev, status_dev);

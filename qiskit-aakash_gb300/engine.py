@@ -166,20 +166,22 @@ class DeviceState:
             self._run_passes(passes)
 
     def _run_passes_tc(self, passes):
+        """Encode and launch pass by pass: the host plans pass i+1 while the GPU runs pass i."""
         torch = _torch()
-        umats = []
-        descs = [encode_pass_tc(p, self.n, umats) for p in passes]
-        host = np.concatenate(umats).view(np.int16)      # FP16 bit patterns
-        h = torch.from_numpy(host).pin_memory()
-        dev = h.to(self.device, non_blocking=True)
-        self.h2d_bytes += host.nbytes
-        mp = ctypes.c_void_p(dev.data_ptr())
         sp = ctypes.c_void_p(self.status.data_ptr())
-        for d in descs:
-            self._call('dm_apply_pass_tc', self.ptr, self.n, ctypes.byref(d), mp, ctypes.c_size_t(host.size), sp,
-                       self.stream, keep=(d, dev))
-        self.passes_run += len(descs)
-        self._keep = (h, dev)
+        keep = []
+        for p in passes:
+            umats = []
+            d = encode_pass_tc(p, self.n, umats)
+            host = np.concatenate(umats).view(np.int16)      # FP16 bit patterns
+            h = torch.from_numpy(host).pin_memory()
+            dev = h.to(self.device, non_blocking=True)
+            self.h2d_bytes += host.nbytes
+            self._call('dm_apply_pass_tc', self.ptr, self.n, ctypes.byref(d), ctypes.c_void_p(dev.data_ptr()),
+                       ctypes.c_size_t(host.size), sp, self.stream, keep=(d, dev))
+            keep.append((h, dev, d))
+        self.passes_run += len(passes)
+        self._keep = keep
         if int(self.status.item()) != 0:
             raise BasicAerError('a tensor-core pass abandoned a bounded wait (status %d)' % int(self.status.item()))
 
