@@ -31,6 +31,8 @@
 // that the epilogue adds); each thread owns one row of each 128-row M block.
 #include <cuda_fp16.h>
 
+#include <mutex>
+
 #include "dm_common.cuh"
 #include "dm_tcgen05.cuh"
 
