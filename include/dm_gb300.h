@@ -389,6 +389,15 @@ int dm_nbasis_probs_noalloc(const void *state_dev, int n, int dtype, const doubl
 int dm_gather(const void *state_dev, int n, int dtype, const int64_t *idx, int count,
               double *out_dev, void *stream);
 
+/* Shot counts from 2**m outcome probabilities (FP64, device), no counterpart
+ * in the reference (its dm_simulator has max_shots = 1 and reports
+ * probabilities only).  counts_dev receives 2**m int64 counts summing to
+ * shots; the draws are a deterministic function of seed.  m <= 20;
+ * scratch_dev: dm_sample_counts_scratch_bytes(m) bytes. */
+size_t dm_sample_counts_scratch_bytes(int m);
+int dm_sample_counts(const double *probs_dev, int m, int64_t shots, uint64_t seed, int64_t *counts_dev,
+                     void *scratch_dev, void *stream);
+
 /* ------------------------------------------------------------------ outputs */
 
 /* out[s] = a[s], with |a[s]| < threshold set to 0 (FP64 output, 4**n).

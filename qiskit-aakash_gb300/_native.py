@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG_DIR, 'csrc')
 INCLUDE = os.path.join(REPO_DIR, 'include')
 BUILD_DIR = os.path.join(PKG_DIR, '_build')
 LIB_PATH = os.path.join(PKG_DIR, 'libdmgb300.so')
-SOURCES = ['dm_misc.cu', 'dm_pass.cu', 'dm_state.cu', 'dm_measure.cu', 'dm_tc.cu', 'dm_mlp.cu']
+SOURCES = ['dm_misc.cu', 'dm_pass.cu', 'dm_state.cu', 'dm_measure.cu', 'dm_tc.cu', 'dm_mlp.cu', 'dm_sample.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '-Xptxas', '-warn-spills',
               '--expt-relaxed-constexpr']
@@ -187,6 +187,8 @@ SIGNATURES = {
     'dm_nbasis_probs': (_i, [_vp, _i, _i, _dp, _d, _vp, _vp, _vp]),
     'dm_nbasis_probs_noalloc': (_i, [_vp, _i, _i, _dp, _d, _vp, _vp]),
     'dm_gather': (_i, [_vp, _i, _i, _i64p, _i, _vp, _vp]),
+    'dm_sample_counts_scratch_bytes': (_sz, [_i]),
+    'dm_sample_counts': (_i, [_vp, _i, ctypes.c_int64, ctypes.c_uint64, _vp, _vp, _vp]),
     'dm_chop_copy': (_i, [_vp, _i, _i, _d, _vp, _vp]),
     'dm_chop_copy_range': (_i, [_vp, _i, _i, ctypes.c_int64, ctypes.c_int64, _d, _vp, _vp]),
     'dm_pauli_to_matrix_scratch_bytes': (_sz, [_i]),

@@ -63,6 +63,9 @@ class HostRecorder:
     def nbasis_probs(self, nvec, err):
         raise BasicAerError('batched programs read out Z ensemble probabilities only')
 
+    def sample_counts(self, shots, seed):
+        raise BasicAerError('batched programs report probabilities, not counts')
+
     def gather(self, indices):
         raise BasicAerError('batched programs read out Z ensemble probabilities only')
 

@@ -34,7 +34,10 @@ default True), ``tile_axes`` (resident axes per tile), ``register_rounds``
 (FP32 passes on tcgen05 as 64x64 transfer matrices in a 3-way FP16 split, default True) and
 ``coefficients_to_host`` (default True; False leaves ``coeffmatrix`` /
 ``densitymatrix`` out of the result, for callers that only need the
-measurement data of a large register).
+measurement data of a large register) and ``counts_shots`` / ``counts_seed``
+(default 0: off; with shots > 0 every ensemble measurement also reports
+``counts``, {bit string: count} of that many shots drawn on the device from
+its outcome probabilities; the reference reports probabilities only).
 """
 import copy
 import logging
@@ -225,6 +228,8 @@ class DmSimulatorGPU(_Base):
         self._fusion = True
         self._tile_axes = None
         self._coefficients_to_host = True
+        self._counts_shots = 0
+        self._counts_seed = 0
         self._register_rounds = True
         self._tensor_cores = True
         self.last_run_stats = {}
@@ -348,6 +353,13 @@ class DmSimulatorGPU(_Base):
             self._register_rounds = bool(backend_options['register_rounds'])
         if 'coefficients_to_host' in backend_options:
             self._coefficients_to_host = bool(backend_options['coefficients_to_host'])
+        if 'counts_shots' in backend_options:
+            shots = int(backend_options['counts_shots'])
+            if shots < 0:
+                raise BasicAerError('counts_shots must be >= 0')
+            self._counts_shots = shots
+        if 'counts_seed' in backend_options:
+            self._counts_seed = int(backend_options['counts_seed'])
 
     def _initialize_errors(self):
         """dm_simulator.py:273-282."""
@@ -692,6 +704,9 @@ class DmSimulatorGPU(_Base):
                             raise BasicAerError('unrecognised ensemble basis %r' % (spec,))
                         prob, _, _ = self._add_ensemble_measure(basis, add_param, err)
                         data['ensemble_probability'] = prob
+                        if self._counts_shots > 0:
+                            cnt = self._dev.sample_counts(self._counts_shots, self._counts_seed)
+                            data['counts'] = {k: int(c) for k, c in zip(prob, cnt) if c}
                         break
                 else:
                     err_msg = '{0} encountered unrecognized operation "{1}"'

@@ -240,6 +240,19 @@ class DeviceState:
         self.last_readout = out
         return self._to_host(out)
 
+    def sample_counts(self, shots, seed):
+        """Shot counts (numpy int64, 2**m) drawn on the device from the last probability read-out."""
+        torch = _torch()
+        probs = self.last_readout
+        m = int(probs.numel()).bit_length() - 1
+        L = N.lib()
+        scratch = torch.empty(max(L.dm_sample_counts_scratch_bytes(m), 8), dtype=torch.uint8, device=self.device)
+        counts = torch.empty(2 ** m, dtype=torch.int64, device=self.device)
+        self._call('dm_sample_counts', ctypes.c_void_p(probs.data_ptr()), m, ctypes.c_int64(int(shots)),
+                   ctypes.c_uint64(int(seed) & (2 ** 64 - 1)), ctypes.c_void_p(counts.data_ptr()),
+                   ctypes.c_void_p(scratch.data_ptr()), self.stream, keep=(counts, scratch))
+        return self._to_host(counts)
+
     def gather(self, indices):
         self.flush()
         torch = _torch()
