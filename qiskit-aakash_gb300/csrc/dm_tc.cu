@@ -123,30 +123,24 @@ __device__ __forceinline__ void digit_tables(const uint32_t *kc, uint32_t (&t)[3
     }
 }
 
-// x -> (h, l): h = fp16(x), l = fp16(2**11 (x - h)), as FP16 bit patterns.
-__device__ __forceinline__ void split_h(float x, unsigned short &h, unsigned short &l) {
-    const __half hh = __float2half_rn(x);
-    h = __half_as_ushort(hh);
-    l = __half_as_ushort(__float2half_rn((x - __half2float(hh)) * kLoScale));
-}
-
-__device__ __forceinline__ void put_split(unsigned char *AH, unsigned char *AL, uint32_t o, float x) {
-    unsigned short h, l;
-    split_h(x, h, l);
-    *reinterpret_cast<unsigned short *>(AH + o) = h;
-    *reinterpret_cast<unsigned short *>(AL + o) = l;
+// x -> (h, l): h = fp16(x), l = fp16(2**11 (x - h)), two values at once with packed conversions
+// (h2 = (fp16(a), fp16(b)) as FP16 bit patterns, l2 likewise)
+__device__ __forceinline__ void split2(float a, float b, uint32_t &h2, uint32_t &l2) {
+    const __half2 hh = __floats2half2_rn(a, b);
+    const float2 hf = __half22float2(hh);
+    const __half2 ll = __floats2half2_rn((a - hf.x) * kLoScale, (b - hf.y) * kLoScale);
+    h2 = *reinterpret_cast<const uint32_t *>(&hh);
+    l2 = *reinterpret_cast<const uint32_t *>(&ll);
 }
 
 // four values adjacent in K: one 64-bit store into each image
 __device__ __forceinline__ void put_split4(unsigned char *AH, unsigned char *AL, uint32_t o, float a, float b,
                                            float c, float d) {
-    unsigned short ha, la, hb, lb, hc, lc, hd, ld;
-    split_h(a, ha, la);
-    split_h(b, hb, lb);
-    split_h(c, hc, lc);
-    split_h(d, hd, ld);
-    *reinterpret_cast<uint2 *>(AH + o) = make_uint2(uint32_t(ha) | (uint32_t(hb) << 16), uint32_t(hc) | (uint32_t(hd) << 16));
-    *reinterpret_cast<uint2 *>(AL + o) = make_uint2(uint32_t(la) | (uint32_t(lb) << 16), uint32_t(lc) | (uint32_t(ld) << 16));
+    uint32_t h0, l0, h1, l1;
+    split2(a, b, h0, l0);
+    split2(c, d, h1, l1);
+    *reinterpret_cast<uint2 *>(AH + o) = make_uint2(h0, h1);
+    *reinterpret_cast<uint2 *>(AL + o) = make_uint2(l0, l1);
 }
 
 // Epilogue stores of one thread's 64 values (K index j = d0 + 4 d1 + 16 d2)
@@ -180,14 +174,23 @@ __device__ __forceinline__ void store_all(const float (&v)[64], int vec, uint32_
         store_vec<1, SPLIT>(v, base, t, AH, AL);
     } else if (vec == 2) {
         store_vec<2, SPLIT>(v, base, t, AH, AL);
+    } else if (SPLIT) {
+#pragma unroll
+        for (int j = 0; j < 64; j += 2) {   // conversions in pairs, 16-bit stores
+            uint32_t h2, l2;
+            split2(v[j], v[j + 1], h2, l2);
+            const uint32_t o0 = base ^ t[0][j & 3] ^ t[1][(j >> 2) & 3] ^ t[2][j >> 4];
+            const uint32_t o1 = o0 ^ t[0][(j & 3) ^ 1] ^ t[0][j & 3];
+            *reinterpret_cast<unsigned short *>(AH + o0) = (unsigned short)(h2 & 0xFFFFu);
+            *reinterpret_cast<unsigned short *>(AL + o0) = (unsigned short)(l2 & 0xFFFFu);
+            *reinterpret_cast<unsigned short *>(AH + o1) = (unsigned short)(h2 >> 16);
+            *reinterpret_cast<unsigned short *>(AL + o1) = (unsigned short)(l2 >> 16);
+        }
     } else {
 #pragma unroll
         for (int j = 0; j < 64; ++j) {
             const uint32_t o = base ^ t[0][j & 3] ^ t[1][(j >> 2) & 3] ^ t[2][j >> 4];
-            if (SPLIT)
-                put_split(AH, AL, o, v[j]);
-            else
-                reinterpret_cast<float *>(AH)[o] = v[j];
+            reinterpret_cast<float *>(AH)[o] = v[j];
         }
     }
 }
@@ -291,13 +294,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
                 const int crow = ((i >> 6) << 3) | (i & 7), c = (i >> 3) & 7;
                 uint32_t hw[4], lw[4];
 #pragma unroll
-                for (int e = 0; e < 8; e += 2) {
-                    unsigned short h0, l0, h1, l1;
-                    split_h(x[q][e] * up, h0, l0);
-                    split_h(x[q][e + 1] * up, h1, l1);
-                    hw[e >> 1] = uint32_t(h0) | (uint32_t(h1) << 16);
-                    lw[e >> 1] = uint32_t(l0) | (uint32_t(l1) << 16);
-                }
+                for (int e = 0; e < 8; e += 2) split2(x[q][e] * up, x[q][e + 1] * up, hw[e >> 1], lw[e >> 1]);
                 const uint32_t o = row_off(crow) + uint32_t(c) * kLBO;
                 *reinterpret_cast<uint4 *>(AH + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
                 *reinterpret_cast<uint4 *>(AL + o) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
