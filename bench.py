@@ -157,7 +157,7 @@ def measured_peaks():
 
 def profiled_traffic():
     """Per-launch DRAM bytes of the pass kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, 'profiles', 'pass_tc_kernel_fp32_n16.md')
+    path = os.path.join(ROOT, 'profiles', 'pass_tc_kernel_fp16_split_fp32_n14.md')
     try:
         for line in open(path):
             if line.startswith('traffic_bytes_per_launch:'):
