@@ -286,6 +286,8 @@ class DmSimulatorGPU(_Base):
         self._decay_factor = self.DEFAULT_OPTIONS["decay_factor"]
         self._depolarization_factor = self.DEFAULT_OPTIONS["depolarization_factor"]
         self._bell_depolarization_factor = self.DEFAULT_OPTIONS["bell_depolarization_factor"]
+        self._counts_shots = 0          # shot counts are a per-run request
+        self._counts_seed = 0
         if backend_options is None:
             backend_options = {}
         if 'initial_densitymatrix' in backend_options:
