@@ -276,13 +276,15 @@ def device_max_abs_diff(torch, a32, b64, chunk=1 << 28):
     return m
 
 
-def per_gate_kind(torch, N, n=14, reps=3):
-    """HBM GB/s of each single-operation sweep at n qubits, FP64 (2 * 4**n * 8 bytes per sweep)."""
+def per_gate_kind(torch, N, n=14, reps=3, dtype=None):
+    """HBM GB/s of each single-operation sweep at n qubits (2 * 4**n * s bytes per sweep, s = 8 FP64 / 4 FP32)."""
     import ctypes
     L = N.lib()
-    st = torch.empty(4 ** n, dtype=torch.float64, device='cuda')
+    dtype = N.DM_F64 if dtype is None else dtype
+    esize = 8 if dtype == N.DM_F64 else 4
+    st = torch.empty(4 ** n, dtype=torch.float64 if dtype == N.DM_F64 else torch.float32, device='cuda')
     v = np.tile(np.array([1.0, 0.0, 0.0, 1.0]), n)
-    N.call('dm_init_product', ctypes.c_void_p(st.data_ptr()), n, N.DM_F64,
+    N.call('dm_init_product', ctypes.c_void_p(st.data_ptr()), n, dtype,
            v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 0.5 ** n, None)
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     ptr = ctypes.c_void_p(st.data_ptr())
@@ -303,16 +305,16 @@ def per_gate_kind(torch, N, n=14, reps=3):
         return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
     kinds = {
-        'u3 (4x4 map, one qubit)': (lambda: N.call('dm_apply_map1', ptr, n, N.DM_F64, n // 2, arr(u3), s), 1),
-        'memory noise (one qubit)': (lambda: N.call('dm_apply_map1', ptr, n, N.DM_F64, 0, arr(noise), s), 1),
-        'cx ideal (signed permutation)': (lambda: N.call('dm_apply_cx', ptr, n, N.DM_F64, 3, 4, arr([1.0, 0.0]), s), 1),
-        'cx with tsp error': (lambda: N.call('dm_apply_cx', ptr, n, N.DM_F64, 3, 4, arr([0.98, 0.02]), s), 1),
+        'u3 (4x4 map, one qubit)': (lambda: N.call('dm_apply_map1', ptr, n, dtype, n // 2, arr(u3), s), 1),
+        'memory noise (one qubit)': (lambda: N.call('dm_apply_map1', ptr, n, dtype, 0, arr(noise), s), 1),
+        'cx ideal (signed permutation)': (lambda: N.call('dm_apply_cx', ptr, n, dtype, 3, 4, arr([1.0, 0.0]), s), 1),
+        'cx with tsp error': (lambda: N.call('dm_apply_cx', ptr, n, dtype, 3, 4, arr([0.98, 0.02]), s), 1),
         'memory noise, every qubit (n sweeps)': (
-            lambda: N.call('dm_apply_memory_noise', ptr, n, N.DM_F64, 0.995, 1.0, 0.998, s), n),
+            lambda: N.call('dm_apply_memory_noise', ptr, n, dtype, 0.995, 1.0, 0.998, s), n),
         'ensemble Z probabilities (2^n gather + WHT)': (
-            lambda: N.call('dm_axis_probs', ptr, n, N.DM_F64, mode, 0.999, ctypes.c_void_p(out.data_ptr()), s), None),
+            lambda: N.call('dm_axis_probs', ptr, n, dtype, mode, 0.999, ctypes.c_void_p(out.data_ptr()), s), None),
         'ensemble N probabilities (full contraction)': (
-            lambda: N.call('dm_nbasis_probs', ptr, n, N.DM_F64, nvec, 0.999, ctypes.c_void_p(out.data_ptr()),
+            lambda: N.call('dm_nbasis_probs', ptr, n, dtype, nvec, 0.999, ctypes.c_void_p(out.data_ptr()),
                            ctypes.c_void_p(scratch.data_ptr()), s), 0.5),
     }
     hbm, _ = measured_peaks()
@@ -330,12 +332,13 @@ def per_gate_kind(torch, N, n=14, reps=3):
         ms = a.elapsed_time(b) / reps
         ent = {'ms': ms}
         if sweeps:
-            gbs = sweeps * 2 * 4 ** n * 8 / (ms / 1e3) / 1e9
+            gbs = sweeps * 2 * 4 ** n * esize / (ms / 1e3) / 1e9
             ent.update(gbs=gbs, frac_of_hbm=gbs / hbm)
         res[name] = ent
     del st, out, scratch
     torch.cuda.empty_cache()
-    return {'n_qubits': n, 'dtype': 'f64', 'bytes_per_sweep': 2 * 4 ** n * 8, 'kinds': res}
+    return {'n_qubits': n, 'dtype': 'f64' if esize == 8 else 'f32', 'bytes_per_sweep': 2 * 4 ** n * esize,
+            'kinds': res}
 
 
 def batch_cpu_sample(pkg, specs, budget_s=8.0):
@@ -647,6 +650,7 @@ def run_ours(args):
         line = {'metric': METRIC, 'legs': sorted(legs), 'note': 'headline leg not run'}
     if 'headline' in legs and not args.no_gate_kinds:
         line['per_gate_kind_fp64'] = per_gate_kind(torch, N)
+        line['per_gate_kind_fp32'] = per_gate_kind(torch, N, dtype=N.DM_F32)
     if 'batch' in legs and args.batch > 0:
         line['batched_sweep'] = batch_leg(args, pkg, torch, N)
     if 'surrogate' in legs and args.surrogate_train > 0:

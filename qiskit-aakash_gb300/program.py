@@ -251,6 +251,8 @@ def plan_rounds(p, width, pad='low'):
         # round's
         nxt = sorted(planned[i + 1].axes) if i + 1 < len(planned) and pad == 'neighbors' else []
         prv = rounds[-1][0] if rounds and pad == 'neighbors' else []
+        if pad == 'neighbors' and i == 0:
+            nxt = [0] + nxt      # round 0 reads the natural tile: axis 0 gives 16-byte loads
         for a in nxt + prv + list(range(k)):
             if len(axes) >= width:
                 break
