@@ -48,7 +48,7 @@ constexpr int kGroups = kTile / 64;            // 256 rows per round
 constexpr uint32_t kABytes = kGroups * 64 * 2; // 32 KB per FP16 operand image
 constexpr uint32_t kBImage = 64 * 64 * 2;      // 8 KB per FP16 matrix image
 constexpr uint32_t kBBytes = 3 * kBImage;      // 24 KB
-constexpr uint32_t kSmemBytes = 2 * kABytes + kBBytes;   // 88 KB: two CTAs per SM
+constexpr uint32_t kSmemBytes = 2 * kABytes + 2 * kBBytes;   // 112 KB: two CTAs per SM
 constexpr int kUHalves = 3 * 64 * 64;          // FP16 values per round image
 constexpr float kLoScale = 2048.0f, kLoUnscale = 1.0f / 2048.0f;
 constexpr uint32_t kTmemCols = 256;            // two M = 128 blocks x N = 128 (D1 | D2)
@@ -243,18 +243,23 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
             cp_async16(AH + 4 * nat_swz(4 * (tid + kThreads * i)), src + hi_off[i]);
         cp_async_commit();
     };
-    auto load_u = [&](int r) {          // round r's three U images into B (contiguous)
+    // U images are double-buffered: round g (counted across tiles) uses B + (g & 1) * kBBytes, and
+    // the images of round g + 2 are fetched as soon as round g's MMAs complete
+    auto load_u = [&](int r, uint32_t buf) {
         const uint16_t *src = umats + p.rounds[r].umoff;
+        unsigned char *dst = B + buf * kBBytes;
 #pragma unroll
         for (int i = 0; i < int(kBBytes) / 16 / kThreads; ++i) {
             const int c = tid + kThreads * i;
-            cp_async16(B + 16 * c, src + 8 * c);
+            cp_async16(dst + 16 * c, src + 8 * c);
         }
         cp_async_commit();
     };
 
     const int64_t t0 = blockIdx.x, dt = gridDim.x;
-    load_u(0);
+    uint32_t g = 0;
+    load_u(0, 0);
+    load_u(p.nrounds > 1 ? 1 : 0, 1);
     for (int64_t t = t0; t < ntiles; t += dt) {
         load_tile(t);
         cp_async_wait_all();
@@ -301,15 +306,15 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
             }
         }
         for (int r = 0; r < p.nrounds; ++r) {
-            // round 0's U was waited for with the tile; later rounds wait for their U
-            if (r > 0) cp_async_wait_all();
+            // this round's U was fetched at least one round ago: only the newest group may stay in flight
+            tcg::cp_async_wait_1();
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (tid == 0) {
                 // D[:, 0:64] = h (2**11 Uh)^T + l Uh^T and D[:, 64:128] = h Ul^T: the h operand is
                 // read once for both of its terms (N = 128 over the stacked images 2**11 Uh | Ul)
-                const uint32_t ah = smem_u32(AH), al = smem_u32(AL), b0 = smem_u32(B);
+                const uint32_t ah = smem_u32(AH), al = smem_u32(AL), b0 = smem_u32(B + (g & 1) * kBBytes);
 #pragma unroll
                 for (int mb = 0; mb < 2; ++mb) {
                     const uint32_t d = tmem + mb * 128;
@@ -349,8 +354,9 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             __syncthreads();
             if (abort_s) break;
-            // B is free: fetch the next round's U (or round 0's, for the next tile)
-            load_u(r + 1 < p.nrounds ? r + 1 : 0);
+            // this round's B buffer is free: fetch the U of the round after next (cyclic over tiles)
+            load_u((r + 2) % p.nrounds, g & 1);
+            ++g;
             // ---- epilogue: D -> next operand (h / l), or the natural tile after the last round ----
             // thread tid holds row tid of M block 0 (TMEM columns 0-127) and of M block 1 (128-255)
             const Round &R = p.rounds[r];
@@ -487,13 +493,21 @@ extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, 
     }
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
+    static int per_sm = 1;
     std::call_once(once, [] {
         attr_err = cudaFuncSetAttribute(tc::pass_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(tc::kSmemBytes));
+        // CTAs that are resident together (two when shared memory and registers allow)
+        if (attr_err == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc::pass_tc_kernel, tc::kThreads,
+                                                          tc::kSmemBytes) != cudaSuccess)
+            per_sm = 1;
+        if (per_sm < 1) per_sm = 1;
+        if (per_sm > tc::kCtasPerSm) per_sm = tc::kCtasPerSm;
     });
     if (attr_err != cudaSuccess) return DM_ERR_CUDA;
     const int64_t ntiles = int64_t(1) << (2 * p.m);
-    int64_t grid = int64_t(sm_count()) * tc::kCtasPerSm;
+    int64_t grid = int64_t(sm_count()) * per_sm;
     if (grid > ntiles) grid = ntiles;
     tc::pass_tc_kernel<<<int(grid), tc::kThreads, tc::kSmemBytes, as_stream(stream)>>>(
         static_cast<float *>(state_dev), p, umats_dev, status_dev);
