@@ -48,7 +48,7 @@ constexpr int kGroups = kTile / 64;            // 256 rows per round
 constexpr uint32_t kABytes = kGroups * 64 * 2; // 32 KB per FP16 operand image
 constexpr uint32_t kBImage = 64 * 64 * 2;      // 8 KB per FP16 matrix image
 constexpr uint32_t kBBytes = 3 * kBImage;      // 24 KB
-constexpr uint32_t kSmemBytes = 2 * kABytes + 2 * kBBytes;   // 112 KB: two CTAs per SM
+constexpr uint32_t kSmemBytes = 2 * kABytes + kBBytes;   // 88 KB: two CTAs per SM
 constexpr int kUHalves = 3 * 64 * 64;          // FP16 values per round image
 constexpr float kLoScale = 2048.0f, kLoUnscale = 1.0f / 2048.0f;
 constexpr uint32_t kTmemCols = 256;            // two M = 128 blocks x N = 128 (D1 | D2)
@@ -243,23 +243,18 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
             cp_async16(AH + 4 * nat_swz(4 * (tid + kThreads * i)), src + hi_off[i]);
         cp_async_commit();
     };
-    // U images are double-buffered: round g (counted across tiles) uses B + (g & 1) * kBBytes, and
-    // the images of round g + 2 are fetched as soon as round g's MMAs complete
-    auto load_u = [&](int r, uint32_t buf) {
+    auto load_u = [&](int r) {          // round r's three U images into B (contiguous)
         const uint16_t *src = umats + p.rounds[r].umoff;
-        unsigned char *dst = B + buf * kBBytes;
 #pragma unroll
         for (int i = 0; i < int(kBBytes) / 16 / kThreads; ++i) {
             const int c = tid + kThreads * i;
-            cp_async16(dst + 16 * c, src + 8 * c);
+            cp_async16(B + 16 * c, src + 8 * c);
         }
         cp_async_commit();
     };
 
     const int64_t t0 = blockIdx.x, dt = gridDim.x;
-    uint32_t g = 0;
-    load_u(0, 0);
-    load_u(p.nrounds > 1 ? 1 : 0, 1);
+    load_u(0);
     for (int64_t t = t0; t < ntiles; t += dt) {
         load_tile(t);
         cp_async_wait_all();
@@ -306,15 +301,15 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
             }
         }
         for (int r = 0; r < p.nrounds; ++r) {
-            // this round's U was fetched at least one round ago: only the newest group may stay in flight
-            tcg::cp_async_wait_1();
+            // round 0's U was waited for with the tile; later rounds wait for their U
+            if (r > 0) cp_async_wait_all();
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (tid == 0) {
                 // D[:, 0:64] = h (2**11 Uh)^T + l Uh^T and D[:, 64:128] = h Ul^T: the h operand is
                 // read once for both of its terms (N = 128 over the stacked images 2**11 Uh | Ul)
-                const uint32_t ah = smem_u32(AH), al = smem_u32(AL), b0 = smem_u32(B + (g & 1) * kBBytes);
+                const uint32_t ah = smem_u32(AH), al = smem_u32(AL), b0 = smem_u32(B);
 #pragma unroll
                 for (int mb = 0; mb < 2; ++mb) {
                     const uint32_t d = tmem + mb * 128;
@@ -354,9 +349,8 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             __syncthreads();
             if (abort_s) break;
-            // this round's B buffer is free: fetch the U of the round after next (cyclic over tiles)
-            load_u((r + 2) % p.nrounds, g & 1);
-            ++g;
+            // B is free: fetch the next round's U (or round 0's, for the next tile)
+            load_u(r + 1 < p.nrounds ? r + 1 : 0);
             // ---- epilogue: D -> next operand (h / l), or the natural tile after the last round ----
             // thread tid holds row tid of M block 0 (TMEM columns 0-127) and of M block 1 (128-255)
             const Round &R = p.rounds[r];
