@@ -514,6 +514,19 @@ def _transition_cost(src, dst_off, vec):
     return n * w + n // 4
 
 
+def _conversion_cost(layout):
+    """Shared-memory load wavefronts of one warp converting the natural tile into round 0 (layout).
+
+    A warp's lanes are (row bits 0-2, chunk bits = K bits 3-4) of 8-value
+    chunks; with local axis 0 as digit 0 the 8 values are two 16-byte loads,
+    otherwise eight 4-byte loads."""
+    offs = tuple(4 * nat_swz(1 << tb) for tb in layout.rowbits[:3]) + \
+        tuple(4 * nat_swz(1 << tb) for tb in layout.kbits[3:5])
+    vec = layout.digits[0] == 0
+    w = _store_wavefronts(offs, 16 if vec else 4)
+    return (2 if vec else 8) * w
+
+
 def _natural_cost(layout):
     vec = 16 if _vec_digit(layout, 0) >= 0 else 0
     return _transition_cost(layout, lambda tb: 4 * nat_swz(1 << tb), vec)
@@ -554,14 +567,17 @@ def _choose_layouts_cached(rounds_axes):
         nonround = [tb for tb in range(2 * TC_AXES) if tb // 2 not in axes]
         nxt_axes = set(rounds_axes[ri + 1]) if ri < nlast else None
         if prev is None:
-            digits = ([0] + [a for a in axes if a != 0]) if 0 in axes else axes
+            # round 0: its rows 0-2 and K bits 3-4 are the lanes of the conversion's natural-tile
+            # loads; its rows 0-4 the lanes of its own epilogue
+            orders = [[0] + [a for a in axes if a != 0]] if 0 in axes else list(itertools.permutations(axes))
             best = None
-            fourth = [None] + ([tb for tb in nonround if tb % 2 == 0 and tb // 2 in nxt_axes] if nxt_axes else [])
-            for f in fourth:
-                cand = TcLayout(digits, _fill_rows([f] if f is not None else [], [], [], nonround))
-                cost = _best_next_cost(cand, nxt_axes) if nxt_axes else _natural_cost(cand)
-                if best is None or cost < best[0]:
-                    best = (cost, cand)
+            for digits in orders:
+                for tri in itertools.combinations(nonround, 3):
+                    cand = TcLayout(list(digits), _fill_rows(list(tri), [], [], nonround))
+                    cost = _conversion_cost(cand)
+                    cost += _best_next_cost(cand, nxt_axes) if nxt_axes else _natural_cost(cand)
+                    if best is None or cost < best[0]:
+                        best = (cost, cand)
             layouts.append(best[1])
             prev = best[1]
             continue
