@@ -487,21 +487,14 @@ extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, 
     }
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
-    static int per_sm = 1;
     std::call_once(once, [] {
         attr_err = cudaFuncSetAttribute(tc::pass_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(tc::kSmemBytes));
-        // CTAs that are resident together (two when shared memory and registers allow)
-        if (attr_err == cudaSuccess &&
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc::pass_tc_kernel, tc::kThreads,
-                                                          tc::kSmemBytes) != cudaSuccess)
-            per_sm = 1;
-        if (per_sm < 1) per_sm = 1;
-        if (per_sm > tc::kCtasPerSm) per_sm = tc::kCtasPerSm;
     });
     if (attr_err != cudaSuccess) return DM_ERR_CUDA;
     const int64_t ntiles = int64_t(1) << (2 * p.m);
-    int64_t grid = int64_t(sm_count()) * per_sm;
+    // 88 KB of shared memory, <= 256 registers and 256 TMEM columns per CTA: two CTAs per SM
+    int64_t grid = int64_t(sm_count()) * tc::kCtasPerSm;
     if (grid > ntiles) grid = ntiles;
     tc::pass_tc_kernel<<<int(grid), tc::kThreads, tc::kSmemBytes, as_stream(stream)>>>(
         static_cast<float *>(state_dev), p, umats_dev, status_dev);

@@ -28,8 +28,6 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-// all but the newest committed group complete
-__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
 // Wait for an mbarrier phase; gives up (returns false) after kSpinLimit polls.
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
