@@ -58,6 +58,8 @@ enum dm_op_kind {
 
 /* flags of DM_OP_MAP1 */
 #define DM_MAP1_ROW0_IDENTITY 1   /* row 0 of the map is (1,0,0,0): the I component is unchanged */
+#define DM_MAP1_XY_UNITAL 2       /* entries (1,0) and (2,0) are 0: X and Y take no I component
+                                     (register rounds only; with ROW0_IDENTITY: 10 FMAs per 4 values) */
 /* flags of DM_OP_CX */
 #define DM_CX_IDEAL 1             /* (c,s,c2,s2,cs) = (1,0,1,0,0): a signed permutation */
 

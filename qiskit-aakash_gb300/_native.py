@@ -32,6 +32,7 @@ DM_MAX_ROUNDS = 48
 DM_ROUND_AXES = {0: 2, 1: 3}     # dtype -> axes per register round
 DM_OP_MAP1, DM_OP_MAP2, DM_OP_DIAG2, DM_OP_CX = 1, 2, 3, 4
 DM_MAP1_ROW0_IDENTITY = 1
+DM_MAP1_XY_UNITAL = 2
 DM_CX_IDEAL = 1
 
 

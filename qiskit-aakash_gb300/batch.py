@@ -149,6 +149,7 @@ class _Plan:
                         m = np.asarray(op.data).reshape(16)
                         row0 = m[0] == 1.0 and not m[1:4].any()
                         flags |= N.DM_MAP1_ROW0_IDENTITY if row0 else 0
+                        flags |= N.DM_MAP1_XY_UNITAL if (m[4] == 0.0 and m[8] == 0.0) else 0
                         size = 16
                     elif op.kind == 'cx':
                         d.kind = N.DM_OP_CX
@@ -164,7 +165,8 @@ class _Plan:
                         raise BasicAerError('batched programs hold 4x4 maps, CX and diagonal pair maps only')
                     d.flags = flags
                     self.slots.append((op.kind, list(op.src), op.ideal,
-                                       (flags & N.DM_MAP1_ROW0_IDENTITY) if op.kind == 'map1' else 0))
+                                       (flags & (N.DM_MAP1_ROW0_IDENTITY | N.DM_MAP1_XY_UNITAL))
+                                       if op.kind == 'map1' else 0))
                     self.mats_len += size
                     o += 1
                 bp.round_end[ri] = o
@@ -181,8 +183,10 @@ class _Plan:
                 for i in src[1:]:
                     m = ops[i].data @ m
                 m = m.reshape(16)
-                if row0 and not (m[0] == 1.0 and not m[1:4].any()):
+                if (row0 & N.DM_MAP1_ROW0_IDENTITY) and not (m[0] == 1.0 and not m[1:4].any()):
                     raise BasicAerError('instance does not share the plan (I row)')
+                if (row0 & N.DM_MAP1_XY_UNITAL) and (m[4] != 0.0 or m[8] != 0.0):
+                    raise BasicAerError('instance does not share the plan (I column)')
                 out[pos:pos + 16] = m
                 pos += 16
             elif kind == 'cx':

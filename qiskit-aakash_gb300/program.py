@@ -309,6 +309,7 @@ def encode_pass(p, mats, dtype_np, round_width=None, n=None):
             o.kind = N.DM_OP_MAP1
             m = np.ascontiguousarray(op.data, dtype=np.float64).reshape(16)
             flags = N.DM_MAP1_ROW0_IDENTITY if (m[0] == 1.0 and not m[1:4].any()) else 0
+            flags |= N.DM_MAP1_XY_UNITAL if (m[4] == 0.0 and m[8] == 0.0) else 0
             o.b = 0
         elif op.kind == 'cx':
             o.kind = N.DM_OP_CX

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from oracle import dm_oracle as O
+from qiskit_aakash_gb300 import _native as N
 from qiskit_aakash_gb300 import program as P
 
 
@@ -299,3 +300,21 @@ def test_fp16_three_way_split_accuracy():
     ul = ((U - uh) * P.TC_LO_SCALE).astype(np.float16).astype(np.float64)
     D = (h @ (uh * P.TC_LO_SCALE).T + lo @ uh.T + h @ ul.T) / P.TC_LO_SCALE
     assert np.max(np.abs(D - x @ U.T)) < 2e-6 * np.abs(x @ U.T).max()
+
+
+def test_xy_unital_flag_marks_exactly_the_maps_without_i_in_x_and_y():
+    """DM_MAP1_XY_UNITAL is set from the composed matrix itself (a product of such maps need not be one)."""
+    n = 6
+    rot = P.u_gate_ptm('u3', [0.3, 0.2, 0.1], {'rx': [1, 0], 'ry': [1, 0], 'rz': [1, 0]})
+    noise = P.noise_ptm(0.99, 0.9, 0.98)
+    assert rot[1, 0] == 0 and rot[2, 0] == 0 and noise[1, 0] == 0 and noise[2, 0] == 0
+    both = rot @ noise                      # noise first, then the rotation: X picks up I
+    assert both[1, 0] != 0 or both[2, 0] != 0
+    ops = [P.Op('map1', (5,), noise), P.Op('map1', (4,), rot), P.Op('map1', (3,), rot @ noise)]
+    mats = []
+    p = P.plan_passes(ops, n, 6, 2)[0]
+    dp = P.encode_pass(p, mats, np.float64, 2, n)
+    for i in range(dp.nops):
+        m = mats[i].reshape(16)
+        xy = m[4] == 0 and m[8] == 0
+        assert bool(dp.ops[i].flags & N.DM_MAP1_XY_UNITAL) == xy
