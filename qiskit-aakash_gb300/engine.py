@@ -13,7 +13,7 @@ import numpy as np
 
 from . import _native as N
 from .exceptions import BasicAerError
-from .program import TC_AXES, Op, cx_coefficients, encode_pass, encode_pass_tc, plan_passes
+from .program import TC_AXES, Op, TcPlanError, cx_coefficients, encode_pass, encode_pass_tc, plan_passes
 
 # Tile sizes of the fused pass: 4**6 FP64 = 32 KB and 4**7 FP32 = 64 KB of
 # shared memory per tile; the two lowest qubit axes (16 contiguous
@@ -172,7 +172,11 @@ class DeviceState:
         keep = []
         for p in passes:
             umats = []
-            d = encode_pass_tc(p, self.n, umats)
+            try:
+                d = encode_pass_tc(p, self.n, umats)
+            except TcPlanError:
+                self._run_passes([p])     # more rounds than a descriptor holds: the CUDA-core pass
+                continue
             host = np.concatenate(umats).view(np.int16)      # FP16 bit patterns
             h = torch.from_numpy(host).pin_memory()
             dev = h.to(self.device, non_blocking=True)
@@ -180,7 +184,7 @@ class DeviceState:
             self._call('dm_apply_pass_tc', self.ptr, self.n, ctypes.byref(d), ctypes.c_void_p(dev.data_ptr()),
                        ctypes.c_size_t(host.size), sp, self.stream, keep=(d, dev))
             keep.append((h, dev, d))
-        self.passes_run += len(passes)
+        self.passes_run += len(keep)
         self._keep = keep
         if int(self.status.item()) != 0:
             raise BasicAerError('a tensor-core pass abandoned a bounded wait (status %d)' % int(self.status.item()))

@@ -344,6 +344,10 @@ def encode_pass(p, mats, dtype_np, round_width=None, n=None):
 
 TC_AXES = 7   # resident axes of a tensor-core pass (tiles of 4**7 FP32 coefficients)
 
+
+class TcPlanError(RuntimeError):
+    """A pass that does not fit a tensor-core descriptor (more rounds than DM_MAX_ROUNDS)."""
+
 # digits (d0, d1, d2) of the 64 round indices j = d0 + 4 d1 + 16 d2
 _J = np.arange(64)
 _DIG = np.stack([_J & 3, (_J >> 2) & 3, _J >> 4])
@@ -705,7 +709,7 @@ def encode_pass_tc(p, n, umats):
     """DmTcPass for dm_apply_pass_tc; appends the rounds' FP16 matrix images (uint16) to ``umats``."""
     pp, layouts, mats = plan_tc_pass(p, n)
     if len(layouts) > N.DM_MAX_ROUNDS:
-        raise RuntimeError('pass needs %d rounds (> %d)' % (len(layouts), N.DM_MAX_ROUNDS))
+        raise TcPlanError('pass needs %d rounds (> %d)' % (len(layouts), N.DM_MAX_ROUNDS))
     conv, rounds = tc_tables(layouts)
     dp = N.DmTcPass()
     for r, q in enumerate(pp.axes):

@@ -148,3 +148,18 @@ def test_rotation_error_defaults_leak_like_the_reference():
     r = dmg.execute(qc, backend).result()['results'][0]['data']['coeffmatrix']
     assert abs(r[3] - (-0.25)) < 1e-12       # Z coefficient: ry contracted by 0.5
     DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
+
+
+def test_tensor_core_round_overflow_falls_back_to_the_cuda_core_pass():
+    """A pass with more rounds than a tensor-core descriptor holds runs on the CUDA cores, same result."""
+    n = 7
+    qc = dmg.QuantumCircuit(n, n)
+    for i in range(120):                   # a CX chain around all 7 qubits, u3 in between
+        qc.u3(0.1 * i, 0.2, 0.3, i % n)
+        qc.cx(i % n, (i + 1) % n)
+    qc.measure(list(range(n)), list(range(n)), basis='Ensemble', add_param='Z')
+    opts = dmg.noise_options(depolarisation=1e-3, decoherence=0.995, decay=0.998)
+    opts['compute_densitymatrix'] = False
+    ref = _oracle(qc.to_experiment(), opts)
+    got, _ = run_gpu(qc.to_experiment(), opts, precision='single')
+    _assert_close(got, ref, n, 2e-5)

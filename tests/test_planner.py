@@ -318,3 +318,18 @@ def test_xy_unital_flag_marks_exactly_the_maps_without_i_in_x_and_y():
         m = mats[i].reshape(16)
         xy = m[4] == 0 and m[8] == 0
         assert bool(dp.ops[i].flags & N.DM_MAP1_XY_UNITAL) == xy
+
+
+def test_too_many_tensor_core_rounds_raise_a_plan_error():
+    """A pass whose rounds overflow the descriptor raises TcPlanError (the engine runs it on the CUDA cores)."""
+    n = 7
+    coef = np.array(P.cx_coefficients([0.99, 0.01])[0])
+    ops = []
+    for i in range(120):           # a CX chain around all 7 qubits: two CX per 3-axis round at most
+        ops.append(P.Op('cx', (i % 7, (i + 1) % 7), coef, False))
+    passes = P.plan_passes(ops, n, 7, 2)
+    counts = [len(P.plan_tc_pass(p, n)[1]) for p in passes]
+    assert max(counts) > N.DM_MAX_ROUNDS
+    with pytest.raises(P.TcPlanError):
+        for p in passes:
+            P.encode_pass_tc(p, n, [])
