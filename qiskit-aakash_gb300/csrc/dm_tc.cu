@@ -21,14 +21,15 @@
 // 128-bit stores.  Every wait on an mbarrier is bounded: a wait that gives
 // up records an error in *status and the kernel drains and returns.
 //
-// Two CTAs of 128 threads share an SM, so one CTA's tile load, barriers
+// Two CTAs of 256 threads share an SM, so one CTA's tile load, barriers
 // and MMA waits overlap the other's work.  Shared memory per CTA (dynamic,
 // 88 KB): AH / AL 32 KB each (round operand h / l, K-major core-matrix FP16
 // layout, 256 rows x 64; together they also hold the natural FP32 tile that
 // cp.async streams in and the last round writes out), B 24 KB (2**11 Uh and
 // Ul stacked as one 128-row operand, then Uh).  The h operand is read once
 // per round for both of its terms (N = 128 into two 64-column accumulators
-// that the epilogue adds); each thread owns one row of each 128-row M block.
+// that the epilogue adds); warps 0-3 own the rows of M block 0 and warps 4-7
+// those of M block 1, one row per thread (TMEM lane quadrant = warp % 4).
 #include <cuda_fp16.h>
 
 #include <mutex>
@@ -40,8 +41,9 @@ namespace dmg {
 
 namespace tc {
 
-constexpr int kThreads = 128;                  // two CTAs per SM
+constexpr int kThreads = 256;                  // two CTAs per SM
 constexpr int kCtasPerSm = 2;
+constexpr int kBlocksPerThread = 256 / kThreads;   // M = 128 blocks in one thread's epilogue
 constexpr int kAxes = 7;                       // resident axes per tile
 constexpr int kTile = 1 << (2 * kAxes);        // 16384 coefficients
 constexpr int kGroups = kTile / 64;            // 256 rows per round
@@ -264,7 +266,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
         // bits, so each 16-byte chunk store of an 8-lane phase covers the 8 rows of one core
         // matrix: all 32 banks.  Every thread reads all of its values before any is written.
         {
-            constexpr int kItems = kGroups * 8 / kThreads;   // 16
+            constexpr int kItems = kGroups * 8 / kThreads;   // 8
             const float *nat = reinterpret_cast<const float *>(AH);
             const float up = p.up;      // 2**n: the tile in units of 2**-n
             float x[kItems][8];
@@ -352,15 +354,16 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
             // B is free: fetch the next round's U (or round 0's, for the next tile)
             load_u(r + 1 < p.nrounds ? r + 1 : 0);
             // ---- epilogue: D -> next operand (h / l), or the natural tile after the last round ----
-            // thread tid holds row tid of M block 0 (TMEM columns 0-127) and of M block 1 (128-255)
+            // the thread holds row tid % 128 of M block tid / 128 (TMEM columns 0-127 / 128-255)
             const Round &R = p.rounds[r];
             uint32_t tk[3][4];
             digit_tables(R.kc, tk);
             const bool last = r + 1 == p.nrounds;
 #pragma unroll 1
-            for (int mb = 0; mb < 2; ++mb) {
+            for (int i = 0; i < kBlocksPerThread; ++i) {
+                const int mb = kBlocksPerThread == 1 ? (warp >> 2) : i;
                 float v[64];
-                const uint32_t ta = tmem + (uint32_t(32 * warp) << 16) + uint32_t(mb * 128);
+                const uint32_t ta = tmem + (uint32_t(32 * (warp & 3)) << 16) + uint32_t(mb * 128);
                 tmem_ld64(ta, v);
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {   // + the h Ul^T half, 16 columns at a time
@@ -369,7 +372,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
 #pragma unroll
                     for (int j = 0; j < 16; ++j) v[16 * c + j] += w[j];
                 }
-                const uint32_t base = xor_bits<8>(uint32_t(tid + 128 * mb), R.rowc);
+                const uint32_t base = xor_bits<8>(uint32_t((tid & 127) + 128 * mb), R.rowc);
                 if (!last) {
 #pragma unroll
                     for (int j = 0; j < 64; ++j) v[j] *= kLoUnscale;
@@ -493,7 +496,7 @@ extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, 
     });
     if (attr_err != cudaSuccess) return DM_ERR_CUDA;
     const int64_t ntiles = int64_t(1) << (2 * p.m);
-    // 88 KB of shared memory, <= 256 registers and 256 TMEM columns per CTA: two CTAs per SM
+    // 88 KB of shared memory, <= 128 registers per thread and 256 TMEM columns per CTA: two CTAs per SM
     int64_t grid = int64_t(sm_count()) * tc::kCtasPerSm;
     if (grid > ntiles) grid = ntiles;
     tc::pass_tc_kernel<<<int(grid), tc::kThreads, tc::kSmemBytes, as_stream(stream)>>>(

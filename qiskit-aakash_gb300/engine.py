@@ -20,6 +20,9 @@ from .program import TC_AXES, Op, TcPlanError, cx_coefficients, encode_pass, enc
 # coefficients, one 128-byte line in FP64) are always resident.
 DEFAULT_TILE_AXES = {'double': 6, 'single': 7}
 DEFAULT_LOW_AXES = 2
+# Queued operations at which the passes they already fix are planned and
+# launched (the rest of the queue waits for later operations or a read-out).
+STREAM_OPS = 4096
 
 # Copy-out of large states: 32 Mi coefficients (256 MB FP64) per chunk, two
 # device and two pinned host buffers per device, host copies in 16 MB slices.
@@ -80,6 +83,7 @@ class DeviceState:
         self.kmax = min(tile_axes or DEFAULT_TILE_AXES[precision], N.DM_MAX_TILE_AXES)
         self.low = low_axes
         self.pending = []
+        self._stream_at = STREAM_OPS
         self.passes_run = 0
         self.h2d_bytes = 0
         self.d2h_bytes = 0
@@ -128,6 +132,7 @@ class DeviceState:
     def init_product(self, vectors, scale):
         v = np.ascontiguousarray(np.asarray(vectors, dtype=np.float64).reshape(self.n, 4))
         self.pending = []
+        self._stream_at = STREAM_OPS
         self._call('dm_init_product', self.ptr, self.n, self.dtype,
                    v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), float(scale), self.stream, keep=(v,))
 
@@ -142,24 +147,45 @@ class DeviceState:
 
     # -- queued operations ---------------------------------------------------
     def map1(self, q, m, tag=None):
-        self.pending.append(Op('map1', (q,), np.asarray(m, dtype=np.float64)))
+        self._queue(Op('map1', (q,), np.asarray(m, dtype=np.float64)))
 
     def cx(self, ctl, tgt, tsp):
         coef, ideal = cx_coefficients(tsp)
-        self.pending.append(Op('cx', (ctl, tgt), np.array(coef), ideal))
+        self._queue(Op('cx', (ctl, tgt), np.array(coef), ideal))
 
     def diag2(self, qa, qb, d):
-        self.pending.append(Op('diag2', (qa, qb), np.asarray(d, dtype=np.float64)))
+        self._queue(Op('diag2', (qa, qb), np.asarray(d, dtype=np.float64)))
+
+    def _queue(self, op):
+        self.pending.append(op)
+        if self.fusion and len(self.pending) >= self._stream_at:
+            self._flush_closed()
+
+    def _flush_closed(self):
+        """Launch the passes that the queued ops already fix; later ops cannot change them.
+
+        The device starts on the first passes while the host is still
+        producing the rest of the circuit's operations.
+        """
+        passes, self.pending = plan_passes(self.pending, self.n, self.kmax, self.low, partial=True)
+        if passes:
+            self._launch(passes)
+        self._stream_at = len(self.pending) + STREAM_OPS
 
     def flush(self):
         """Run every queued operation (fused passes, or one sweep per operation)."""
+        self._stream_at = STREAM_OPS
         if not self.pending:
             return
         ops, self.pending = self.pending, []
         if not self.fusion:
             self._run_unfused(ops)
             return
-        passes = plan_passes(ops, self.n, self.kmax, self.low)
+        self._launch(plan_passes(ops, self.n, self.kmax, self.low))
+        if self.tensor_cores and int(self.status.item()) != 0:
+            raise BasicAerError('a tensor-core pass abandoned a bounded wait (status %d)' % int(self.status.item()))
+
+    def _launch(self, passes):
         if self.tensor_cores:
             self._run_passes_tc(passes)
         else:
@@ -186,8 +212,6 @@ class DeviceState:
             keep.append((h, dev, d))
         self.passes_run += len(keep)
         self._keep = keep
-        if int(self.status.item()) != 0:
-            raise BasicAerError('a tensor-core pass abandoned a bounded wait (status %d)' % int(self.status.item()))
 
     def _run_passes(self, passes):
         torch = _torch()

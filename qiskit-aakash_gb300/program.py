@@ -172,13 +172,18 @@ class Pass:
         return self.axes.index(q)
 
 
-def plan_passes(ops, n, kmax, low):
+def plan_passes(ops, n, kmax, low, partial=False):
     """Group ``ops`` (program order) into fused passes.
 
     Returns a list of Pass; each pass's op list preserves program order
     among the ops it holds, and per axis the ops of successive passes are
     consecutive runs of that axis's ops, so applying the passes in order
     equals applying ``ops`` in order.
+
+    With ``partial`` the ops are a prefix of a longer stream: only the
+    passes whose scan closed before the end of ``ops`` are returned (they
+    are exactly the passes the whole stream would give), together with the
+    ops they left, in order: ``(passes, rest)``.
     """
     kmax = min(kmax, n)
     low = min(low, kmax)
@@ -190,6 +195,7 @@ def plan_passes(ops, n, kmax, low):
         resident = set(base)
         full = len(resident) >= kmax
         blocked = set()
+        closed = False
         taken_idx = []
         body = []          # list of Op (possibly composed)
         last_on_axis = {}  # axis -> index into body of the last op touching it
@@ -202,6 +208,7 @@ def plan_passes(ops, n, kmax, low):
                 # Once the pass is full and every resident axis is held back,
                 # no later operation can be taken.
                 if (full and blocked.issuperset(resident)) or len(blocked) >= n:
+                    closed = True
                     break
                 continue
             grow = [a for a in axes if a not in resident]
@@ -223,11 +230,13 @@ def plan_passes(ops, n, kmax, low):
                 full = True
         if not taken_idx:
             raise RuntimeError('planner made no progress')
+        if partial and not closed:
+            return passes, pending     # later ops could still join this pass
         keep = set(taken_idx)
         pending = [op for i, op in enumerate(pending) if i not in keep]
         axes = sorted(resident, reverse=True)
         passes.append(Pass(axes, body))
-    return passes
+    return (passes, []) if partial else passes
 
 
 def plan_rounds(p, width, pad='low'):

@@ -165,6 +165,45 @@ def test_brick_layers_fuse_into_few_passes():
     assert len(passes) / 6 <= 4.0
 
 
+def _same_passes(a, b):
+    assert len(a) == len(b)
+    for p, q in zip(a, b):
+        assert list(p.axes) == list(q.axes)
+        assert len(p.ops) == len(q.ops)
+        for x, y in zip(p.ops, q.ops):
+            assert x.kind == y.kind and tuple(x.axes) == tuple(y.axes)
+            np.testing.assert_array_equal(np.asarray(x.data), np.asarray(y.data))
+
+
+@pytest.mark.parametrize('n,kmax,low,chunk', [(6, 4, 2, 7), (9, 6, 2, 40), (12, 7, 2, 150), (16, 7, 2, 500)])
+def test_streamed_planning_gives_the_passes_of_the_whole_stream(n, kmax, low, chunk):
+    """Planning a growing prefix and launching only its closed passes (the engine's
+    streaming flush) yields exactly the passes of planning the whole op list at once."""
+    rng = np.random.default_rng(7 * n + chunk)
+    ops = []
+    noise = P.noise_ptm(0.995, 1.0, 0.998)
+    for L in range(8):
+        for q in range(n):
+            ops.append(P.Op('map1', (q,), rng.normal(size=(4, 4))))
+            ops.append(P.Op('map1', (q,), noise))
+        for a in range(L % 2, n - 1, 2):
+            coef, ideal = P.cx_coefficients([1.0, 0.0])
+            ops.append(P.Op('cx', (a, a + 1), np.array(coef), ideal))
+            for q in range(n):
+                ops.append(P.Op('map1', (q,), noise))
+    ops += random_ops(rng, n, 80)
+    whole = P.plan_passes(ops, n, kmax, low)
+    streamed, pending, launched_early = [], [], 0
+    for i in range(0, len(ops), chunk):
+        pending = pending + ops[i:i + chunk]
+        done, pending = P.plan_passes(pending, n, kmax, low, partial=True)
+        launched_early += len(done)
+        streamed += done
+    streamed += P.plan_passes(pending, n, kmax, low)
+    _same_passes(streamed, whole)
+    assert launched_early > len(whole) // 2     # most passes start before the stream ends
+
+
 @pytest.mark.parametrize('width', [2, 3])
 @pytest.mark.parametrize('n,kmax,low', [(5, 4, 2), (7, 6, 2), (8, 7, 2), (9, 7, 3)])
 def test_register_rounds_equal_program_order(n, kmax, low, width):
