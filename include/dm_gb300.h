@@ -214,6 +214,34 @@ int dm_batch_run(int dtype, void *states_dev, size_t states_count, double *probs
                  const dm_batch_instance *insts_dev, int ninst, const dm_batch_pass *passes_host,
                  const dm_batch_pass *passes_dev, int npasses, int *counter_dev, int *status_dev, void *stream);
 
+/* One pass of a batched program on the tensor cores: 7 resident axes, every
+ * round a 64x64 transfer matrix composed on the device from the instance's
+ * own coefficients.  ops.k = 7; ops.round_axes[r][0..2] are round r's local
+ * axes in K-digit order (they must equal tables.rounds[r].digits) and the
+ * digit positions in the op flags refer to that order; tables holds the
+ * conversion and epilogue tables (tables.axes and rounds[].umoff are not
+ * read). */
+typedef struct dm_batch_tc_pass {
+    dm_batch_pass ops;
+    dm_tc_pass tables;
+} dm_batch_tc_pass;
+
+/* Device scratch dm_batch_run_tc needs for the round matrices it composes
+ * (DM_MAX_ROUNDS FP16 image sets per CTA). */
+size_t dm_batch_tc_scratch_bytes(void);
+
+/* dm_batch_run for FP32 instances of 7..12 qubits with every pass on the
+ * tensor cores (the dm_apply_pass_tc kernel): at the start of each pass a
+ * CTA composes the pass's round matrices from the instance's coefficient
+ * block (FP32, the ops applied to the 64 unit vectors) into its slice of
+ * scratch_dev as the 3-way FP16 split images, then streams the instance's
+ * tiles.  status_dev is set to 1 if a bounded tensor-core wait gives up. */
+int dm_batch_run_tc(float *states_dev, size_t states_count, double *probs_dev, size_t probs_count,
+                    const float *mats_dev, size_t mats_count, const dm_batch_instance *insts_host,
+                    const dm_batch_instance *insts_dev, int ninst, const dm_batch_tc_pass *passes_host,
+                    const dm_batch_tc_pass *passes_dev, int npasses, int *counter_dev, void *scratch_dev,
+                    size_t scratch_bytes, int *status_dev, void *stream);
+
 /* Parametric batched programs: every instance runs the same circuit
  * template (one plan) and differs only in its noise parameters.  Each
  * operation of the template is a recipe; a slot of a pass composes a chain

@@ -115,6 +115,10 @@ class DmBatchPass(ctypes.Structure):
                 ('ops', DmOp * DM_MAX_PASS_OPS)]
 
 
+class DmBatchTcPass(ctypes.Structure):
+    _fields_ = [('ops', DmBatchPass), ('tables', DmTcPass)]
+
+
 class DmBatchInstance(ctypes.Structure):
     _fields_ = [('n', ctypes.c_int32), ('npasses', ctypes.c_int32), ('pass_begin', ctypes.c_int32),
                 ('pad', ctypes.c_int32), ('state_off', ctypes.c_int64), ('prob_off', ctypes.c_int64),
@@ -174,6 +178,9 @@ SIGNATURES = {
     'dm_apply_pass_tc': (_i, [_vp, _i, ctypes.POINTER(DmTcPass), _vp, _sz, _vp, _vp]),
     'dm_batch_run': (_i, [_i, _vp, _sz, _vp, _sz, _vp, _sz, ctypes.POINTER(DmBatchInstance), _vp, _i,
                           ctypes.POINTER(DmBatchPass), _vp, _i, _vp, _vp, _vp]),
+    'dm_batch_tc_scratch_bytes': (_sz, []),
+    'dm_batch_run_tc': (_i, [_vp, _sz, _vp, _sz, _vp, _sz, ctypes.POINTER(DmBatchInstance), _vp, _i,
+                             ctypes.POINTER(DmBatchTcPass), _vp, _i, _vp, _vp, _sz, _vp, _vp]),
     'dm_batch_run_params': (_i, [_i, ctypes.POINTER(DmParamProgram), ctypes.POINTER(DmParamProgram), _vp, _i, _i,
                                  _vp, _sz, _vp, _sz, _vp, _vp]),
     'dm_mlp_gemm_run': (_i, [ctypes.POINTER(DmMlpGemm), _vp, _vp]),

@@ -114,64 +114,74 @@ def _signature(ops):
 
 
 class _Plan:
-    """A pass / round plan shared by instances of one structure."""
+    """A pass / round plan shared by instances of one structure (CUDA-core register rounds)."""
+
+    kind = 'cuda'
 
     def __init__(self, ops, n, kmax, dtype):
         self.n = n
         width = N.DM_ROUND_AXES[N.DM_F64 if dtype == np.float64 else N.DM_F32]
         self.passes = []     # dm_batch_pass
-        self.slots = []      # (kind, src, ideal) per coefficient block entry, in mats order
+        self.slots = []      # (kind, src, ideal, flags) per coefficient block entry, in mats order
         self.mats_len = 0
         for p in P.plan_passes(ops, n, kmax, 2):
             pp = p if len(p.axes) >= width else P.pad_pass(p, n, width)
             rounds = P.plan_rounds(pp, width)
             bp = N.DmBatchPass()
-            bp.k = len(pp.axes)
-            for r, q in enumerate(pp.axes):
-                bp.axes[r] = q
-            bp.nrounds = len(rounds)
-            if bp.nrounds > N.DM_MAX_ROUNDS:
-                raise BasicAerError('pass needs too many rounds')
-            o = 0
-            for ri, (axes, rops) in enumerate(rounds):
-                for i, a in enumerate(axes):
-                    bp.round_axes[ri][i] = a
-                for i in range(len(axes), 4):
-                    bp.round_axes[ri][i] = -1
-                for op in rops:
-                    d = bp.ops[o]
-                    d.a = op.axes[0]
-                    d.moff = self.mats_len
-                    flags = axes.index(op.axes[0]) << 8
-                    if op.kind == 'map1':
-                        d.kind = N.DM_OP_MAP1
-                        d.b = 0
-                        m = np.asarray(op.data).reshape(16)
-                        row0 = m[0] == 1.0 and not m[1:4].any()
-                        flags |= N.DM_MAP1_ROW0_IDENTITY if row0 else 0
-                        flags |= N.DM_MAP1_XY_UNITAL if (m[4] == 0.0 and m[8] == 0.0) else 0
-                        size = 16
-                    elif op.kind == 'cx':
-                        d.kind = N.DM_OP_CX
-                        d.b = op.axes[1]
-                        flags |= (N.DM_CX_IDEAL if op.ideal else 0) | (axes.index(op.axes[1]) << 12)
-                        size = 5
-                    elif op.kind == 'diag2':
-                        d.kind = N.DM_OP_DIAG2
-                        d.b = op.axes[1]
-                        flags |= axes.index(op.axes[1]) << 12
-                        size = 16
-                    else:
-                        raise BasicAerError('batched programs hold 4x4 maps, CX and diagonal pair maps only')
-                    d.flags = flags
-                    self.slots.append((op.kind, list(op.src), op.ideal,
-                                       (flags & (N.DM_MAP1_ROW0_IDENTITY | N.DM_MAP1_XY_UNITAL))
-                                       if op.kind == 'map1' else 0))
-                    self.mats_len += size
-                    o += 1
-                bp.round_end[ri] = o
-            bp.nops = o
+            self._fill(bp, pp, rounds, [axes for axes, _ in rounds])
             self.passes.append(bp)
+
+    def _fill(self, bp, pp, rounds, digit_orders):
+        """Pass header, round axes (in ``digit_orders``) and ops of one dm_batch_pass."""
+        bp.k = len(pp.axes)
+        for r, q in enumerate(pp.axes):
+            bp.axes[r] = q
+        bp.nrounds = len(rounds)
+        if bp.nrounds > N.DM_MAX_ROUNDS:
+            raise P.TcPlanError('pass needs %d rounds (> %d)' % (len(rounds), N.DM_MAX_ROUNDS))
+        o = 0
+        for ri, ((_, rops), axes) in enumerate(zip(rounds, digit_orders)):
+            axes = list(axes)
+            for i, a in enumerate(axes):
+                bp.round_axes[ri][i] = a
+            for i in range(len(axes), 4):
+                bp.round_axes[ri][i] = -1
+            for op in rops:
+                d = bp.ops[o]
+                d.a = op.axes[0]
+                d.moff = self.mats_len
+                flags = axes.index(op.axes[0]) << 8
+                if op.kind == 'map1':
+                    d.kind = N.DM_OP_MAP1
+                    d.b = 0
+                    m = np.asarray(op.data).reshape(16)
+                    row0 = m[0] == 1.0 and not m[1:4].any()
+                    flags |= N.DM_MAP1_ROW0_IDENTITY if row0 else 0
+                    flags |= N.DM_MAP1_XY_UNITAL if (m[4] == 0.0 and m[8] == 0.0) else 0
+                    size = 16
+                elif op.kind == 'cx':
+                    d.kind = N.DM_OP_CX
+                    d.b = op.axes[1]
+                    flags |= (N.DM_CX_IDEAL if op.ideal else 0) | (axes.index(op.axes[1]) << 12)
+                    size = 5
+                elif op.kind == 'diag2':
+                    d.kind = N.DM_OP_DIAG2
+                    d.b = op.axes[1]
+                    flags |= axes.index(op.axes[1]) << 12
+                    size = 16
+                else:
+                    raise BasicAerError('batched programs hold 4x4 maps, CX and diagonal pair maps only')
+                d.flags = flags
+                self.slots.append((op.kind, list(op.src), op.ideal,
+                                   (flags & (N.DM_MAP1_ROW0_IDENTITY | N.DM_MAP1_XY_UNITAL))
+                                   if op.kind == 'map1' else 0))
+                self.mats_len += size
+                o += 1
+            bp.round_end[ri] = o
+        bp.nops = o
+
+    def table_bytes(self):
+        return bytes((N.DmBatchPass * len(self.passes))(*self.passes))
 
     def coefficients(self, ops, dtype):
         """The coefficient block of one instance (its own op matrices, composed along the plan)."""
@@ -196,6 +206,65 @@ class _Plan:
                 out[pos:pos + 16] = np.asarray(ops[src[0]].data).reshape(16)
                 pos += 16
         return out.astype(dtype)
+
+
+class _TcPlan(_Plan):
+    """A tensor-core plan shared by instances of one structure: passes of 7
+    resident axes, rounds of 3 axes in the digit order their layouts chose;
+    the device composes each round's 64x64 matrix from the instance's block."""
+
+    kind = 'tc'
+
+    def __init__(self, ops, n):
+        self.n = n
+        self.passes = []     # dm_batch_tc_pass
+        self.slots = []
+        self.mats_len = 0
+        for p in P.plan_passes(ops, n, P.TC_AXES, 2):
+            pp = P.pad_pass(p, n)
+            rounds = P.plan_rounds(pp, 3, pad='neighbors')
+            if len(rounds) > N.DM_MAX_ROUNDS:
+                raise P.TcPlanError('pass needs %d rounds (> %d)' % (len(rounds), N.DM_MAX_ROUNDS))
+            layouts = P._choose_layouts([axes for axes, _ in rounds])
+            conv, rtables = P.tc_tables(layouts)
+            bp = N.DmBatchTcPass()
+            self._fill(bp.ops, pp, rounds, [L.digits for L in layouts])
+            t = bp.tables
+            for r, q in enumerate(pp.axes):
+                t.axes[r] = q
+            t.nrounds = len(layouts)
+            t.vec0 = conv['vec0']
+            for i in range(8):
+                t.natrow[i] = conv['natrow'][i]
+            for i in range(6):
+                t.natk[i] = conv['natk'][i]
+            for r, rt in enumerate(rtables):
+                for i in range(3):
+                    t.rounds[r].digits[i] = rt['digits'][i]
+                t.rounds[r].vec = rt['vec']
+                t.rounds[r].umoff = 0
+                for i in range(8):
+                    t.rounds[r].rowc[i] = rt['rowc'][i]
+                for i in range(6):
+                    t.rounds[r].kc[i] = rt['kc'][i]
+            self.passes.append(bp)
+
+    def table_bytes(self):
+        return bytes((N.DmBatchTcPass * len(self.passes))(*self.passes))
+
+
+TC = 'tc'    # resident-axes choice of a qubit count whose instances run on the tensor cores
+
+
+def _make_plan(ops, n, k, np_dtype):
+    if k == TC:
+        if np_dtype != np.float32 or n < P.TC_AXES:
+            raise BasicAerError('tensor-core batched passes need FP32 instances of >= %d qubits' % P.TC_AXES)
+        try:
+            return _TcPlan(ops, n)
+        except P.TcPlanError:       # more rounds than a pass table holds: the CUDA-core plan
+            return _Plan(ops, n, P.TC_AXES, np_dtype)
+    return _Plan(ops, n, min(k, n), np_dtype)
 
 
 def sweep_specs(count, seed=0, n_range=(6, 12), depth_range=(10, 50), noise_range=(1e-4, 1e-2)):
@@ -243,11 +312,10 @@ def compile_group(specs, variants):
             sig = _signature(rec.ops)
             if sig not in by_sig:
                 by_sig[sig] = len(plans)
-                plans.append(_Plan(rec.ops, spec['n'], min(k, spec['n']), np_dtype))
+                plans.append(_make_plan(rec.ops, spec['n'], k, np_dtype))
             pi = by_sig[sig]
             insts.append((pi, plans[pi].coefficients(rec.ops, np.float64), rec.readouts[0][3]))
-        out.append(([(bytes((N.DmBatchPass * len(pl.passes))(*pl.passes)), len(pl.passes), pl.mats_len)
-                     for pl in plans], insts))
+        out.append(([(pl.table_bytes(), len(pl.passes), pl.mats_len, pl.kind) for pl in plans], insts))
     return out
 
 
@@ -327,6 +395,10 @@ def compile_sweep(specs, variants, workers=None, kmax=None):
                 raise BasicAerError('batched instances hold %d..%d qubits' % (lo, MAX_QUBITS))
     for per_n in kmax.values():
         for n, k in per_n.items():
+            if k == TC:
+                if n < P.TC_AXES:
+                    raise BasicAerError('tensor-core batched passes need >= %d qubits' % P.TC_AXES)
+                continue
             if k < min(4, n):
                 # the two lowest qubits are always resident: a CX elsewhere needs two more axes
                 raise BasicAerError('a pass of %d-qubit instances needs at least %d resident axes' % (n, min(4, n)))
@@ -363,13 +435,48 @@ def compile_sweep(specs, variants, workers=None, kmax=None):
     return tables
 
 
+class _Part:
+    """The instances of a batch that one kernel runs: their table entries, passes and coefficients."""
+
+    def __init__(self, pass_type, np_dtype):
+        self.pass_type = pass_type
+        self.np_dtype = np_dtype
+        self.insts, self.blobs, self.blocks = [], [], []
+        self.pass_begin = {}
+        self.npasses = 0
+        self.mats_off = 0
+
+    def add(self, pi, raw, npasses, mats_len, block, I):
+        if pi not in self.pass_begin:
+            self.pass_begin[pi] = self.npasses
+            self.blobs.append(raw)
+            self.npasses += npasses
+        I.npasses = npasses
+        I.pass_begin = self.pass_begin[pi]
+        I.mats_off, I.mats_len = self.mats_off, mats_len
+        self.mats_off += mats_len
+        self.insts.append(I)
+        self.blocks.append(block)
+
+    def finish(self):
+        self.ninst = len(self.insts)
+        self.insts = (N.DmBatchInstance * self.ninst)(*self.insts)
+        blob = b''.join(self.blobs)
+        self.passes = (self.pass_type * self.npasses).from_buffer_copy(blob) if blob else (self.pass_type * 0)()
+        self.mats = (np.concatenate(self.blocks) if self.blocks else np.zeros(0)).astype(self.np_dtype)
+        del self.blobs, self.blocks
+
+
 class BatchTables:
     """Host tables of a batch: instance table, shared pass plans and coefficient blocks.
 
     Instances are laid out largest first (4**n x depth), the order the
     device's work counter hands them out; ``index[i]`` is the slot of input
-    instance i.  States, outcome probabilities and coefficient blocks are
-    packed back to back in slot order.  Built by ``compile_sweep``; the
+    instance i.  States and outcome probabilities are packed back to back in
+    slot order.  Instances whose plan runs on the CUDA-core rounds form the
+    main part (``insts``, ``passes``, ``mats``, ``ninst``, ``npasses``);
+    those planned for the tensor cores form ``tc`` (same fields), each part
+    with its own coefficient array.  Built by ``compile_sweep``; the
     constructor with ``specs`` only compiles one variant.
     """
 
@@ -385,37 +492,34 @@ class BatchTables:
         self.np_dtype = np.float32 if precision == 'single' else np.float64
         self.specs = specs
         order = sorted(range(len(specs)), key=lambda i: -(4 ** specs[i]['n'] * specs[i]['depth']))
-        pass_begin, passes, npass_total = {}, [], 0
-        insts, mats = [], []
-        state_off = prob_off = mats_off = 0
-        self.index = np.empty(len(specs), dtype=np.int64)
-        for slot, i in enumerate(order):
+        main, tc = _Part(N.DmBatchPass, self.np_dtype), _Part(N.DmBatchTcPass, self.np_dtype)
+        state_off = prob_off = 0
+        self.index = []
+        for i in order:
             pi, block, err = per_instance[i]
-            raw, npasses, mats_len = plans[pi]
-            if pi not in pass_begin:
-                pass_begin[pi] = npass_total
-                passes.append(raw)
-                npass_total += npasses
+            raw, npasses, mats_len = plans[pi][:3]
+            kind = plans[pi][3] if len(plans[pi]) > 3 else 'cuda'
             n = specs[i]['n']
             I = N.DmBatchInstance()
             I.n = n
-            I.npasses = npasses
-            I.pass_begin = pass_begin[pi]
-            I.state_off, I.prob_off, I.mats_off, I.mats_len = state_off, prob_off, mats_off, mats_len
+            I.state_off, I.prob_off = state_off, prob_off
             I.meas_err = err
-            insts.append(I)
-            mats.append(block)
+            part = tc if kind == 'tc' else main
+            self.index.append((part, len(part.insts)))
+            part.add(pi, raw, npasses, mats_len, block, I)
             state_off += 4 ** n
             prob_off += 2 ** n
-            mats_off += mats_len
-            self.index[i] = slot
-        self.nplans = len(pass_begin)
-        self.insts = (N.DmBatchInstance * len(insts))(*insts)
-        blob = b''.join(passes)
-        self.npasses = len(blob) // ctypes.sizeof(N.DmBatchPass)
-        self.passes = (N.DmBatchPass * self.npasses).from_buffer_copy(blob) if blob else (N.DmBatchPass * 0)()
-        self.ninst = len(insts)
-        self.mats = np.concatenate(mats).astype(self.np_dtype)
+        main.finish()
+        tc.finish()
+        slots = [None] * len(specs)
+        for i, ref in zip(order, self.index):
+            slots[i] = ref
+        self.index = slots
+        self.nplans = len(main.pass_begin) + len(tc.pass_begin)
+        self.insts, self.passes, self.mats = main.insts, main.passes, main.mats
+        self.ninst, self.npasses = main.ninst, main.npasses
+        self.tc = tc
+        self.ninst_total = main.ninst + tc.ninst
         self.states_count = state_off
         self.probs_count = prob_off
         self.compile_seconds = compile_seconds
@@ -423,7 +527,16 @@ class BatchTables:
 
     def instance(self, i):
         """The instance table entry of input instance i."""
-        return self.insts[int(self.index[i])]
+        part, slot = self.index[i]
+        return part.insts[slot]
+
+    def all_instances(self):
+        """Every instance table entry (main part, then tensor-core part)."""
+        return list(self.insts) + list(self.tc.insts)
+
+    def swept_bytes(self, esize):
+        """State bytes read and written by all passes of all instances (one pass = one sweep of 4**n)."""
+        return sum(2 * 4 ** I.n * esize * I.npasses for I in self.all_instances())
 
     def split(self, probs):
         """Per-instance outcome probabilities (input order) from the packed output."""
@@ -441,7 +554,7 @@ class BatchProgram:
         import torch
         if not torch.cuda.is_available():
             raise BasicAerError('batched sweeps need a CUDA device')
-        N.lib()
+        L = N.lib()
         self.t = tables
         self.dtype = tables.dtype
         self.device = torch.device(device or 'cuda')
@@ -449,29 +562,48 @@ class BatchProgram:
 
         def to_dev(buf):
             raw = np.frombuffer(bytes(buf), dtype=np.uint8)
-            return torch.from_numpy(raw.copy()).to(dev)
+            return torch.from_numpy(raw.copy() if raw.size else np.zeros(16, dtype=np.uint8)).to(dev)
 
         self.insts_dev = to_dev(tables.insts)
         self.passes_dev = to_dev(tables.passes)
-        self.mats_dev = torch.from_numpy(tables.mats).to(dev)
+        self.mats_dev = torch.from_numpy(tables.mats if tables.mats.size else np.zeros(1, tables.mats.dtype)).to(dev)
+        tc = tables.tc
+        self.h2d_bytes = ctypes.sizeof(tables.insts) + ctypes.sizeof(tables.passes) + tables.mats.nbytes
+        if tc.ninst:
+            if self.dtype != N.DM_F32:
+                raise BasicAerError('tensor-core batched passes run FP32 states only')
+            self.tc_insts_dev = to_dev(tc.insts)
+            self.tc_passes_dev = to_dev(tc.passes)
+            self.tc_mats_dev = torch.from_numpy(tc.mats).to(dev)
+            self.tc_scratch = torch.empty(L.dm_batch_tc_scratch_bytes(), dtype=torch.uint8, device=dev)
+            self.h2d_bytes += ctypes.sizeof(tc.insts) + ctypes.sizeof(tc.passes) + tc.mats.nbytes
         tdt = torch.float32 if self.dtype == N.DM_F32 else torch.float64
         self.states = torch.empty(tables.states_count, dtype=tdt, device=dev)
         self.probs = torch.zeros(tables.probs_count, dtype=torch.float64, device=dev)
-        self.counter = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.counter = torch.zeros(2, dtype=torch.int32, device=dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
-        self.h2d_bytes = ctypes.sizeof(tables.insts) + ctypes.sizeof(tables.passes) + tables.mats.nbytes
         self.graph = None
 
     def launch(self, stream=None):
+        """The tensor-core part (the largest instances) first, then the CUDA-core part, on one stream."""
         import torch
         s = stream if stream is not None else torch.cuda.current_stream(self.device)
         vp = ctypes.c_void_p
         t = self.t
-        N.call('dm_batch_run', self.dtype, vp(self.states.data_ptr()), ctypes.c_size_t(t.states_count),
-               vp(self.probs.data_ptr()), ctypes.c_size_t(t.probs_count), vp(self.mats_dev.data_ptr()),
-               ctypes.c_size_t(t.mats.size), t.insts, vp(self.insts_dev.data_ptr()), t.ninst,
-               t.passes, vp(self.passes_dev.data_ptr()), t.npasses, vp(self.counter.data_ptr()),
-               vp(self.status.data_ptr()), vp(s.cuda_stream))
+        tc = t.tc
+        if tc.ninst:
+            N.call('dm_batch_run_tc', vp(self.states.data_ptr()), ctypes.c_size_t(t.states_count),
+                   vp(self.probs.data_ptr()), ctypes.c_size_t(t.probs_count), vp(self.tc_mats_dev.data_ptr()),
+                   ctypes.c_size_t(tc.mats.size), tc.insts, vp(self.tc_insts_dev.data_ptr()), tc.ninst,
+                   tc.passes, vp(self.tc_passes_dev.data_ptr()), tc.npasses, vp(self.counter.data_ptr() + 4),
+                   vp(self.tc_scratch.data_ptr()), ctypes.c_size_t(self.tc_scratch.numel()),
+                   vp(self.status.data_ptr()), vp(s.cuda_stream))
+        if t.ninst:
+            N.call('dm_batch_run', self.dtype, vp(self.states.data_ptr()), ctypes.c_size_t(t.states_count),
+                   vp(self.probs.data_ptr()), ctypes.c_size_t(t.probs_count), vp(self.mats_dev.data_ptr()),
+                   ctypes.c_size_t(t.mats.size), t.insts, vp(self.insts_dev.data_ptr()), t.ninst,
+                   t.passes, vp(self.passes_dev.data_ptr()), t.npasses, vp(self.counter.data_ptr()),
+                   vp(self.status.data_ptr()), vp(s.cuda_stream))
 
     def capture(self):
         """Capture one launch in a CUDA graph (after a first, uncaptured launch)."""
@@ -492,6 +624,8 @@ class BatchProgram:
 
     def results(self):
         """Outcome probabilities per instance (input order; qubit 0 is the most significant bit)."""
+        if int(self.status.item()) != 0:
+            raise BasicAerError('a tensor-core batched pass abandoned a bounded wait')
         return self.t.split(self.probs.cpu().numpy())
 
 
@@ -502,12 +636,13 @@ def autotune(specs, precision='single', candidates=None, sample=8, fill=None, re
     recorded once and planned for every candidate k; each plan runs as a
     batch of ``fill`` instances (the sample repeated; default one per SM, so
     the timing sees a full GPU's memory traffic) and the fastest k wins.
-    Returns ({n: k}, {(n, k): ms per launch}).
+    FP32 instances of >= 7 qubits also try ``TC`` (every pass on the
+    tensor cores).  Returns ({n: k}, {(n, k): ms per launch}).
     """
     import torch
     lo = N.DM_ROUND_AXES[N.DM_F32 if precision == 'single' else N.DM_F64]
     hi = 7 if precision == 'single' else 6
-    candidates = candidates or list(range(max(lo, hi - 2), hi + 1))
+    candidates = candidates or (([TC] if precision == 'single' else []) + list(range(hi, max(lo, hi - 2) - 1, -1)))
     if fill is None:
         fill = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     by_n = {}
@@ -515,7 +650,8 @@ def autotune(specs, precision='single', candidates=None, sample=8, fill=None, re
         by_n.setdefault(s['n'], []).append(s)
     choice, timings = {}, {}
     for n, group in sorted(by_n.items()):
-        ks = [k for k in candidates if lo <= k <= min(n, hi)]
+        ks = [k for k in candidates if (k == TC and n >= P.TC_AXES and precision == 'single') or
+              (k != TC and lo <= k <= min(n, hi))]
         if len(ks) <= 1:
             choice[n] = ks[0] if ks else min(n, hi)
             continue
@@ -525,7 +661,7 @@ def autotune(specs, precision='single', candidates=None, sample=8, fill=None, re
         per_spec = [compile_group([sp], [(precision, k) for k in ks]) for sp in smp]
         reps_specs = [smp[j % len(smp)] for j in range(max(fill, len(smp)))]
         best = None
-        for vi, k in sorted(enumerate(ks), key=lambda t: -t[1]):    # widest first: usually the fastest
+        for vi, k in enumerate(ks):    # in candidate order: the usually fastest first
             plans, per_instance = [], []
             for j in range(len(reps_specs)):
                 gplans, ginsts = per_spec[j % len(smp)][vi]

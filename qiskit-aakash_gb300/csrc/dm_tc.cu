@@ -34,7 +34,9 @@
 
 #include <mutex>
 
+#include "dm_batch.cuh"
 #include "dm_common.cuh"
+#include "dm_rounds.cuh"
 #include "dm_tcgen05.cuh"
 
 namespace dmg {
@@ -197,28 +199,26 @@ __device__ __forceinline__ void store_all(const float (&v)[64], int vec, uint32_
     }
 }
 
-__global__ void __launch_bounds__(kThreads, kCtasPerSm)
-    pass_tc_kernel(float *__restrict__ st, const __grid_constant__ Pass p, const uint16_t *__restrict__ umats,
-                   int *status) {
-    extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *AH = smem;             // operand h; with AL, the natural tile before and after the rounds
-    unsigned char *AL = AH + kABytes;
-    unsigned char *B = AL + kABytes;
-    __shared__ __align__(8) uint64_t mbar;
-    __shared__ uint32_t tmem_base_s;
-    __shared__ int64_t hi_off[kTile / 4 / kThreads];
-    __shared__ int abort_s;
+// Per-CTA tensor-core state shared by the single-state and the batched kernels.
+struct TcCta {
+    unsigned char *AH, *AL, *B;   // operand images h / l (the natural tile before and after the rounds), U
+    uint64_t *mbar;               // MMA completion barrier
+    int64_t *hi_off;              // kTile / 4 / kThreads chunk offsets of the current pass
+    int *abort_s;                 // set when a bounded wait gave up
+    uint32_t tmem;                // accumulator columns
+    uint32_t phase;               // mbarrier phase to wait for next
+    bool pending;                 // an MMA batch committed but not yet waited for
+};
 
+// mbarrier init and accumulator allocation (all threads).
+__device__ __forceinline__ void tc_setup(TcCta &c, uint32_t *tmem_base_s) {
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int64_t ntiles = int64_t(1) << (2 * p.m);
-    const int64_t off_tid = tile_offset(p, 4 * tid);
-    for (int i = tid; i < kTile / 4 / kThreads; i += kThreads) hi_off[i] = tile_offset(p, 4 * kThreads * i);
     if (tid == 0) {
-        abort_s = 0;
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+        *c.abort_s = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(c.mbar)));
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_base_s)),
                      "n"(kTmemCols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
@@ -226,9 +226,40 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t tmem = tmem_base_s;
-    uint32_t phase = 0;
-    bool pending = false;   // an MMA batch committed but not yet waited for
+    c.tmem = *tmem_base_s;
+    c.phase = 0;
+    c.pending = false;
+}
+
+// Drain what is in flight and release the accumulator (all threads).
+__device__ __forceinline__ void tc_teardown(TcCta &c) {
+    if (c.pending) mbar_wait(smem_u32(c.mbar), c.phase);   // drain before the accumulator is released
+    cp_async_wait_all();
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(c.tmem), "n"(kTmemCols));
+}
+
+// Streams tiles t0, t0 + dt, ... of one pass through the rounds (all threads
+// of the CTA); round r's images are at umats + p.rounds[r].umoff.  Returns
+// false when a bounded wait gave up (*status is then set).
+__device__ __forceinline__ bool tc_pass_tiles(float *__restrict__ st, const Pass &p,
+                                              const uint16_t *__restrict__ umats, int64_t t0, int64_t dt, TcCta &c,
+                                              int *status) {
+    unsigned char *AH = c.AH, *AL = c.AL, *B = c.B;
+    uint64_t &mbar = *c.mbar;
+    int64_t *hi_off = c.hi_off;
+    volatile int &abort_s = *c.abort_s;
+    const uint32_t tmem = c.tmem;
+    uint32_t phase = c.phase;
+    bool pending = c.pending;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int64_t ntiles = int64_t(1) << (2 * p.m);
+    const int64_t off_tid = tile_offset(p, 4 * tid);
+    __syncthreads();   // earlier readers of hi_off are done
+    for (int i = tid; i < kTile / 4 / kThreads; i += kThreads) hi_off[i] = tile_offset(p, 4 * kThreads * i);
+    __syncthreads();
 
     auto tile_base = [&](int64_t t) {
         int64_t base = 0;
@@ -255,7 +286,6 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
         cp_async_commit();
     };
 
-    const int64_t t0 = blockIdx.x, dt = gridDim.x;
     load_u(0);
     for (int64_t t = t0; t < ntiles; t += dt) {
         load_tile(t);
@@ -364,14 +394,9 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
                 const int mb = kBlocksPerThread == 1 ? (warp >> 2) : i;
                 float v[64];
                 const uint32_t ta = tmem + (uint32_t(32 * (warp & 3)) << 16) + uint32_t(mb * 128);
-                tmem_ld64(ta, v);
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {   // + the h Ul^T half, 16 columns at a time
-                    float w[16];
-                    tmem_ld16(ta + 64 + 16 * c, w);
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) v[16 * c + j] += w[j];
-                }
+                // D[:, 0:64] + D[:, 64:128], 32 columns of each at a time (one wait per half)
+                tcg::tmem_ld32_pair_add(ta, ta + 64, v);
+                tcg::tmem_ld32_pair_add(ta + 32, ta + 96, v + 32);
                 const uint32_t base = xor_bits<8>(uint32_t((tid & 127) + 128 * mb), R.rowc);
                 if (!last) {
 #pragma unroll
@@ -401,11 +426,132 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
         }
         __syncthreads();
     }
-    if (pending) mbar_wait(smem_u32(&mbar), phase);   // drain before the accumulator is released
-    cp_async_wait_all();
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    cp_async_wait_all();   // round 0's images prefetched for a tile that does not come
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(kTmemCols));
+    c.phase = phase;
+    c.pending = pending;
+    return !abort_s;
+}
+
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
+    pass_tc_kernel(float *__restrict__ st, const __grid_constant__ Pass p, const uint16_t *__restrict__ umats,
+                   int *status) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int64_t hi_off[kTile / 4 / kThreads];
+    __shared__ int abort_s;
+    TcCta c{smem, smem + kABytes, smem + 2 * kABytes, &mbar, hi_off, &abort_s, 0, 0, false};
+    tc_setup(c, &tmem_base_s);
+    tc_pass_tiles(st, p, umats, blockIdx.x, gridDim.x, c, status);
+    tc_teardown(c);
+}
+
+// ---------------------------------------------------------------------------
+// batched sweeps on the tensor cores
+// ---------------------------------------------------------------------------
+
+constexpr int64_t kScratchHalves = int64_t(DM_MAX_ROUNDS) * kUHalves;   // round images per CTA
+
+// Kernel parameters of one batched pass (thread 0 the scalars, all threads the rounds).
+__device__ void batch_tc_setup(Pass &ps, const dm_batch_tc_pass &bp, int n) {
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        ps.n = n;
+        ps.m = n - kAxes;
+        int low = 0;
+        while (low < kAxes && bp.ops.axes[low] == n - 1 - low) ++low;
+        ps.low = low;
+        ps.nrounds = bp.ops.nrounds;
+        ps.vec0 = bp.tables.vec0 == 0 ? 0 : -1;
+        ps.up = ldexpf(1.0f, n);
+        ps.down = ldexpf(1.0f, -n);
+        unsigned resident = 0;
+        for (int r = 0; r < kAxes; ++r) {
+            resident |= 1u << bp.ops.axes[r];
+            ps.res_stride[r] = int64_t(1) << (2 * (n - 1 - bp.ops.axes[r]));
+        }
+        int m = 0;
+        for (int q = n - 1; q >= 0; --q)
+            if (!((resident >> q) & 1)) ps.nonres_stride[m++] = int64_t(1) << (2 * (n - 1 - q));
+        for (int i = 0; i < 8; ++i) ps.natrow[i] = bp.tables.natrow[i];
+        for (int i = 0; i < 6; ++i) ps.natk[i] = bp.tables.natk[i];
+    }
+    for (int r = tid; r < bp.ops.nrounds; r += kThreads) {
+        const dm_tc_round &in = bp.tables.rounds[r];
+        Round &o = ps.rounds[r];
+        for (int i = 0; i < 3; ++i) o.digits[i] = in.digits[i];
+        o.vec = in.vec;
+        o.umoff = int32_t(r * kUHalves);
+        for (int i = 0; i < 8; ++i) o.rowc[i] = in.rowc[i];
+        for (int i = 0; i < 6; ++i) o.kc[i] = in.kc[i];
+    }
+}
+
+// Round r's matrix U (64 x 64 in its K-digit order) is the round's operations
+// applied to the 64 unit vectors: column k of U = ops(e_k), in FP32 with the
+// register-round code.  Written as the three FP16 images the MMAs read
+// (2**11 Uh, Ul = fp16(2**11 (U - Uh)), Uh; value (n%8)*8 + k%8 + (k/8)*64 +
+// (n/8)*512 for output n, input k).
+__device__ void compose_rounds(const dm_batch_pass &bp, const float *__restrict__ mats, uint16_t *__restrict__ umats) {
+    const int nr = bp.nrounds;
+    for (int w = threadIdx.x; w < nr * 64; w += kThreads) {
+        const int r = w >> 6, k = w & 63;
+        float v[64];
+#pragma unroll
+        for (int j = 0; j < 64; ++j) v[j] = j == k ? 1.0f : 0.0f;
+        const int ob = r > 0 ? bp.round_end[r - 1] : 0, oe = bp.round_end[r];
+        for (int o = ob; o < oe; ++o) reg_apply<float, 3>(v, bp.ops[o], mats);
+        uint16_t *img = umats + int64_t(r) * kUHalves;
+        const uint32_t kpos = uint32_t(k & 7) + uint32_t(k >> 3) * 64;
+#pragma unroll
+        for (int j = 0; j < 64; ++j) {
+            const uint32_t pos = kpos + uint32_t(j & 7) * 8 + uint32_t(j >> 3) * 512;
+            const __half h = __float2half_rn(v[j]);
+            const float hf = __half2float(h);
+            img[pos] = __half_as_ushort(__float2half_rn(hf * kLoScale));
+            img[4096 + pos] = __half_as_ushort(__float2half_rn((v[j] - hf) * kLoScale));
+            img[8192 + pos] = __half_as_ushort(h);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
+    batch_tc_kernel(float *__restrict__ states, double *__restrict__ probs, const float *__restrict__ mats,
+                    const dm_batch_instance *__restrict__ insts, int ninst, const dm_batch_tc_pass *__restrict__ passes,
+                    int *counter, uint16_t *__restrict__ scratch, int *status) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int64_t hi_off[kTile / 4 / kThreads];
+    __shared__ int abort_s;
+    __shared__ int inst_s;
+    __shared__ Pass ps;
+    TcCta c{smem, smem + kABytes, smem + 2 * kABytes, &mbar, hi_off, &abort_s, 0, 0, false};
+    tc_setup(c, &tmem_base_s);
+    uint16_t *umats = scratch + int64_t(blockIdx.x) * kScratchHalves;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) inst_s = atomicAdd(counter, 1);
+        __syncthreads();
+        const int ii = inst_s;
+        if (ii >= ninst) break;
+        const dm_batch_instance I = insts[ii];
+        float *st = states + I.state_off;
+        batch_init_zero<float, kThreads>(st, I.n);
+        bool ok = true;
+        for (int pi = 0; pi < I.npasses && ok; ++pi) {
+            const dm_batch_tc_pass &bp = passes[I.pass_begin + pi];
+            batch_tc_setup(ps, bp, I.n);
+            compose_rounds(bp.ops, mats + I.mats_off, umats);
+            __threadfence_block();
+            __syncthreads();
+            ok = tc_pass_tiles(st, ps, umats, 0, 1, c, status);
+        }
+        if (!ok) break;
+        batch_z_readout<float, kThreads>(st, I.n, I.meas_err, probs + I.prob_off, reinterpret_cast<double *>(smem));
+    }
+    tc_teardown(c);
 }
 
 }  // namespace tc
@@ -413,6 +559,8 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
 }  // namespace dmg
 
 using namespace dmg;
+
+constexpr int kBatchTcMaxQubits = 12;   // the Z read-out's 2**n doubles fit the operand region
 
 // Offsets must be distinct powers of two (operand) so that their XOR stays inside
 // a 32 KB operand image, or natural-tile element offsets below 4**7.
@@ -501,6 +649,92 @@ extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, 
     if (grid > ntiles) grid = ntiles;
     tc::pass_tc_kernel<<<int(grid), tc::kThreads, tc::kSmemBytes, as_stream(stream)>>>(
         static_cast<float *>(state_dev), p, umats_dev, status_dev);
+    count_launch();
+    return launch_status();
+}
+
+extern "C" size_t dm_batch_tc_scratch_bytes(void) {
+    return size_t(sm_count()) * tc::kCtasPerSm * size_t(tc::kScratchHalves) * sizeof(uint16_t);
+}
+
+// One tensor-core batched pass against an instance of n qubits with a coefficient block of mats_len values.
+static int validate_batch_tc_pass(const dm_batch_tc_pass &bp, int n, int64_t mats_len) {
+    const dm_batch_pass &o = bp.ops;
+    if (o.k != tc::kAxes || o.nrounds < 1 || o.nrounds > DM_MAX_ROUNDS) return DM_ERR_PROGRAM;
+    if (o.nops < 0 || o.nops > DM_MAX_PASS_OPS) return DM_ERR_PROGRAM;
+    if (o.axes[0] != n - 1) return DM_ERR_PROGRAM;   // 16-byte chunks need the lowest axis resident
+    for (int r = 0; r < tc::kAxes; ++r)
+        if (o.axes[r] < 0 || o.axes[r] >= n || (r > 0 && o.axes[r] >= o.axes[r - 1])) return DM_ERR_PROGRAM;
+    const int vec0 = bp.tables.vec0 == 0 ? 0 : -1;
+    if (!valid_tables(bp.tables.natrow, bp.tables.natk, vec0, true)) return DM_ERR_PROGRAM;
+    int prev_end = 0;
+    for (int r = 0; r < o.nrounds; ++r) {
+        const dm_tc_round &tr = bp.tables.rounds[r];
+        for (int i = 0; i < 3; ++i) {
+            const int a = o.round_axes[r][i];
+            if (a < 0 || a >= tc::kAxes || tr.digits[i] != a) return DM_ERR_PROGRAM;
+            for (int j = 0; j < i; ++j)
+                if (o.round_axes[r][j] == a) return DM_ERR_PROGRAM;
+        }
+        if (!valid_tables(tr.rowc, tr.kc, tr.vec, r + 1 == o.nrounds)) return DM_ERR_PROGRAM;
+        const int end = o.round_end[r];
+        if (end < prev_end || end > o.nops) return DM_ERR_PROGRAM;
+        for (int i = prev_end; i < end; ++i) {
+            const dm_op &op = o.ops[i];
+            int64_t need = 0;
+            switch (op.kind) {
+                case DM_OP_MAP1: need = 16; break;
+                case DM_OP_DIAG2: need = 16; break;
+                case DM_OP_CX: need = 5; break;
+                default: return DM_ERR_PROGRAM;
+            }
+            if (op.moff < 0 || op.moff + need > mats_len) return DM_ERR_PROGRAM;
+            const int da = (op.flags >> 8) & 3, db = (op.flags >> 12) & 3;
+            if (op.a < 0 || op.a >= tc::kAxes || da >= 3 || o.round_axes[r][da] != op.a) return DM_ERR_PROGRAM;
+            if (op.kind != DM_OP_MAP1 &&
+                (op.b < 0 || op.b >= tc::kAxes || op.b == op.a || db >= 3 || db == da || o.round_axes[r][db] != op.b))
+                return DM_ERR_PROGRAM;
+        }
+        prev_end = end;
+    }
+    return prev_end == o.nops ? DM_OK : DM_ERR_PROGRAM;
+}
+
+extern "C" int dm_batch_run_tc(float *states_dev, size_t states_count, double *probs_dev, size_t probs_count,
+                               const float *mats_dev, size_t mats_count, const dm_batch_instance *insts_host,
+                               const dm_batch_instance *insts_dev, int ninst, const dm_batch_tc_pass *passes_host,
+                               const dm_batch_tc_pass *passes_dev, int npasses, int *counter_dev, void *scratch_dev,
+                               size_t scratch_bytes, int *status_dev, void *stream) {
+    DM_CHECK_ARG(states_dev && probs_dev && mats_dev && insts_host && insts_dev && passes_host && passes_dev &&
+                 counter_dev && scratch_dev && status_dev && ninst >= 1 && npasses >= 1);
+    if (reinterpret_cast<uintptr_t>(states_dev) & 15 || reinterpret_cast<uintptr_t>(scratch_dev) & 15) return DM_ERR_ARG;
+    for (int i = 0; i < ninst; ++i) {
+        const dm_batch_instance &I = insts_host[i];
+        if (I.n < tc::kAxes || I.n > kBatchTcMaxQubits) return DM_ERR_RANGE;
+        const int64_t total = int64_t(1) << (2 * I.n);
+        if (I.state_off < 0 || (I.state_off & 3) || size_t(I.state_off + total) > states_count) return DM_ERR_ARG;
+        if (I.prob_off < 0 || size_t(I.prob_off + (int64_t(1) << I.n)) > probs_count) return DM_ERR_ARG;
+        if (I.mats_off < 0 || I.mats_len < 0 || size_t(I.mats_off + I.mats_len) > mats_count) return DM_ERR_ARG;
+        if (I.npasses < 0 || I.pass_begin < 0 || I.pass_begin + I.npasses > npasses) return DM_ERR_PROGRAM;
+        for (int p = 0; p < I.npasses; ++p) {
+            const int rc = validate_batch_tc_pass(passes_host[I.pass_begin + p], I.n, I.mats_len);
+            if (rc) return rc;
+        }
+    }
+    if (scratch_bytes < dm_batch_tc_scratch_bytes()) return DM_ERR_ARG;
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(tc::batch_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int(tc::kSmemBytes));
+    });
+    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    cudaStream_t s = as_stream(stream);
+    DM_CUDA_TRY(cudaMemsetAsync(counter_dev, 0, sizeof(int), s));
+    const int grid = sm_count() * tc::kCtasPerSm;
+    tc::batch_tc_kernel<<<grid, tc::kThreads, tc::kSmemBytes, s>>>(states_dev, probs_dev, mats_dev, insts_dev, ninst,
+                                                                     passes_dev, counter_dev,
+                                                                     static_cast<uint16_t *>(scratch_dev), status_dev);
     count_launch();
     return launch_status();
 }

@@ -30,6 +30,97 @@ _COPY_CHUNK = 1 << 25
 _HOST_SLICE = 1 << 21
 _COPY_BUFFERS = {}
 _POOL = []
+# Host result memory of large copy-outs, up to two blocks per size (a loop
+# that keeps the previous result while it runs the next alternates between
+# them): touched once by the host threads and page-locked, so later copy-outs
+# go straight from the device into it.  A block is handed out as one numpy
+# array and reused only after that array and every view of it have been
+# released.  Blocks are made only while the host has room for them.
+_RESULT_BLOCKS = {}
+_BLOCKS_PER_SIZE = 2
+
+
+class _ResultBlock:
+    def __init__(self, nbytes):
+        import mmap
+        self.mm = mmap.mmap(-1, nbytes)
+        self.nbytes = nbytes
+        self.free = True
+        arr = np.frombuffer(self.mm, dtype=np.uint8)
+        parts = [(s0, min(nbytes, s0 + 8 * _HOST_SLICE)) for s0 in range(0, nbytes, 8 * _HOST_SLICE)]
+        list(_host_pool().map(lambda r: arr[r[0]:r[1]].fill(0), parts))     # first touch, in parallel
+        self.ptr = arr.ctypes.data
+        del arr
+        self.pinned = _page_lock(self.ptr, nbytes)
+        self._unlock = _page_unlock
+
+    def __del__(self):
+        # unregister before the mapping can go away (a later mapping may reuse the addresses)
+        if getattr(self, 'pinned', False):
+            try:
+                self._unlock(self.ptr)
+            except Exception:       # interpreter shutdown
+                pass
+
+
+def _page_lock(ptr, nbytes):
+    """Register host memory with CUDA (page-locked, device-copyable); False if refused."""
+    return int(_torch().cuda.cudart().cudaHostRegister(ptr, nbytes, 0)) == 0
+
+
+def _page_unlock(ptr):
+    _torch().cuda.cudart().cudaHostUnregister(ptr)
+
+
+def _release_block(blk):
+    blk.free = True
+
+
+def _host_bytes_available():
+    """Bytes the host can still hand out: MemAvailable, capped by the cgroup's free allowance."""
+    avail = 0
+    try:
+        with open('/proc/meminfo') as f:
+            for line in f:
+                if line.startswith('MemAvailable:'):
+                    avail = int(line.split()[1]) * 1024
+    except OSError:
+        return 0
+    for lim_file, cur_file in (('/sys/fs/cgroup/memory.max', '/sys/fs/cgroup/memory.current'),
+                               ('/sys/fs/cgroup/memory/memory.limit_in_bytes',
+                                '/sys/fs/cgroup/memory/memory.usage_in_bytes')):
+        try:
+            with open(lim_file) as f:
+                lim = f.read().strip()
+            with open(cur_file) as f:
+                cur = int(f.read().strip())
+        except (OSError, ValueError):
+            continue
+        if lim != 'max' and int(lim) < (1 << 60):
+            avail = min(avail, int(lim) - cur)
+    return avail
+
+
+def _result_array(total):
+    """(float64 array of ``total`` values, whether its memory is page-locked) for one copy-out."""
+    import weakref
+    nbytes = total * 8
+    blocks = _RESULT_BLOCKS.setdefault(nbytes, [])
+    blk = next((b for b in blocks if b.free), None)
+    if blk is None and blocks:
+        # a released result may still sit in an unreachable reference cycle (job, future, result)
+        import gc
+        gc.collect()
+        blk = next((b for b in blocks if b.free), None)
+    if blk is None:
+        if len(blocks) >= _BLOCKS_PER_SIZE or _host_bytes_available() < 2 * nbytes:
+            return np.empty(total, dtype=np.float64), False     # earlier results still held, or no room
+        blk = _ResultBlock(nbytes)
+        blocks.append(blk)
+    arr = np.frombuffer(blk.mm, dtype=np.float64, count=total)
+    blk.free = False
+    weakref.finalize(arr, _release_block, blk)
+    return arr, blk.pinned
 
 
 def _copy_buffers(device):
@@ -299,9 +390,11 @@ class DeviceState:
         """FP64 copy of the coefficients with |a| < chop_threshold set to 0.
 
         Large states stream out in chunks: the chop kernel fills one of two
-        device buffers, an async copy moves it to one of two pinned host
-        buffers, and host threads copy the previous chunk into the result
-        while the GPU works on the next one.
+        device buffers and an async copy moves it into the page-locked
+        result block.  When that block is still held by an earlier result,
+        the chunks go to one of two pinned staging buffers instead and host
+        threads copy the previous chunk into a fresh array while the GPU
+        works on the next one.
         """
         self.flush()
         torch = _torch()
@@ -311,9 +404,21 @@ class DeviceState:
             N.call('dm_chop_copy', self.ptr, self.n, self.dtype, float(chop_threshold),
                    ctypes.c_void_p(out.data_ptr()), self.stream)
             return self._to_host(out)
-        result = np.empty(total, dtype=np.float64)
+        result, direct = _result_array(total)
         dev, pinned = _copy_buffers(self.device)
         stream = torch.cuda.current_stream(self.device)
+        if direct:
+            # page-locked result: each chunk goes from the device buffer straight into it
+            host = torch.from_numpy(result)
+            for i, off in enumerate(range(0, total, _COPY_CHUNK)):
+                b = i % 2
+                cnt = min(_COPY_CHUNK, total - off)
+                N.call('dm_chop_copy_range', self.ptr, self.n, self.dtype, ctypes.c_int64(off), ctypes.c_int64(cnt),
+                       float(chop_threshold), ctypes.c_void_p(dev[b].data_ptr()), self.stream)
+                host[off:off + cnt].copy_(dev[b][:cnt], non_blocking=True)
+            stream.synchronize()
+            self.d2h_bytes += total * 8
+            return result
         events = [None, None]
         pending = None
         pool = _host_pool()

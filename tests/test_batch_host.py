@@ -23,9 +23,12 @@ def emulate_instance(T, i):
     for m in range(2 ** n):
         idx = sum((3 if (m >> (n - 1 - q)) & 1 else 0) * 4 ** (n - 1 - q) for q in range(n))
         st[idx] = 2.0 ** -n
-    mats = T.mats[I.mats_off:I.mats_off + I.mats_len].astype(np.float64)
+    part = T.index[i][0]
+    mats = part.mats[I.mats_off:I.mats_off + I.mats_len].astype(np.float64)
     for p in range(I.pass_begin, I.pass_begin + I.npasses):
-        bp = T.passes[p]
+        bp = part.passes[p]
+        if isinstance(bp, N.DmBatchTcPass):
+            bp = bp.ops
         axes = [bp.axes[r] for r in range(bp.k)]
         assert axes[0] == n - 1 and axes == sorted(axes, reverse=True)
         o = 0
@@ -127,3 +130,71 @@ def test_worker_processes_compile_the_same_tables():
         assert bytes(a[prec].insts) == bytes(b[prec].insts)
         assert bytes(a[prec].passes) == bytes(b[prec].passes)
         assert np.array_equal(a[prec].mats, b[prec].mats)
+
+
+def test_tensor_core_batch_tables_replay_equals_oracle():
+    """Instances planned for the tensor cores (7 resident axes, rounds in their layouts' digit order)."""
+    specs = B.sweep_specs(5, seed=11, n_range=(7, 9), depth_range=(2, 5))
+    T = B.BatchTables(specs, 'single', kmax={7: B.TC, 8: B.TC, 9: B.TC})
+    assert T.tc.ninst == len(specs) and T.ninst == 0
+    for i, spec in enumerate(specs):
+        np.testing.assert_allclose(emulate_instance(T, i), oracle_probs(spec), atol=2e-6)
+
+
+def _op_from_table(d, rax, mats):
+    from qiskit_aakash_gb300 import program as P
+    da, db = (d.flags >> 8) & 3, (d.flags >> 12) & 3
+    if d.kind == N.DM_OP_MAP1:
+        return P.Op('map1', (rax[da],), mats[d.moff:d.moff + 16].reshape(4, 4))
+    if d.kind == N.DM_OP_CX:
+        return P.Op('cx', (rax[da], rax[db]), mats[d.moff:d.moff + 5], bool(d.flags & N.DM_CX_IDEAL))
+    return P.Op('diag2', (rax[da], rax[db]), mats[d.moff:d.moff + 16])
+
+
+def test_tensor_core_round_matrices_from_the_table_equal_the_single_state_plan():
+    """The device composes round r's U from the table (ops on the 64 unit vectors, K digits in the
+    round's order); that U equals the one the single-state tensor-core path composes on the host."""
+    from qiskit_aakash_gb300 import program as P
+    spec = B.sweep_specs(1, seed=5, n_range=(9, 9), depth_range=(6, 6))[0]
+    rec = B.compile_experiment(*B.instance_experiment(spec))
+    plan = B._TcPlan(rec.ops, spec['n'])
+    mats = plan.coefficients(rec.ops, np.float64)
+    host_passes = P.plan_passes(rec.ops, spec['n'], P.TC_AXES, 2)
+    assert len(host_passes) == len(plan.passes)
+    for hp, bp in zip(host_passes, plan.passes):
+        _, layouts, want = P.plan_tc_pass(hp, spec['n'])
+        o = bp.ops
+        assert o.nrounds == len(want)
+        begin = 0
+        for r in range(o.nrounds):
+            rax = [o.round_axes[r][j] for j in range(3)]
+            assert rax == list(layouts[r].digits) == [bp.tables.rounds[r].digits[j] for j in range(3)]
+            U = np.eye(64)
+            for idx in range(begin, o.round_end[r]):
+                U = P.op_matrix64(_op_from_table(o.ops[idx], rax, mats), rax) @ U
+            np.testing.assert_allclose(U, want[r], atol=1e-14)
+            begin = o.round_end[r]
+
+
+def test_mixed_batch_packs_both_parts():
+    specs = B.sweep_specs(12, seed=3, n_range=(6, 8), depth_range=(2, 4))
+    T = B.BatchTables(specs, 'single', kmax={7: B.TC, 8: B.TC})
+    n_small = sum(1 for s in specs if s['n'] == 6)
+    assert T.ninst == n_small and T.tc.ninst == len(specs) - n_small
+    seen_states, seen_probs = [], []
+    for i, spec in enumerate(specs):
+        I = T.instance(i)
+        assert I.n == spec['n']
+        seen_states.append((I.state_off, 4 ** I.n))
+        seen_probs.append((I.prob_off, 2 ** I.n))
+        part = T.index[i][0]
+        assert (part is T.tc) == (spec['n'] >= 7)
+        assert I.mats_off + I.mats_len <= part.mats.size
+    for seen, total in ((seen_states, T.states_count), (seen_probs, T.probs_count)):
+        seen.sort()
+        pos = 0
+        for off, size in seen:
+            assert off == pos
+            pos += size
+        assert pos == total
+    assert T.swept_bytes(4) == sum(2 * 4 ** I.n * 4 * I.npasses for I in T.all_instances())

@@ -48,7 +48,8 @@ def test_struct_layout_matches_header(tmp_path):
         'offsetof(dm_batch_pass, round_end), offsetof(dm_batch_pass, ops), sizeof(dm_batch_instance), '
         'offsetof(dm_batch_instance, meas_err)); printf("%zu %zu %zu\\n", sizeof(dm_mlp_gemm), '
         'offsetof(dm_mlp_gemm, A), offsetof(dm_mlp_gemm, t_ms)); printf("%zu %zu %zu %zu\\n", sizeof(dm_recipe), '
-        'offsetof(dm_recipe, angle), sizeof(dm_param_program), offsetof(dm_param_program, consts)); return 0; }\n')
+        'offsetof(dm_recipe, angle), sizeof(dm_param_program), offsetof(dm_param_program, consts)); '
+        'printf("%zu %zu\\n", sizeof(dm_batch_tc_pass), offsetof(dm_batch_tc_pass, tables)); return 0; }\n')
     exe = tmp_path / 'layout'
     subprocess.run(['gcc', '-I', os.path.dirname(HEADER), str(src), '-o', str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
@@ -58,7 +59,8 @@ def test_struct_layout_matches_header(tmp_path):
             N.DmBatchPass.round_end.offset, N.DmBatchPass.ops.offset, ctypes.sizeof(N.DmBatchInstance),
             N.DmBatchInstance.meas_err.offset, ctypes.sizeof(N.DmMlpGemm), N.DmMlpGemm.A.offset,
             N.DmMlpGemm.t_ms.offset, ctypes.sizeof(N.DmRecipe), N.DmRecipe.angle.offset,
-            ctypes.sizeof(N.DmParamProgram), N.DmParamProgram.consts.offset]
+            ctypes.sizeof(N.DmParamProgram), N.DmParamProgram.consts.offset,
+            ctypes.sizeof(N.DmBatchTcPass), N.DmBatchTcPass.tables.offset]
     assert got == want
     text = open(HEADER).read()
     assert int(re.search(r'#define DM_MAX_TILE_AXES (\d+)', text).group(1)) == N.DM_MAX_TILE_AXES

@@ -111,3 +111,103 @@ def test_batch_rejects_bad_tables():
     insts[0].mats_len = 1
     with pytest.raises(N.NativeError):
         N.call('dm_batch_run', *args(insts, t.passes, t.npasses))
+
+
+TC_KMAX = {n: B.TC for n in range(7, 13)}
+
+
+def test_tensor_core_batch_matches_oracle(small_sweep):
+    """Mixed batch: 7- and 8-qubit instances on the tensor cores, the rest on the CUDA-core rounds."""
+    specs, want = small_sweep
+    T = B.BatchTables(specs, 'single', kmax=TC_KMAX)
+    assert T.tc.ninst > 0 and T.ninst > 0
+    prog = B.BatchProgram(T)
+    prog.launch()
+    got = prog.results()
+    for i, spec in enumerate(specs):
+        assert np.max(np.abs(got[i] - want[i])) < TOL['single'], (i, spec)
+        assert abs(got[i].sum() - 1.0) < TOL['single']
+
+
+def test_tensor_core_batch_large_instances_match_fp64_backend():
+    from qiskit_aakash_gb300.dm_simulator import DmSimulatorGPU
+    specs = B.sweep_specs(8, seed=14, n_range=(9, 12), depth_range=(6, 24))
+    T = B.BatchTables(specs, 'single', kmax=TC_KMAX)
+    assert T.tc.ninst == len(specs)
+    prog = B.BatchProgram(T)
+    prog.launch()
+    got = prog.results()
+    for i, spec in enumerate(specs):
+        exp, opts = B.instance_experiment(spec)
+        DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
+        be = DmSimulatorGPU()
+        be._set_options(backend_options=dict(opts, compute_densitymatrix=False, precision='double'))
+        res = be.run_experiment(exp)
+        p = res['data']['ensemble_probability']
+        ref = np.array([p[k] for k in O.bitstring_keys(spec['n'])])
+        assert np.max(np.abs(got[i] - ref)) < TOL['single'] * 10, i
+
+
+def test_tensor_core_batch_graph_replay():
+    import torch
+    specs = B.sweep_specs(20, seed=9, n_range=(6, 10), depth_range=(2, 8))
+    prog = B.BatchProgram(B.BatchTables(specs, 'single', kmax=TC_KMAX))
+    prog.capture()
+    torch.cuda.synchronize()
+    first = [r.copy() for r in prog.results()]
+    prog.probs.zero_()
+    prog.states.fill_(float('nan'))
+    for _ in range(3):
+        prog.run()
+    torch.cuda.synchronize()
+    for a, b in zip(first, prog.results()):
+        assert np.array_equal(a, b)
+
+
+def test_tensor_core_batch_rejects_bad_tables():
+    specs = B.sweep_specs(2, seed=2, n_range=(7, 8), depth_range=(2, 4))
+    prog = B.BatchProgram(B.BatchTables(specs, 'single', kmax=TC_KMAX))
+    tc = prog.t.tc
+    t = prog.t
+    vp = ctypes.c_void_p
+
+    def call(insts, passes):
+        N.call('dm_batch_run_tc', vp(prog.states.data_ptr()), ctypes.c_size_t(t.states_count),
+               vp(prog.probs.data_ptr()), ctypes.c_size_t(t.probs_count), vp(prog.tc_mats_dev.data_ptr()),
+               ctypes.c_size_t(tc.mats.size), insts, vp(prog.tc_insts_dev.data_ptr()), tc.ninst, passes,
+               vp(prog.tc_passes_dev.data_ptr()), tc.npasses, vp(prog.counter.data_ptr()),
+               vp(prog.tc_scratch.data_ptr()), ctypes.c_size_t(prog.tc_scratch.numel()),
+               vp(prog.status.data_ptr()), None)
+
+    def fresh_passes():
+        return (N.DmBatchTcPass * tc.npasses).from_buffer_copy(bytes(tc.passes))
+
+    bad = fresh_passes()
+    bad[0].tables.rounds[0].digits[0] = (bad[0].ops.round_axes[0][0] + 1) % 7   # table and op digits disagree
+    with pytest.raises(N.NativeError) as e:
+        call(tc.insts, bad)
+    assert e.value.code == N.DM_ERR_PROGRAM
+    bad = fresh_passes()
+    bad[0].ops.k = 6
+    with pytest.raises(N.NativeError) as e:
+        call(tc.insts, bad)
+    assert e.value.code == N.DM_ERR_PROGRAM
+    bad = fresh_passes()
+    bad[0].tables.rounds[0].rowc[0] = 0                                  # a zero destination offset
+    with pytest.raises(N.NativeError) as e:
+        call(tc.insts, bad)
+    assert e.value.code == N.DM_ERR_PROGRAM
+    insts = (N.DmBatchInstance * tc.ninst).from_buffer_copy(bytes(tc.insts))
+    insts[0].n = 6
+    with pytest.raises(N.NativeError) as e:
+        call(insts, tc.passes)
+    assert e.value.code == N.DM_ERR_RANGE
+    with pytest.raises(N.NativeError) as e:
+        N.call('dm_batch_run_tc', vp(prog.states.data_ptr()), ctypes.c_size_t(t.states_count),
+               vp(prog.probs.data_ptr()), ctypes.c_size_t(t.probs_count), vp(prog.tc_mats_dev.data_ptr()),
+               ctypes.c_size_t(tc.mats.size), tc.insts, vp(prog.tc_insts_dev.data_ptr()), tc.ninst, tc.passes,
+               vp(prog.tc_passes_dev.data_ptr()), tc.npasses, vp(prog.counter.data_ptr()),
+               vp(prog.tc_scratch.data_ptr()), ctypes.c_size_t(16), vp(prog.status.data_ptr()), None)
+    assert e.value.code == N.DM_ERR_ARG
+    prog.launch()                                       # the good tables still run
+    assert int(prog.status.item()) == 0

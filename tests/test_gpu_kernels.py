@@ -260,7 +260,8 @@ def test_tensor_core_pass_rejects_bad_programs(torch):
 
 @pytest.mark.parametrize('dtype', [N.DM_F64, N.DM_F32])
 def test_chunked_copy_out_equals_one_shot(torch, dtype, monkeypatch):
-    """DeviceState.coefficients in chunks (chop range kernel, pinned double buffers) = dm_chop_copy."""
+    """DeviceState.coefficients in chunks (chop range kernel; straight into a page-locked result
+    block, or through pinned staging buffers when the blocks are held) = dm_chop_copy."""
     from qiskit_aakash_gb300 import engine
     n = 7
     rng = np.random.default_rng(5)
@@ -271,8 +272,25 @@ def test_chunked_copy_out_equals_one_shot(torch, dtype, monkeypatch):
     one = ds.coefficients(1e-15)
     monkeypatch.setattr(engine, '_COPY_CHUNK', 1000)     # 17 chunks, the last one ragged
     monkeypatch.setattr(engine, '_HOST_SLICE', 96)
-    chunked = ds.coefficients(1e-15)
+    engine._RESULT_BLOCKS.pop(8 * 4 ** n, None)
+    chunked = ds.coefficients(1e-15)                     # page-locked block 1, device -> block copies
     assert np.array_equal(one, chunked)
+    blocks = engine._RESULT_BLOCKS[8 * 4 ** n]
+    assert len(blocks) == 1 and blocks[0].pinned and not blocks[0].free
+    second = ds.coefficients(1e-15)                      # block 1 held: block 2
+    third = ds.coefficients(1e-15)                       # both held: staging buffers + host copies
+    assert len(blocks) == 2 and blocks[1].pinned
+    for got in (chunked, second, third):
+        assert np.array_equal(one, got)
+    del second
+    import gc
+    gc.collect()
+    assert blocks[1].free
+    again = ds.coefficients(1e-15)                       # released block 2 is reused
+    assert np.array_equal(one, again) and not blocks[1].free
+    del chunked, third, again
+    engine._RESULT_BLOCKS.pop(8 * 4 ** n)               # unregistered when dropped
+    gc.collect()
     with pytest.raises(N.NativeError):
         out = torch.empty(10, dtype=torch.float64, device='cuda')
         N.call('dm_chop_copy_range', ds.ptr, n, dtype, ctypes.c_int64(4 ** n - 5), ctypes.c_int64(10), 0.0,
