@@ -576,9 +576,11 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
     del warm, warm2
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    each = []
     for _ in range(args.e2e_steps):
         DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
         res = pkg.execute(qc, backend, **copy.deepcopy(e2e_opts)).result()
+        each.append(time.perf_counter() - t0 - sum(each))
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
     e2e_s = allmax(torch, world, e2e_s)
@@ -630,6 +632,7 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
                      'mean_launch_ms': mean_pass_ms,
                      'algorithmic_bytes_per_launch': 2 * N4 * 4, 'peak_kind': peak_kind},
         'e2e': {'value': world * layers / e2e_s, 'unit': 'gate-layers/s', 'seconds_per_step': e2e_s,
+                'seconds_each': each,
                 'h2d_bytes_per_step': int(st['h2d_bytes']), 'd2h_bytes_per_step': int(st['d2h_bytes']),
                 'api': "BasicAer.get_backend('dm_simulator') + execute(...).result()"},
         'gpu_launches': int(launches),

@@ -232,12 +232,13 @@ size_t dm_batch_tc_scratch_bytes(void);
 
 /* dm_batch_run for FP32 instances of 7..12 qubits with every pass on the
  * tensor cores (the dm_apply_pass_tc kernel): at the start of each pass a
- * CTA composes the pass's round matrices from the instance's coefficient
- * block (FP32, the ops applied to the 64 unit vectors) into its slice of
- * scratch_dev as the 3-way FP16 split images, then streams the instance's
- * tiles.  status_dev is set to 1 if a bounded tensor-core wait gives up. */
+ * CTA composes the pass's round matrices from the instance's FP64
+ * coefficient block (the ops applied to the 64 unit vectors, in FP64) into
+ * its slice of scratch_dev as the 3-way FP16 split images, then streams the
+ * instance's tiles.  status_dev is set to 1 if a bounded tensor-core wait
+ * gives up. */
 int dm_batch_run_tc(float *states_dev, size_t states_count, double *probs_dev, size_t probs_count,
-                    const float *mats_dev, size_t mats_count, const dm_batch_instance *insts_host,
+                    const double *mats_dev, size_t mats_count, const dm_batch_instance *insts_host,
                     const dm_batch_instance *insts_dev, int ninst, const dm_batch_tc_pass *passes_host,
                     const dm_batch_tc_pass *passes_dev, int npasses, int *counter_dev, void *scratch_dev,
                     size_t scratch_bytes, int *status_dev, void *stream);

@@ -492,7 +492,8 @@ class BatchTables:
         self.np_dtype = np.float32 if precision == 'single' else np.float64
         self.specs = specs
         order = sorted(range(len(specs)), key=lambda i: -(4 ** specs[i]['n'] * specs[i]['depth']))
-        main, tc = _Part(N.DmBatchPass, self.np_dtype), _Part(N.DmBatchTcPass, self.np_dtype)
+        # the tensor-core part keeps FP64 coefficients: its round matrices are composed in FP64
+        main, tc = _Part(N.DmBatchPass, self.np_dtype), _Part(N.DmBatchTcPass, np.float64)
         state_off = prob_off = 0
         self.index = []
         for i in order:

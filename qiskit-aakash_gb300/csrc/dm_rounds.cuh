@@ -26,6 +26,43 @@ __device__ __forceinline__ void map4(const T *m, bool row0_id, T &x0, T &x1, T &
     x3 = y3;
 }
 
+// x[4*pc + pt]: control Pauli pc, target Pauli pt.  basicaertools.py:346-363
+// (the control > target branch, :371-388, is the same map in (control,
+// target) coordinates).
+template <typename T>
+__device__ __forceinline__ void cx16(T *x, const CxCoef<T> &k, bool ideal) {
+    if (ideal) {
+        T t;
+        t = x[2]; x[2] = x[14]; x[14] = t;          // IY <-> ZY
+        t = x[3]; x[3] = x[15]; x[15] = t;          // IZ <-> ZZ
+        t = x[4]; x[4] = x[5]; x[5] = t;            // XI <-> XX
+        t = x[8]; x[8] = x[9]; x[9] = t;            // YI <-> YX
+        T xy = x[6], xz = x[7], yy = x[10], yz = x[11];
+        x[6] = yz;                                  // XY <-  YZ
+        x[7] = -yy;                                 // XZ <- -YY
+        x[10] = -xz;                                // YY <- -XZ
+        x[11] = xy;                                 // YZ <-  XY
+        return;
+    }
+    const T c = k.c, s = k.s, c2 = k.c2, s2 = k.s2, cs = k.cs;
+    T i2 = x[2], i3 = x[3], z2 = x[14], z3 = x[15];
+    T x0 = x[4], x1 = x[5], x2 = x[6], x3 = x[7];
+    T y0 = x[8], y1 = x[9], y2 = x[10], y3 = x[11];
+    T d3 = i3 - z3, d2 = i2 - z2;
+    x[2] = fma(s2, i2, fma(c2, z2, -cs * d3));
+    x[14] = fma(c2, i2, fma(s2, z2, cs * d3));
+    x[3] = fma(s2, i3, fma(c2, z3, cs * d2));
+    x[15] = fma(c2, i3, fma(s2, z3, -cs * d2));
+    x[4] = fma(c, x1, -s * y0);
+    x[5] = fma(c, x0, -s * y1);
+    x[6] = fma(-s, y2, c * y3);
+    x[7] = fma(-c, y2, -s * y3);
+    x[8] = fma(s, x0, c * y1);
+    x[9] = fma(s, x1, c * y0);
+    x[10] = fma(s, x2, -c * x3);
+    x[11] = fma(c, x2, s * x3);
+}
+
 // Register index j of a group holds round digits (j & 3, (j >> 2) & 3, j >> 4).
 // The common trace-preserving map whose X and Y rows take no I component
 // (gates, memory noise, measurements, resets): 10 FMAs per 4 values.

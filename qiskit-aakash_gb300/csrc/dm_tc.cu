@@ -488,36 +488,90 @@ __device__ void batch_tc_setup(Pass &ps, const dm_batch_tc_pass &bp, int n) {
     }
 }
 
-// Round r's matrix U (64 x 64 in its K-digit order) is the round's operations
-// applied to the 64 unit vectors: column k of U = ops(e_k), in FP32 with the
-// register-round code.  Written as the three FP16 images the MMAs read
-// (2**11 Uh, Ul = fp16(2**11 (U - Uh)), Uh; value (n%8)*8 + k%8 + (k/8)*64 +
-// (n/8)*512 for output n, input k).
-__device__ void compose_rounds(const dm_batch_pass &bp, const float *__restrict__ mats, uint16_t *__restrict__ umats) {
-    const int nr = bp.nrounds;
-    for (int w = threadIdx.x; w < nr * 64; w += kThreads) {
-        const int r = w >> 6, k = w & 63;
-        float v[64];
+// One operation on a 64-coefficient column in shared memory (index j = d0 +
+// 4 d1 + 16 d2 over the round's digits; digit positions from the op flags),
+// in FP64: the same maps as the register rounds, with runtime digits.
+__device__ void col_apply(double *col, const dm_op &op, const double *__restrict__ mats) {
+    const double *mg = mats + op.moff;
+    const int da = (op.flags >> 8) & 3, db = (op.flags >> 12) & 3;
+    if (op.kind == DM_OP_MAP1) {
+        double m[16];
 #pragma unroll
-        for (int j = 0; j < 64; ++j) v[j] = j == k ? 1.0f : 0.0f;
+        for (int i = 0; i < 16; ++i) m[i] = mg[i];
+        const int S = 1 << (2 * da);
+#pragma unroll 1
+        for (int o = 0; o < 16; ++o) {
+            const int j0 = ((o >> (2 * da)) << (2 * da + 2)) | (o & (S - 1));
+            double x0 = col[j0], x1 = col[j0 + S], x2 = col[j0 + 2 * S], x3 = col[j0 + 3 * S];
+            map4(m, false, x0, x1, x2, x3);
+            col[j0] = x0;
+            col[j0 + S] = x1;
+            col[j0 + 2 * S] = x2;
+            col[j0 + 3 * S] = x3;
+        }
+        return;
+    }
+    const int SA = 1 << (2 * da), SB = 1 << (2 * db), SC = 1 << (2 * (3 - da - db));
+    CxCoef<double> cx{1.0, 0.0, 1.0, 0.0, 0.0};
+    const bool ideal = (op.flags & DM_CX_IDEAL) != 0;
+    if (op.kind == DM_OP_CX && !ideal) cx = CxCoef<double>{mg[0], mg[1], mg[2], mg[3], mg[4]};
+#pragma unroll 1
+    for (int o = 0; o < 4; ++o) {   // the four groups of the third digit
+        const int j0 = o * SC;
+        double x[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) x[i] = col[j0 + (i >> 2) * SA + (i & 3) * SB];
+        if (op.kind == DM_OP_CX) {
+            cx16(x, cx, ideal);
+        } else {   // DM_OP_DIAG2: entry (pa, pb) scaled by mg[4 pa + pb]
+#pragma unroll
+            for (int i = 0; i < 16; ++i) x[i] *= mg[i];
+        }
+#pragma unroll
+        for (int i = 0; i < 16; ++i) col[j0 + (i >> 2) * SA + (i & 3) * SB] = x[i];
+    }
+}
+
+// Round r's matrix U (64 x 64 in its K-digit order) is the round's operations
+// applied to the 64 unit vectors: column k of U = ops(e_k), composed in FP64
+// on a column held in shared memory (one thread per column, two rounds at a
+// time; the pass's operand and matrix regions are free between passes).
+// Written as the three FP16 images the MMAs read (2**11 Uh,
+// Ul = fp16(2**11 (U - Uh)), Uh; value (n%8)*8 + k%8 + (k/8)*64 + (n/8)*512
+// for output n, input k).
+constexpr int kColStride = 65;   // doubles per column: a warp's 32 columns spread over the banks
+static_assert(2 * 64 * kColStride * 8 <= int(kSmemBytes), "two rounds of FP64 columns fit the pass's shared memory");
+
+__device__ void compose_rounds(const dm_batch_pass &bp, const double *__restrict__ mats, uint16_t *__restrict__ umats,
+                               double *work) {
+    const int nr = bp.nrounds;
+    const int tid = threadIdx.x;
+    if (tid >= 128) return;
+    double *col = work + tid * kColStride;
+    for (int r0 = 0; r0 < nr; r0 += 2) {
+        const int r = r0 + (tid >> 6), k = tid & 63;
+        if (r >= nr) break;
+#pragma unroll 1
+        for (int j = 0; j < 64; ++j) col[j] = j == k ? 1.0 : 0.0;
         const int ob = r > 0 ? bp.round_end[r - 1] : 0, oe = bp.round_end[r];
-        for (int o = ob; o < oe; ++o) reg_apply<float, 3>(v, bp.ops[o], mats);
+        for (int o = ob; o < oe; ++o) col_apply(col, bp.ops[o], mats);
         uint16_t *img = umats + int64_t(r) * kUHalves;
         const uint32_t kpos = uint32_t(k & 7) + uint32_t(k >> 3) * 64;
-#pragma unroll
+#pragma unroll 4
         for (int j = 0; j < 64; ++j) {
             const uint32_t pos = kpos + uint32_t(j & 7) * 8 + uint32_t(j >> 3) * 512;
-            const __half h = __float2half_rn(v[j]);
-            const float hf = __half2float(h);
-            img[pos] = __half_as_ushort(__float2half_rn(hf * kLoScale));
-            img[4096 + pos] = __half_as_ushort(__float2half_rn((v[j] - hf) * kLoScale));
+            const double u = col[j];
+            const __half h = __double2half(u);
+            const double hd = double(__half2float(h));
+            img[pos] = __half_as_ushort(__float2half_rn(float(hd * double(kLoScale))));
+            img[4096 + pos] = __half_as_ushort(__double2half((u - hd) * double(kLoScale)));
             img[8192 + pos] = __half_as_ushort(h);
         }
     }
 }
 
 __global__ void __launch_bounds__(kThreads, kCtasPerSm)
-    batch_tc_kernel(float *__restrict__ states, double *__restrict__ probs, const float *__restrict__ mats,
+    batch_tc_kernel(float *__restrict__ states, double *__restrict__ probs, const double *__restrict__ mats,
                     const dm_batch_instance *__restrict__ insts, int ninst, const dm_batch_tc_pass *__restrict__ passes,
                     int *counter, uint16_t *__restrict__ scratch, int *status) {
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -543,7 +597,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
         for (int pi = 0; pi < I.npasses && ok; ++pi) {
             const dm_batch_tc_pass &bp = passes[I.pass_begin + pi];
             batch_tc_setup(ps, bp, I.n);
-            compose_rounds(bp.ops, mats + I.mats_off, umats);
+            compose_rounds(bp.ops, mats + I.mats_off, umats, reinterpret_cast<double *>(smem));
             __threadfence_block();
             __syncthreads();
             ok = tc_pass_tiles(st, ps, umats, 0, 1, c, status);
@@ -701,7 +755,7 @@ static int validate_batch_tc_pass(const dm_batch_tc_pass &bp, int n, int64_t mat
 }
 
 extern "C" int dm_batch_run_tc(float *states_dev, size_t states_count, double *probs_dev, size_t probs_count,
-                               const float *mats_dev, size_t mats_count, const dm_batch_instance *insts_host,
+                               const double *mats_dev, size_t mats_count, const dm_batch_instance *insts_host,
                                const dm_batch_instance *insts_dev, int ninst, const dm_batch_tc_pass *passes_host,
                                const dm_batch_tc_pass *passes_dev, int npasses, int *counter_dev, void *scratch_dev,
                                size_t scratch_bytes, int *status_dev, void *stream) {
