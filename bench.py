@@ -71,7 +71,8 @@ def parse():
     ap.add_argument('--surrogate-epochs', type=int, default=40)
     ap.add_argument('--legs', default='headline,batch,surrogate',
                     help='comma list of legs to run (the JSON line keeps only what ran)')
-    ap.add_argument('--no-autotune', action='store_true', help='batched sweep with the widest passes, untuned')
+    ap.add_argument('--no-autotune', action='store_true',
+                    help='batched sweep without timing candidates: tensor cores from 9 qubits, 7 resident axes below')
     return ap.parse_args()
 
 
@@ -370,7 +371,7 @@ def batch_leg(args, pkg, torch, N):
     specs = B.sweep_specs(args.batch, seed=args.seed)
     t0 = time.perf_counter()
     if args.no_autotune:
-        choice, tune_ms = {n: min(7, n) for n in range(6, 13)}, {}
+        choice, tune_ms = {n: (B.TC if n >= 9 else min(7, n)) for n in range(6, 13)}, {}
     else:
         choice, tune_ms = B.autotune(specs, 'single')
     tune_s = time.perf_counter() - t0

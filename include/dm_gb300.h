@@ -162,8 +162,8 @@ typedef struct dm_tc_pass {
 
 /* The fused pass on the tensor cores (FP32 state only, n >= 7): the rounds
  * run as tcgen05.mma kind::f16 on a 3-way FP16 split (the tile in units of
- * 2**-n, x = h + 2**-11 l; U = Uh + 2**-11 Ul; one FP32 accumulator in
- * tensor memory collects h (2**11 Uh)^T + l Uh^T + h Ul^T).  The state must
+ * 2**-n, x = h + 2**-11 l; U = Uh + 2**-11 Ul; FP32 accumulators in
+ * tensor memory collect h (2**11 Uh)^T and h Ul^T + l Uh^T).  The state must
  * be physical enough that |2**n a| < 65504.  umats_dev holds umats_count
  * FP16 values (uint16_t bits).  status_dev (device int, 0 before the first
  * call) is set to 1 if the kernel abandons a bounded wait.  Same role as

@@ -4,7 +4,8 @@
 // coefficients is streamed into shared memory (cp.async, 16-byte chunks),
 // then the pass's register rounds run as matrix products on the tensor
 // cores.  A round names 3 of the tile's axes; the round's operations,
-// composed on the host in FP64, form one 64x64 real transfer matrix U acting
+// composed in FP64 (on the host, or per instance on the device for the
+// batched sweeps), form one 64x64 real transfer matrix U acting
 // on the 64 coefficients that differ only in those axes.  With the tile
 // viewed as 256 groups x 64 (one row per group), the round is
 //     D[g][j'] = sum_j X[g][j] * U[j'][j]           (M = 256, N = 64, K = 64)
@@ -12,8 +13,10 @@
 // accuracy comes from a 3-way FP16 split: inside the pass the tile is held
 // in units of 2**-n (x = 2**n a, |x| <= 1), x = h + 2**-11 l with
 // h = fp16(x), l = fp16(2**11 (x - h)), and U = Uh + 2**-11 Ul likewise;
-//     D = h (2**11 Uh)^T + l Uh^T + h Ul^T = 2**11 x U^T + O(2**-22 |x|)
-// (the l Ul term is below FP32), and the epilogue scales D by 2**-11.
+//     D = h (2**11 Uh)^T + [h Ul^T + l Uh^T] = 2**11 x U^T + O(2**-22 |x|)
+// (the l Ul term is below FP32), the large term and the bracketed
+// corrections in separate FP32 accumulators, and the epilogue adds them and
+// scales by 2**-11.
 // FP16 runs at twice the TF32 rate and halves the operand bytes.  The
 // epilogue reads D from TMEM (tcgen05.ld, one group per thread) and writes
 // the h / l split directly in the operand layout of the next round; after
@@ -339,15 +342,17 @@ __device__ __forceinline__ bool tc_pass_tiles(float *__restrict__ st, const Pass
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (tid == 0) {
-                // D[:, 0:64] = h (2**11 Uh)^T + l Uh^T and D[:, 64:128] = h Ul^T: the h operand is
-                // read once for both of its terms (N = 128 over the stacked images 2**11 Uh | Ul)
+                // D[:, 0:64] = h (2**11 Uh)^T and D[:, 64:128] = h Ul^T + l Uh^T: the h operand is
+                // read once for both of its terms (N = 128 over the stacked images 2**11 Uh | Ul); the
+                // large term's accumulator takes only its own four K steps, the two correction terms
+                // (2**-11 smaller) share the other, and the epilogue adds the two in FP32
                 const uint32_t ah = smem_u32(AH), al = smem_u32(AL), b0 = smem_u32(B);
 #pragma unroll
                 for (int mb = 0; mb < 2; ++mb) {
-                    const uint32_t d = tmem + mb * 128;
                     const uint32_t aoff = mb * (kABytes / 2);
 #pragma unroll
                     for (int term = 0; term < 2; ++term) {
+                        const uint32_t d = tmem + mb * 128 + (term == 0 ? 0u : 64u);
                         const uint32_t a = (term == 0 ? ah : al) + aoff;
                         const uint32_t b = b0 + term * 2 * kBImage;
                         const uint32_t idesc = term == 0 ? kIdesc128 : kIdesc64;

@@ -32,44 +32,27 @@ _COPY_BUFFERS = {}
 _POOL = []
 # Host result memory of large copy-outs, up to two blocks per size (a loop
 # that keeps the previous result while it runs the next alternates between
-# them): touched once by the host threads and page-locked, so later copy-outs
-# go straight from the device into it.  A block is handed out as one numpy
-# array and reused only after that array and every view of it have been
-# released.  Blocks are made only while the host has room for them.
+# them): page-locked (pinned) allocations, so copy-outs go straight from the
+# device into them.  A block is handed out as one numpy array and reused only
+# after that array and every view of it have been released.  Blocks are made
+# only while the host has room for them.
 _RESULT_BLOCKS = {}
 _BLOCKS_PER_SIZE = 2
 
 
 class _ResultBlock:
-    def __init__(self, nbytes):
-        import mmap
-        self.mm = mmap.mmap(-1, nbytes)
+    def __init__(self, nbytes, buf):
         self.nbytes = nbytes
+        self.buf = buf          # page-locked host memory (torch uint8 tensor)
         self.free = True
-        arr = np.frombuffer(self.mm, dtype=np.uint8)
-        parts = [(s0, min(nbytes, s0 + 8 * _HOST_SLICE)) for s0 in range(0, nbytes, 8 * _HOST_SLICE)]
-        list(_host_pool().map(lambda r: arr[r[0]:r[1]].fill(0), parts))     # first touch, in parallel
-        self.ptr = arr.ctypes.data
-        del arr
-        self.pinned = _page_lock(self.ptr, nbytes)
-        self._unlock = _page_unlock
-
-    def __del__(self):
-        # unregister before the mapping can go away (a later mapping may reuse the addresses)
-        if getattr(self, 'pinned', False):
-            try:
-                self._unlock(self.ptr)
-            except Exception:       # interpreter shutdown
-                pass
 
 
-def _page_lock(ptr, nbytes):
-    """Register host memory with CUDA (page-locked, device-copyable); False if refused."""
-    return int(_torch().cuda.cudart().cudaHostRegister(ptr, nbytes, 0)) == 0
-
-
-def _page_unlock(ptr):
-    _torch().cuda.cudart().cudaHostUnregister(ptr)
+def _pinned_host(nbytes):
+    """nbytes of page-locked host memory as a torch uint8 tensor, or None if it cannot be had."""
+    try:
+        return _torch().empty(nbytes, dtype=_torch().uint8, pin_memory=True)
+    except RuntimeError:
+        return None
 
 
 def _release_block(blk):
@@ -102,7 +85,7 @@ def _host_bytes_available():
 
 
 def _result_array(total):
-    """(float64 array of ``total`` values, whether its memory is page-locked) for one copy-out."""
+    """(float64 array of ``total`` values, the page-locked torch view of it or None) for one copy-out."""
     import weakref
     nbytes = total * 8
     blocks = _RESULT_BLOCKS.setdefault(nbytes, [])
@@ -113,14 +96,18 @@ def _result_array(total):
         gc.collect()
         blk = next((b for b in blocks if b.free), None)
     if blk is None:
-        if len(blocks) >= _BLOCKS_PER_SIZE or _host_bytes_available() < 2 * nbytes:
-            return np.empty(total, dtype=np.float64), False     # earlier results still held, or no room
-        blk = _ResultBlock(nbytes)
+        buf = None
+        if len(blocks) < _BLOCKS_PER_SIZE and _host_bytes_available() >= 2 * nbytes:
+            buf = _pinned_host(nbytes)
+        if buf is None:          # earlier results still held, or no room: plain memory
+            return np.empty(total, dtype=np.float64), None
+        blk = _ResultBlock(nbytes, buf)
         blocks.append(blk)
-    arr = np.frombuffer(blk.mm, dtype=np.float64, count=total)
+    host = blk.buf.view(_torch().float64)
+    arr = host.numpy()
     blk.free = False
     weakref.finalize(arr, _release_block, blk)
-    return arr, blk.pinned
+    return arr, host
 
 
 def _copy_buffers(device):
@@ -404,12 +391,11 @@ class DeviceState:
             N.call('dm_chop_copy', self.ptr, self.n, self.dtype, float(chop_threshold),
                    ctypes.c_void_p(out.data_ptr()), self.stream)
             return self._to_host(out)
-        result, direct = _result_array(total)
+        result, host = _result_array(total)
         dev, pinned = _copy_buffers(self.device)
         stream = torch.cuda.current_stream(self.device)
-        if direct:
+        if host is not None:
             # page-locked result: each chunk goes from the device buffer straight into it
-            host = torch.from_numpy(result)
             for i, off in enumerate(range(0, total, _COPY_CHUNK)):
                 b = i % 2
                 cnt = min(_COPY_CHUNK, total - off)

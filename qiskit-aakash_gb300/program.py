@@ -415,9 +415,10 @@ def cx_matrix16(coef, ideal):
 # FP16 3-split of the tensor-core rounds.  Inside a pass the tile is held in
 # scaled units x' = 2**n a (|x'| <= 1 for a physical state), split as
 # x' = h + 2**-11 l with h = fp16(x'), l = fp16(2**11 (x' - h)); the round
-# matrix likewise U = Uh + 2**-11 Ul.  One FP32 accumulator collects
-#     h (2**11 Uh)^T + l Uh^T + h Ul^T = 2**11 (x' U^T) + O(2**-22)
-# and the epilogue multiplies by 2**-11 (exact).
+# matrix likewise U = Uh + 2**-11 Ul.  Two FP32 accumulators collect
+#     h (2**11 Uh)^T   and   h Ul^T + l Uh^T,
+# whose sum is 2**11 (x' U^T) + O(2**-22); the epilogue adds them and
+# multiplies by 2**-11 (exact).
 TC_LO_SCALE = 2048.0
 TC_IMAGE_HALVES = 3 * 4096          # per round: 2**11 Uh, Ul (one 128-row operand), Uh (FP16 bits)
 

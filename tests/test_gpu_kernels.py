@@ -276,10 +276,10 @@ def test_chunked_copy_out_equals_one_shot(torch, dtype, monkeypatch):
     chunked = ds.coefficients(1e-15)                     # page-locked block 1, device -> block copies
     assert np.array_equal(one, chunked)
     blocks = engine._RESULT_BLOCKS[8 * 4 ** n]
-    assert len(blocks) == 1 and blocks[0].pinned and not blocks[0].free
+    assert len(blocks) == 1 and blocks[0].buf.is_pinned() and not blocks[0].free
     second = ds.coefficients(1e-15)                      # block 1 held: block 2
     third = ds.coefficients(1e-15)                       # both held: staging buffers + host copies
-    assert len(blocks) == 2 and blocks[1].pinned
+    assert len(blocks) == 2 and blocks[1].buf.is_pinned()
     for got in (chunked, second, third):
         assert np.array_equal(one, got)
     del second
@@ -289,7 +289,7 @@ def test_chunked_copy_out_equals_one_shot(torch, dtype, monkeypatch):
     again = ds.coefficients(1e-15)                       # released block 2 is reused
     assert np.array_equal(one, again) and not blocks[1].free
     del chunked, third, again
-    engine._RESULT_BLOCKS.pop(8 * 4 ** n)               # unregistered when dropped
+    engine._RESULT_BLOCKS.pop(8 * 4 ** n)
     gc.collect()
     with pytest.raises(N.NativeError):
         out = torch.empty(10, dtype=torch.float64, device='cuda')
