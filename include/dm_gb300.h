@@ -295,6 +295,19 @@ int dm_batch_run_params(int dtype, const dm_param_program *host, const dm_param_
                         const double *params_dev, int params_stride, int ninst, void *states_dev,
                         size_t states_count, double *probs_dev, size_t probs_count, int *counter_dev, void *stream);
 
+/* dm_batch_run_params with every pass on the tensor cores (FP32, 7 <= n <=
+ * 12): the passes are tensor-core passes (passes_host / passes_dev, npasses
+ * = host->npasses; host->passes is not read), op o of each pass with moff =
+ * 16 o.  Per instance and pass the slots' recipe chains are composed in FP64,
+ * then the round matrices from them (as in dm_batch_run_tc) into scratch_dev
+ * (dm_batch_tc_scratch_bytes), then the tiles run.  status_dev is set to 1
+ * if a bounded tensor-core wait gives up. */
+int dm_batch_run_params_tc(const dm_param_program *host, const dm_param_program *dev,
+                           const dm_batch_tc_pass *passes_host, const dm_batch_tc_pass *passes_dev,
+                           const double *params_dev, int params_stride, int ninst, float *states_dev,
+                           size_t states_count, double *probs_dev, size_t probs_count, int *counter_dev,
+                           void *scratch_dev, size_t scratch_bytes, int *status_dev, void *stream);
+
 /* ---------------------------------------------------------- noise surrogate
  *
  * No counterpart in the reference.  A small MLP ensemble learns the map from

@@ -181,6 +181,9 @@ SIGNATURES = {
     'dm_batch_tc_scratch_bytes': (_sz, []),
     'dm_batch_run_tc': (_i, [_vp, _sz, _vp, _sz, _vp, _sz, ctypes.POINTER(DmBatchInstance), _vp, _i,
                              ctypes.POINTER(DmBatchTcPass), _vp, _i, _vp, _vp, _sz, _vp, _vp]),
+    'dm_batch_run_params_tc': (_i, [ctypes.POINTER(DmParamProgram), ctypes.POINTER(DmParamProgram),
+                                    ctypes.POINTER(DmBatchTcPass), _vp, _vp, _i, _i, _vp, _sz, _vp, _sz, _vp, _vp,
+                                    _sz, _vp, _vp]),
     'dm_batch_run_params': (_i, [_i, ctypes.POINTER(DmParamProgram), ctypes.POINTER(DmParamProgram), _vp, _i, _i,
                                  _vp, _sz, _vp, _sz, _vp, _vp]),
     'dm_mlp_gemm_run': (_i, [ctypes.POINTER(DmMlpGemm), _vp, _vp]),

@@ -208,6 +208,28 @@ class _Plan:
         return out.astype(dtype)
 
 
+def fill_tc_tables(t, pp, layouts):
+    """The conversion and epilogue tables of a 7-axis pass (dm_tc_pass; umoff left 0)."""
+    conv, rtables = P.tc_tables(layouts)
+    for r, q in enumerate(pp.axes):
+        t.axes[r] = q
+    t.nrounds = len(layouts)
+    t.vec0 = conv['vec0']
+    for i in range(8):
+        t.natrow[i] = conv['natrow'][i]
+    for i in range(6):
+        t.natk[i] = conv['natk'][i]
+    for r, rt in enumerate(rtables):
+        for i in range(3):
+            t.rounds[r].digits[i] = rt['digits'][i]
+        t.rounds[r].vec = rt['vec']
+        t.rounds[r].umoff = 0
+        for i in range(8):
+            t.rounds[r].rowc[i] = rt['rowc'][i]
+        for i in range(6):
+            t.rounds[r].kc[i] = rt['kc'][i]
+
+
 class _TcPlan(_Plan):
     """A tensor-core plan shared by instances of one structure: passes of 7
     resident axes, rounds of 3 axes in the digit order their layouts chose;
@@ -226,27 +248,9 @@ class _TcPlan(_Plan):
             if len(rounds) > N.DM_MAX_ROUNDS:
                 raise P.TcPlanError('pass needs %d rounds (> %d)' % (len(rounds), N.DM_MAX_ROUNDS))
             layouts = P._choose_layouts([axes for axes, _ in rounds])
-            conv, rtables = P.tc_tables(layouts)
             bp = N.DmBatchTcPass()
             self._fill(bp.ops, pp, rounds, [L.digits for L in layouts])
-            t = bp.tables
-            for r, q in enumerate(pp.axes):
-                t.axes[r] = q
-            t.nrounds = len(layouts)
-            t.vec0 = conv['vec0']
-            for i in range(8):
-                t.natrow[i] = conv['natrow'][i]
-            for i in range(6):
-                t.natk[i] = conv['natk'][i]
-            for r, rt in enumerate(rtables):
-                for i in range(3):
-                    t.rounds[r].digits[i] = rt['digits'][i]
-                t.rounds[r].vec = rt['vec']
-                t.rounds[r].umoff = 0
-                for i in range(8):
-                    t.rounds[r].rowc[i] = rt['rowc'][i]
-                for i in range(6):
-                    t.rounds[r].kc[i] = rt['kc'][i]
+            fill_tc_tables(bp.tables, pp, layouts)
             self.passes.append(bp)
 
     def table_bytes(self):

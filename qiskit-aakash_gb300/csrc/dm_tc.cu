@@ -613,6 +613,60 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm)
     tc_teardown(c);
 }
 
+// Template sweeps on the tensor cores: per instance and pass, the slots'
+// recipe chains are composed in FP64 (as in the CUDA-core template kernel)
+// into shared memory, the round matrices composed from those coefficients,
+// then the tiles streamed.  Slot s of the program is op s of the
+// concatenated tensor-core passes; op o of a pass reads coef + 16 o.
+constexpr int kCoefOffset = 2 * 64 * kColStride * 8;   // after the two rounds of FP64 columns
+static_assert(kCoefOffset + DM_MAX_PASS_OPS * kCoefStride * 8 <= int(kSmemBytes), "slot coefficients fit");
+
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
+    batch_param_tc_kernel(float *__restrict__ states, double *__restrict__ probs, const dm_param_program P,
+                          const dm_batch_tc_pass *__restrict__ passes, const double *__restrict__ params,
+                          int params_stride, int ninst, int *counter, uint16_t *__restrict__ scratch, int *status) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int64_t hi_off[kTile / 4 / kThreads];
+    __shared__ int abort_s;
+    __shared__ int inst_s;
+    __shared__ Pass ps;
+    __shared__ double prm[DM_PARAMS_MIN_STRIDE];
+    TcCta c{smem, smem + kABytes, smem + 2 * kABytes, &mbar, hi_off, &abort_s, 0, 0, false};
+    tc_setup(c, &tmem_base_s);
+    uint16_t *umats = scratch + int64_t(blockIdx.x) * kScratchHalves;
+    double *coef = reinterpret_cast<double *>(smem + kCoefOffset);
+    const int tid = threadIdx.x;
+    const int n = P.n;
+    for (;;) {
+        if (tid == 0) inst_s = atomicAdd(counter, 1);
+        __syncthreads();
+        const int ii = inst_s;
+        if (ii >= ninst) break;
+        if (tid < DM_PARAMS_MIN_STRIDE) prm[tid] = params[int64_t(ii) * params_stride + tid];
+        float *st = states + (int64_t(ii) << (2 * n));
+        batch_init_zero<float, kThreads>(st, n);   // its barriers also publish prm
+        bool ok = true;
+        int slot_base = 0;
+        for (int pi = 0; pi < P.npasses && ok; ++pi) {
+            const dm_batch_tc_pass &bp = passes[pi];
+            batch_tc_setup(ps, bp, n);
+            for (int o = tid; o < bp.ops.nops; o += kThreads)
+                compose_slot(P, slot_base + o, prm, coef + o * kCoefStride);
+            __syncthreads();
+            compose_rounds(bp.ops, coef, umats, reinterpret_cast<double *>(smem));
+            __threadfence_block();
+            __syncthreads();
+            ok = tc_pass_tiles(st, ps, umats, 0, 1, c, status);
+            slot_base += bp.ops.nops;
+        }
+        if (!ok) break;
+        batch_z_readout<float, kThreads>(st, n, prm[11], probs + (int64_t(ii) << n), reinterpret_cast<double *>(smem));
+    }
+    tc_teardown(c);
+}
+
 }  // namespace tc
 
 }  // namespace dmg
@@ -794,6 +848,52 @@ extern "C" int dm_batch_run_tc(float *states_dev, size_t states_count, double *p
     tc::batch_tc_kernel<<<grid, tc::kThreads, tc::kSmemBytes, s>>>(states_dev, probs_dev, mats_dev, insts_dev, ninst,
                                                                      passes_dev, counter_dev,
                                                                      static_cast<uint16_t *>(scratch_dev), status_dev);
+    count_launch();
+    return launch_status();
+}
+
+extern "C" int dm_batch_run_params_tc(const dm_param_program *host, const dm_param_program *dev,
+                                      const dm_batch_tc_pass *passes_host, const dm_batch_tc_pass *passes_dev,
+                                      const double *params_dev, int params_stride, int ninst, float *states_dev,
+                                      size_t states_count, double *probs_dev, size_t probs_count, int *counter_dev,
+                                      void *scratch_dev, size_t scratch_bytes, int *status_dev, void *stream) {
+    DM_CHECK_ARG(host && dev && passes_host && passes_dev && params_dev && states_dev && probs_dev && counter_dev &&
+                 scratch_dev && status_dev);
+    DM_CHECK_ARG(ninst >= 1 && params_stride >= DM_PARAMS_MIN_STRIDE);
+    if (reinterpret_cast<uintptr_t>(states_dev) & 15 || reinterpret_cast<uintptr_t>(scratch_dev) & 15) return DM_ERR_ARG;
+    const dm_param_program &P = *host;
+    if (P.n < tc::kAxes || P.n > kBatchTcMaxQubits) return DM_ERR_RANGE;
+    if (P.npasses < 1) return DM_ERR_PROGRAM;
+    for (int p = 0; p < P.npasses; ++p) {
+        // op o of a pass reads the o-th 16-value slot of the shared-memory coefficients
+        const dm_batch_pass &o = passes_host[p].ops;
+        if (o.nops < 0 || o.nops > DM_MAX_PASS_OPS) return DM_ERR_PROGRAM;
+        for (int i = 0; i < o.nops; ++i)
+            if (o.ops[i].moff != i * kCoefStride) return DM_ERR_PROGRAM;
+        const int rc = validate_batch_tc_pass(passes_host[p], P.n, int64_t(o.nops) * kCoefStride);
+        if (rc) return rc;
+    }
+    const int rc = validate_param_slots(
+        P, P.npasses, [&](int p) { return int(passes_host[p].ops.nops); },
+        [&](int p, int o) { return passes_host[p].ops.ops[o].kind; });
+    if (rc) return rc;
+    if (host->n != dev->n || host->npasses != dev->npasses || host->nslots != dev->nslots) return DM_ERR_ARG;
+    if (size_t(ninst) * (size_t(1) << (2 * P.n)) > states_count) return DM_ERR_ARG;
+    if (size_t(ninst) * (size_t(1) << P.n) > probs_count) return DM_ERR_ARG;
+    if (scratch_bytes < dm_batch_tc_scratch_bytes()) return DM_ERR_ARG;
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [] {
+        attr_err = cudaFuncSetAttribute(tc::batch_param_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int(tc::kSmemBytes));
+    });
+    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    cudaStream_t s = as_stream(stream);
+    DM_CUDA_TRY(cudaMemsetAsync(counter_dev, 0, sizeof(int), s));
+    const int grid = sm_count() * tc::kCtasPerSm;
+    tc::batch_param_tc_kernel<<<grid, tc::kThreads, tc::kSmemBytes, s>>>(
+        states_dev, probs_dev, *dev, passes_dev, params_dev, params_stride, ninst, counter_dev,
+        static_cast<uint16_t *>(scratch_dev), status_dev);
     count_launch();
     return launch_status();
 }

@@ -726,7 +726,8 @@ class DmSimulatorGPU(_Base):
         end_runtime = time.time()
         self.last_run_stats = {'passes': self._dev.passes_run, 'levels': levels,
                                'kernel_launches': N.lib().dm_kernel_launch_count() - launches0,
-                               'h2d_bytes': self._dev.h2d_bytes, 'd2h_bytes': self._dev.d2h_bytes}
+                               'h2d_bytes': self._dev.h2d_bytes, 'd2h_bytes': self._dev.d2h_bytes,
+                               'copy_out': dict(getattr(self._dev, 'copy_stats', {}))}
         if self._record_next:
             self.recorded_state = self._dev
             self._record_next = False

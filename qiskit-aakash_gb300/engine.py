@@ -166,6 +166,7 @@ class DeviceState:
         self.h2d_bytes = 0
         self.d2h_bytes = 0
         self.tape = None          # list of recorded C-ABI calls (see record())
+        self.copy_stats = {}      # the last large copy-out: seconds, whether it went into a result block
         self._keep_alive = []
 
     # -- recording -----------------------------------------------------------
@@ -391,7 +392,10 @@ class DeviceState:
             N.call('dm_chop_copy', self.ptr, self.n, self.dtype, float(chop_threshold),
                    ctypes.c_void_p(out.data_ptr()), self.stream)
             return self._to_host(out)
+        import time
+        t0 = time.perf_counter()
         result, host = _result_array(total)
+        self.copy_stats = {'result_block': host is not None, 'block_seconds': time.perf_counter() - t0}
         dev, pinned = _copy_buffers(self.device)
         stream = torch.cuda.current_stream(self.device)
         if host is not None:
@@ -404,6 +408,7 @@ class DeviceState:
                 host[off:off + cnt].copy_(dev[b][:cnt], non_blocking=True)
             stream.synchronize()
             self.d2h_bytes += total * 8
+            self.copy_stats['seconds'] = time.perf_counter() - t0
             return result
         events = [None, None]
         pending = None
@@ -429,6 +434,7 @@ class DeviceState:
             pending = (b, off, cnt)
         drain(pending)
         self.d2h_bytes += total * 8
+        self.copy_stats['seconds'] = time.perf_counter() - t0
         return result
 
     def raw_coefficients(self):

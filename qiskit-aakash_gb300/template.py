@@ -50,7 +50,7 @@ def param_vector(options):
 class TemplateProgram:
     """Host tables of one template: passes, slots, recipe chains, recipes, constants."""
 
-    def __init__(self, experiment, options, precision='single', kmax=None, probe_options=None):
+    def __init__(self, experiment, options, precision='single', kmax=None, probe_options=None, tensor_cores=None):
         from .batch import compile_experiment
         self.precision = precision
         self.dtype = N.DM_F32 if precision == 'single' else N.DM_F64
@@ -101,7 +101,68 @@ class TemplateProgram:
         self.nrecipes = len(recipes)
         self.consts = np.concatenate(consts) if consts else np.zeros(16)
         self.nconsts = len(consts) * 16
-        self._plan(rec.ops, n, min((kmax or {}).get(n, 7 if precision == 'single' else 6), n), width)
+        if tensor_cores is None:        # FP32 templates of >= 9 qubits run faster on the tensor cores
+            tensor_cores = precision == 'single' and n >= 9
+        if tensor_cores and (precision != 'single' or n < P.TC_AXES):
+            raise BasicAerError('tensor-core template sweeps need FP32 and >= %d qubits' % P.TC_AXES)
+        self.tc = False
+        if tensor_cores:
+            try:
+                self._plan_tc(rec.ops, n)
+                self.tc = True
+            except P.TcPlanError:       # a pass with more rounds than a table holds: the CUDA-core plan
+                pass
+        if not self.tc:
+            self._plan(rec.ops, n, min((kmax or {}).get(n, 7 if precision == 'single' else 6), n), width)
+
+    def _plan_tc(self, ops, n):
+        """Tensor-core passes: 7 resident axes, rounds in their layouts' digit order; op o of a pass
+        reads the o-th 16-value slot of the coefficients the kernel composes per pass."""
+        from .batch import fill_tc_tables
+        passes, slots, chain = [], [], []
+        for p in P.plan_passes(ops, n, P.TC_AXES, 2):
+            pp = P.pad_pass(p, n)
+            rounds = P.plan_rounds(pp, 3, pad='neighbors')
+            if len(rounds) > N.DM_MAX_ROUNDS:
+                raise P.TcPlanError('pass needs %d rounds (> %d)' % (len(rounds), N.DM_MAX_ROUNDS))
+            layouts = P._choose_layouts([axes for axes, _ in rounds])
+            bp = N.DmBatchTcPass()
+            o = bp.ops
+            o.k = len(pp.axes)
+            for r, q in enumerate(pp.axes):
+                o.axes[r] = q
+            o.nrounds = len(rounds)
+            idx = 0
+            for ri, ((_, rops), L) in enumerate(zip(rounds, layouts)):
+                digits = list(L.digits)
+                for i, a in enumerate(digits):
+                    o.round_axes[ri][i] = a
+                o.round_axes[ri][3] = -1
+                for op in rops:
+                    d = o.ops[idx]
+                    d.a = op.axes[0]
+                    d.moff = idx * 16
+                    flags = digits.index(op.axes[0]) << 8
+                    if op.kind == 'map1':
+                        d.kind = N.DM_OP_MAP1
+                        d.b = 0
+                    else:
+                        d.kind = N.DM_OP_CX if op.kind == 'cx' else N.DM_OP_DIAG2
+                        d.b = op.axes[1]
+                        flags |= digits.index(op.axes[1]) << 12
+                    d.flags = flags
+                    slots.append((len(chain), len(op.src)))
+                    chain.extend(op.src)
+                    idx += 1
+                o.round_end[ri] = idx
+            o.nops = idx
+            fill_tc_tables(bp.tables, pp, layouts)
+            passes.append(bp)
+        self.passes = (N.DmBatchTcPass * len(passes))(*passes)
+        self.npasses = len(passes)
+        self.slots = (N.DmParamSlot * len(slots))(*[N.DmParamSlot(b, l) for b, l in slots])
+        self.nslots = len(slots)
+        self.chain = np.asarray(chain, dtype=np.int32)
 
     def _plan(self, ops, n, k, width):
         passes, slots, chain = [], [], []
@@ -160,7 +221,7 @@ class TemplateProgram:
         P_ = N.DmParamProgram()
         P_.n, P_.npasses, P_.nslots = self.n, self.npasses, self.nslots
         P_.nchain, P_.nrecipes, P_.nconsts = self.chain.size, self.nrecipes, self.nconsts
-        P_.passes = ctypes.cast(self.passes, ctypes.c_void_p)
+        P_.passes = None if self.tc else ctypes.cast(self.passes, ctypes.c_void_p)
         P_.slots = ctypes.cast(self.slots, ctypes.c_void_p)
         P_.chain = self.chain.ctypes.data_as(ctypes.c_void_p)
         P_.recipes = ctypes.cast(self.recipes, ctypes.c_void_p)
@@ -187,6 +248,11 @@ class TemplateRunner:
                       up(program.recipes), torch.from_numpy(program.consts.copy()).to(dev)]
         d = program.host_struct()
         d.passes, d.slots, d.chain, d.recipes, d.consts = [b.data_ptr() for b in self._bufs]
+        if program.tc:
+            d.passes = None
+            self.tc_passes_dev = self._bufs[0]
+            self.scratch = torch.empty(N.lib().dm_batch_tc_scratch_bytes(), dtype=torch.uint8, device=dev)
+            self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.dev_struct = d
         self.host = program.host_struct()
         esize = 4 if program.dtype == N.DM_F32 else 8
@@ -212,9 +278,20 @@ class TemplateRunner:
         stream = torch.cuda.current_stream(self.device)
         for s0 in range(0, S, c):
             k = min(c, S - s0)
+            if self.p.tc:
+                N.call('dm_batch_run_params_tc', ctypes.byref(self.host), ctypes.byref(self.dev_struct),
+                       self.p.passes, ctypes.c_void_p(self.tc_passes_dev.data_ptr()),
+                       ctypes.c_void_p(prm[s0].data_ptr()), prm.shape[1], k, ctypes.c_void_p(self.states.data_ptr()),
+                       ctypes.c_size_t(self.states.numel()), ctypes.c_void_p(out[s0].data_ptr()),
+                       ctypes.c_size_t(k * npr), ctypes.c_void_p(self.counter.data_ptr()),
+                       ctypes.c_void_p(self.scratch.data_ptr()), ctypes.c_size_t(self.scratch.numel()),
+                       ctypes.c_void_p(self.status.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+                continue
             N.call('dm_batch_run_params', self.p.dtype, ctypes.byref(self.host), ctypes.byref(self.dev_struct),
                    ctypes.c_void_p(prm[s0].data_ptr()), prm.shape[1], k, ctypes.c_void_p(self.states.data_ptr()),
                    ctypes.c_size_t(self.states.numel()), ctypes.c_void_p(out[s0].data_ptr()),
                    ctypes.c_size_t(k * npr), ctypes.c_void_p(self.counter.data_ptr()),
                    ctypes.c_void_p(stream.cuda_stream))
+        if self.p.tc and int(self.status.item()) != 0:
+            raise BasicAerError('a tensor-core template pass abandoned a bounded wait')
         return out

@@ -73,6 +73,62 @@ def test_template_sweep_equals_batched_instances():
     DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
 
 
+def test_tensor_core_template_sweep_matches_oracle_and_cuda_core_form():
+    """FP32 template of 9 qubits on the tensor cores: every instance vs the oracle, and vs the
+    CUDA-core template form of the same program."""
+    n, layers = 9, 6
+    qc = random_layer_circuit(n, layers, seed=4)
+    raw = S.sample_noise(12, seed=3)
+    tc = TP.TemplateProgram(qc.to_experiment(), S.options_of(raw[0]), 'single')
+    cc = TP.TemplateProgram(qc.to_experiment(), S.options_of(raw[0]), 'single', tensor_cores=False)
+    assert tc.tc and not cc.tc
+    runner = TP.TemplateRunner(tc, max_states_bytes=5 * 4 ** n * 4)      # three chunks
+    got = runner.run(S.param_vectors(raw)).cpu().numpy()
+    ref = TP.TemplateRunner(cc).run(S.param_vectors(raw)).cpu().numpy()
+    assert int(runner.status.item()) == 0
+    for i in range(len(raw)):
+        res = O.OracleDmSimulator(dict(S.options_of(raw[i]), compute_densitymatrix=False)).run_experiment(
+            qc.to_experiment())
+        want = np.array([res['data']['ensemble_probability'][k] for k in O.bitstring_keys(n)])
+        assert np.max(np.abs(got[i] - want)) < 2e-6, i
+        assert np.max(np.abs(got[i] - ref[i])) < 2e-6, i
+
+
+def test_tensor_core_template_rejects_bad_tables():
+    torch = _torch()
+    n = 9
+    qc = random_layer_circuit(n, 3, seed=1)
+    raw = S.sample_noise(2, seed=1)
+    prog = TP.TemplateProgram(qc.to_experiment(), S.options_of(raw[0]), 'single')
+    runner = TP.TemplateRunner(prog)
+    prm = torch.as_tensor(S.param_vectors(raw), dtype=torch.float64).cuda()
+    states = torch.empty(2 * 4 ** n, dtype=torch.float32, device='cuda')
+    out = torch.empty(2 * 2 ** n, dtype=torch.float64, device='cuda')
+    vp = ctypes.c_void_p
+
+    def call(passes):
+        N.call('dm_batch_run_params_tc', ctypes.byref(runner.host), ctypes.byref(runner.dev_struct), passes,
+               vp(runner.tc_passes_dev.data_ptr()), vp(prm.data_ptr()), prm.shape[1], 2, vp(states.data_ptr()),
+               ctypes.c_size_t(states.numel()), vp(out.data_ptr()), ctypes.c_size_t(out.numel()),
+               vp(runner.counter.data_ptr()), vp(runner.scratch.data_ptr()), ctypes.c_size_t(runner.scratch.numel()),
+               vp(runner.status.data_ptr()), None)
+
+    bad = (N.DmBatchTcPass * prog.npasses).from_buffer_copy(bytes(prog.passes))
+    bad[0].ops.ops[1].moff = 0                       # op 1 must read coefficient slot 1
+    with pytest.raises(N.NativeError) as e:
+        call(bad)
+    assert e.value.code == N.DM_ERR_PROGRAM
+    bad = (N.DmBatchTcPass * prog.npasses).from_buffer_copy(bytes(prog.passes))
+    bad[0].ops.nops -= 1                             # slots no longer line up with the ops
+    bad[0].ops.round_end[bad[0].ops.nrounds - 1] -= 1
+    with pytest.raises(N.NativeError) as e:
+        call(bad)
+    assert e.value.code == N.DM_ERR_PROGRAM
+    call(prog.passes)                                # the good tables run
+    torch.cuda.synchronize()
+    assert int(runner.status.item()) == 0
+
+
 def _gemm(epi, A, Bm, members, bias=None, pre=None, want_f32=True, want_bf=False, want_t=False):
     torch = _torch()
     M, K = A.shape[1], A.shape[2]

@@ -58,6 +58,9 @@ def emulate(prog, prm):
     slot = 0
     for p in range(prog.npasses):
         bp = prog.passes[p]
+        if isinstance(bp, N.DmBatchTcPass):
+            bp = bp.ops
+            assert all(bp.ops[o].moff == 16 * o for o in range(bp.nops))
         axes = [bp.axes[r] for r in range(bp.k)]
         for o in range(bp.nops):
             d = bp.ops[o]
@@ -88,6 +91,23 @@ def test_template_program_replay_equals_oracle(precision, n, layers):
     qc = random_layer_circuit(n, layers, seed=7)
     prog = TP.TemplateProgram(qc.to_experiment(), instance_options(rng), precision)
     for _ in range(3):
+        opts = instance_options(rng)
+        prm = TP.param_vector(opts)
+        want = O.OracleDmSimulator(dict(opts, compute_densitymatrix=False)).run_experiment(qc.to_experiment())
+        want = np.array([want['data']['ensemble_probability'][k] for k in O.bitstring_keys(n)])
+        assert np.max(np.abs(emulate(prog, prm) - want)) < 1e-12
+
+
+def test_tensor_core_template_program_replay_equals_oracle():
+    """FP32 templates of >= 9 qubits are planned for the tensor cores (7 resident axes, rounds in
+    their layouts' digit order, op o of a pass on coefficient slot o)."""
+    n, layers = 9, 3
+    rng = np.random.default_rng(77)
+    qc = random_layer_circuit(n, layers, seed=3)
+    prog = TP.TemplateProgram(qc.to_experiment(), instance_options(rng), 'single')
+    assert prog.tc and isinstance(prog.passes[0], N.DmBatchTcPass)
+    assert not TP.TemplateProgram(qc.to_experiment(), instance_options(rng), 'single', tensor_cores=False).tc
+    for _ in range(2):
         opts = instance_options(rng)
         prm = TP.param_vector(opts)
         want = O.OracleDmSimulator(dict(opts, compute_densitymatrix=False)).run_experiment(qc.to_experiment())
