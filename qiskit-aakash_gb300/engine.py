@@ -8,6 +8,7 @@ passes and each pass is one launch of the library's pass kernel.  Every
 numerical step runs in libdmgb300.so; there is no host fallback.
 """
 import ctypes
+import time
 
 import numpy as np
 
@@ -392,7 +393,6 @@ class DeviceState:
             N.call('dm_chop_copy', self.ptr, self.n, self.dtype, float(chop_threshold),
                    ctypes.c_void_p(out.data_ptr()), self.stream)
             return self._to_host(out)
-        import time
         t0 = time.perf_counter()
         result, host = _result_array(total)
         self.copy_stats = {'result_block': host is not None, 'block_seconds': time.perf_counter() - t0}

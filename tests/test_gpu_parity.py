@@ -163,3 +163,23 @@ def test_tensor_core_round_overflow_falls_back_to_the_cuda_core_pass():
     ref = _oracle(qc.to_experiment(), opts)
     got, _ = run_gpu(qc.to_experiment(), opts, precision='single')
     _assert_close(got, ref, n, 2e-5)
+
+
+@pytest.mark.parametrize('precision', ['double', 'single'])
+def test_streamed_launches_equal_one_flush(precision, monkeypatch):
+    """The engine launches passes while the run loop still queues operations; with a tiny streaming
+    threshold (many partial flushes) the state is bit for bit the one of launching everything at the
+    first read-out, and both match the oracle."""
+    from qiskit_aakash_gb300 import engine
+    n = 9
+    qc = dmg.random_layer_circuit(n, 4, 21, barrier_after_gate=True)
+    opts = dmg.noise_options(depolarisation=1e-3, decoherence=0.995, decay=0.998, rotation_sigma=1e-3)
+    opts['compute_densitymatrix'] = False
+    monkeypatch.setattr(engine, 'STREAM_OPS', 10 ** 9)
+    whole, b1 = run_gpu(qc.to_experiment(), opts, precision=precision)
+    monkeypatch.setattr(engine, 'STREAM_OPS', 40)
+    streamed, b2 = run_gpu(qc.to_experiment(), opts, precision=precision)
+    assert b1.last_run_stats['passes'] == b2.last_run_stats['passes']
+    assert np.array_equal(whole['data']['coeffmatrix'], streamed['data']['coeffmatrix'])
+    ref = _oracle(qc.to_experiment(), opts)
+    _assert_close(streamed, ref, n, 1e-12 if precision == 'double' else 2e-5)
