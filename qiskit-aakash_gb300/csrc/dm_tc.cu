@@ -140,12 +140,23 @@ __device__ __forceinline__ void split2(float a, float b, uint32_t &h2, uint32_t 
     l2 = *reinterpret_cast<const uint32_t *>(&ll);
 }
 
-// four values adjacent in K: one 64-bit store into each image
+// The same split of accumulator values a = 2**11 x: h = fp16(2**-11 a) and
+// l = fp16(a - 2**11 h), one FMA, exact (a - 2**11 h = 2**11 (x - h) is an
+// FP32 number), so the result equals split2(2**-11 a, 2**-11 b) bit for bit.
+__device__ __forceinline__ void split2_acc(float a, float b, uint32_t &h2, uint32_t &l2) {
+    const __half2 hh = __floats2half2_rn(a * kLoUnscale, b * kLoUnscale);
+    const float2 hf = __half22float2(hh);
+    const __half2 ll = __floats2half2_rn(fmaf(-kLoScale, hf.x, a), fmaf(-kLoScale, hf.y, b));
+    h2 = *reinterpret_cast<const uint32_t *>(&hh);
+    l2 = *reinterpret_cast<const uint32_t *>(&ll);
+}
+
+// four accumulator values adjacent in K: one 64-bit store into each image
 __device__ __forceinline__ void put_split4(unsigned char *AH, unsigned char *AL, uint32_t o, float a, float b,
                                            float c, float d) {
     uint32_t h0, l0, h1, l1;
-    split2(a, b, h0, l0);
-    split2(c, d, h1, l1);
+    split2_acc(a, b, h0, l0);
+    split2_acc(c, d, h1, l1);
     *reinterpret_cast<uint2 *>(AH + o) = make_uint2(h0, h1);
     *reinterpret_cast<uint2 *>(AL + o) = make_uint2(l0, l1);
 }
@@ -185,7 +196,7 @@ __device__ __forceinline__ void store_all(const float (&v)[64], int vec, uint32_
 #pragma unroll
         for (int j = 0; j < 64; j += 2) {   // conversions in pairs, 16-bit stores
             uint32_t h2, l2;
-            split2(v[j], v[j + 1], h2, l2);
+            split2_acc(v[j], v[j + 1], h2, l2);
             const uint32_t o0 = base ^ t[0][j & 3] ^ t[1][(j >> 2) & 3] ^ t[2][j >> 4];
             const uint32_t o1 = o0 ^ t[0][(j & 3) ^ 1] ^ t[0][j & 3];
             *reinterpret_cast<unsigned short *>(AH + o0) = (unsigned short)(h2 & 0xFFFFu);
@@ -404,9 +415,7 @@ __device__ __forceinline__ bool tc_pass_tiles(float *__restrict__ st, const Pass
                 tcg::tmem_ld32_pair_add(ta + 32, ta + 96, v + 32);
                 const uint32_t base = xor_bits<8>(uint32_t((tid & 127) + 128 * mb), R.rowc);
                 if (!last) {
-#pragma unroll
-                    for (int j = 0; j < 64; ++j) v[j] *= kLoUnscale;
-                    store_all<true>(v, R.vec, base, tk, AH, AL);
+                    store_all<true>(v, R.vec, base, tk, AH, AL);   // split from the accumulator scale
                 } else {
                     const float down = p.down * kLoUnscale;   // back to coefficients
 #pragma unroll
