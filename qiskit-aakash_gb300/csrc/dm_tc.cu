@@ -73,8 +73,6 @@ using tcg::cp_async_commit;
 using tcg::cp_async_wait_all;
 using tcg::mbar_wait;
 using tcg::smem_u32;
-using tcg::tmem_ld16;
-using tcg::tmem_ld64;
 
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) { return tcg::smem_desc(saddr, kLBO, kSBO); }
 
