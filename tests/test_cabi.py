@@ -113,3 +113,54 @@ def test_malformed_pass_is_rejected_on_host(lib):
     p.k = 8                                            # beyond DM_MAX_TILE_AXES
     rc = lib.dm_apply_pass(ctypes.c_void_p(16), 9, 0, ctypes.byref(p), ctypes.c_void_p(16), 16, None)
     assert rc == N.DM_ERR_PROGRAM
+
+
+def test_malformed_tensor_core_batch_tables_are_rejected_on_host(lib):
+    """dm_batch_run_tc / dm_batch_run_params_tc validate every table before any CUDA call."""
+    from qiskit_aakash_gb300 import batch as B
+    from qiskit_aakash_gb300 import template as TP
+    from qiskit_aakash_gb300.circuit import noise_options, random_layer_circuit
+    specs = B.sweep_specs(2, seed=4, n_range=(8, 8), depth_range=(2, 3))
+    t = B.BatchTables(specs, 'single', kmax={8: B.TC}, workers=1)
+    tc = t.tc
+    dev = ctypes.c_void_p(1 << 20)                     # never dereferenced: validation fails first
+
+    def run(insts, passes):
+        return lib.dm_batch_run_tc(dev, t.states_count, dev, t.probs_count, dev, tc.mats.size, insts, dev,
+                                   tc.ninst, passes, dev, tc.npasses, dev, dev, 1 << 40, dev, None)
+
+    def fresh():
+        return (N.DmBatchTcPass * tc.npasses).from_buffer_copy(bytes(tc.passes))
+
+    bad = fresh()
+    bad[0].ops.round_axes[0][1] = bad[0].ops.round_axes[0][0]          # a digit twice
+    assert run(tc.insts, bad) == N.DM_ERR_PROGRAM
+    bad = fresh()
+    bad[0].ops.ops[0].moff = 10 ** 6                                    # beyond the coefficient block
+    assert run(tc.insts, bad) == N.DM_ERR_PROGRAM
+    bad = fresh()
+    bad[0].tables.natrow[0] = 0
+    assert run(tc.insts, bad) == N.DM_ERR_PROGRAM
+    insts = (N.DmBatchInstance * tc.ninst).from_buffer_copy(bytes(tc.insts))
+    insts[0].n = 13
+    assert run(insts, tc.passes) == N.DM_ERR_RANGE
+    insts = (N.DmBatchInstance * tc.ninst).from_buffer_copy(bytes(tc.insts))
+    insts[0].state_off = t.states_count
+    assert run(insts, tc.passes) == N.DM_ERR_ARG
+
+    qc = random_layer_circuit(9, 2, seed=1)
+    opts = noise_options(depolarisation=1e-3, decoherence=0.99, decay=0.99, rotation_sigma=1e-2)
+    prog = TP.TemplateProgram(qc.to_experiment(), opts, 'single')
+    assert prog.tc
+    host = prog.host_struct()
+
+    def run_params(passes):
+        return lib.dm_batch_run_params_tc(ctypes.byref(host), ctypes.byref(host), passes, dev, dev, 16, 1, dev,
+                                          4 ** 9, dev, 2 ** 9, dev, dev, 1 << 40, dev, None)
+
+    bad = (N.DmBatchTcPass * prog.npasses).from_buffer_copy(bytes(prog.passes))
+    bad[0].ops.ops[0].moff = 16                                         # op 0 must read slot 0
+    assert run_params(bad) == N.DM_ERR_PROGRAM
+    bad = (N.DmBatchTcPass * prog.npasses).from_buffer_copy(bytes(prog.passes))
+    bad[0].ops.ops[0].kind = N.DM_OP_CX if bad[0].ops.ops[0].kind == N.DM_OP_MAP1 else N.DM_OP_MAP1
+    assert run_params(bad) == N.DM_ERR_PROGRAM                          # slot recipe no longer fits the op
