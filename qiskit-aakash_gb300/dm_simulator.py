@@ -415,9 +415,7 @@ class DmSimulatorGPU(_Base):
     # ------------------------------------------------------------- operations
     def _add_unitary_single(self, gate, qubit):
         """dm_simulator.py:367-384: the u1/u3 rotations as one composed 4x4 map."""
-        m = np.eye(4)
-        for axis, angle in gate:
-            m = P.rotation_ptm(axis, angle, self._error_params['one_qubit_gates'][axis]) @ m
+        m = P.rotations_ptm(gate, self._error_params['one_qubit_gates'])
         self._dev.map1(qubit, m, tag=('rot', tuple((axis, float(angle)) for axis, angle in gate)))
 
     def _add_unitary_two(self, qubit0, qubit1):
@@ -430,7 +428,7 @@ class DmSimulatorGPU(_Base):
     def _add_decoherence_and_amp_decay(self, level, f, p, g):
         """dm_simulator.py:397-425: memory noise on every qubit."""
         m = P.noise_ptm(f, p, g)
-        if np.array_equal(m, np.eye(4)):
+        if np.array_equal(m, P.IDENTITY4):
             return
         for q in range(self._number_of_qubits):
             self._dev.map1(q, m, tag=('noise',))

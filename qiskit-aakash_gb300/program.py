@@ -55,6 +55,26 @@ def rotation_ptm(axis, angle, err):
     return m
 
 
+def rotations_ptm(gate, errors):
+    """4x4 map of the rotations [(axis, angle), ...] applied in order, each with its axis's
+    error (<cos>, mean) from ``errors`` (basicaertools.py:106-124): rotation_ptm(...) @ ... @ I
+    composed on plain floats (a rotation mixes two rows), one array at the end."""
+    m = [[1.0, 0.0, 0.0, 0.0], [0.0, 1.0, 0.0, 0.0], [0.0, 0.0, 1.0, 0.0], [0.0, 0.0, 0.0, 1.0]]
+    for axis, angle in gate:
+        planes = _ROT_PLANES.get(axis)
+        if planes is None:
+            from .exceptions import QiskitError
+            raise QiskitError('Gate is not among the valid decomposition types: %s' % axis)
+        e0, e1 = errors[axis][0], errors[axis][1]
+        c = e0 * math.cos(angle + e1)
+        s = e0 * math.sin(angle + e1)
+        k0, k1 = planes
+        r0, r1 = m[k0], m[k1]
+        m[k0] = [c * a - s * b for a, b in zip(r0, r1)]
+        m[k1] = [s * a + c * b for a, b in zip(r0, r1)]
+    return np.array(m)
+
+
 def u_gate_ptm(name, params, rotation_error):
     """u1 / u3 as the product of its rotations (basicaertools.py:69-90)."""
     p = [float(x) for x in params]
