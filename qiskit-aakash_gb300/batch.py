@@ -292,7 +292,7 @@ def instance_experiment(spec):
     qc = random_layer_circuit(spec['n'], spec['depth'], spec['seed'])
     opts = noise_options(depolarisation=spec['depolarisation'], decoherence=spec['decoherence'],
                          decay=spec['decay'])
-    return qc.to_experiment(), opts
+    return qc.to_experiment(copy=False), opts
 
 
 def _structure(spec):

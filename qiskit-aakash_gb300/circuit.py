@@ -166,9 +166,11 @@ class QuantumCircuit:
         return self
 
     # -- qobj ----------------------------------------------------------------
-    def to_experiment(self):
-        return QobjExperiment([_clone(i) for i in self.instructions], self.n_qubits,
-                              self.n_clbits, name=self.name)
+    def to_experiment(self, copy=True):
+        """The circuit as a qobj experiment; ``copy=False`` hands over the instructions
+        themselves (for a circuit that is not used again)."""
+        insts = [_clone(i) for i in self.instructions] if copy else list(self.instructions)
+        return QobjExperiment(insts, self.n_qubits, self.n_clbits, name=self.name)
 
     def to_qobj(self):
         return Qobj([self.to_experiment()])

@@ -427,9 +427,14 @@ class DmSimulatorGPU(_Base):
 
     def _add_decoherence_and_amp_decay(self, level, f, p, g):
         """dm_simulator.py:397-425: memory noise on every qubit."""
-        m = P.noise_ptm(f, p, g)
-        if np.array_equal(m, P.IDENTITY4):
+        key = (f, p, g)
+        cached = getattr(self, '_noise_map', None)
+        if cached is None or cached[0] != key:     # the same map every level of a run
+            m = P.noise_ptm(f, p, g)
+            cached = self._noise_map = (key, m, np.array_equal(m, P.IDENTITY4))
+        if cached[2]:
             return
+        m = cached[1]
         for q in range(self._number_of_qubits):
             self._dev.map1(q, m, tag=('noise',))
 
