@@ -341,6 +341,48 @@ def test_fp16_three_way_split_accuracy():
     assert np.max(np.abs(D - x @ U.T)) < 2e-6 * np.abs(x @ U.T).max()
 
 
+def _tc_split_round(st, n, qubits, U):
+    """One tensor-core round in numpy: the state (units of 2**-n, FP32 between rounds) split into
+    FP16 h / l, U into Uh / Ul, products exact, FP32 rounding of the sum."""
+    perm = [q for q in range(n) if q not in qubits] + [qubits[2], qubits[1], qubits[0]]
+    X = np.transpose(st, perm).reshape(-1, 64).astype(np.float32).astype(np.float64)
+    h = X.astype(np.float16).astype(np.float64)
+    lo = ((X - h) * P.TC_LO_SCALE).astype(np.float16).astype(np.float64)
+    uh = U.astype(np.float16).astype(np.float64)
+    ul = ((U - uh) * P.TC_LO_SCALE).astype(np.float16).astype(np.float64)
+    D = ((h @ (P.TC_LO_SCALE * uh).T + (h @ ul.T + lo @ uh.T)) / P.TC_LO_SCALE).astype(np.float32)
+    return np.transpose(D.astype(np.float64).reshape([4] * n), np.argsort(perm))
+
+
+def test_tensor_core_split_model_stays_at_fp32_accuracy_over_a_deep_noisy_circuit():
+    """The 3-way FP16 split with exactly rounded FP32 sums, applied round by round (the planner's
+    rounds, digit orders and composed matrices) to a low-noise 40-layer 8-qubit circuit, stays
+    within 1e-6 TV of exact FP64 application: the split itself is not the accuracy limit."""
+    import copy
+    from qiskit_aakash_gb300 import batch as B
+    spec = dict(B.sweep_specs(1, seed=12, n_range=(8, 8), depth_range=(40, 40))[0],
+                depolarisation=1e-4, decoherence=1 - 1e-4, decay=1 - 1e-4)
+    rec = B.compile_experiment(*B.instance_experiment(spec))
+    n = rec.n
+    exact = np.zeros([4] * n)
+    for m in range(2 ** n):
+        exact[tuple(3 if (m >> (n - 1 - q)) & 1 else 0 for q in range(n))] = 1.0   # |0..0> in units of 2**-n
+    split = exact.copy()
+    for p in P.plan_passes(rec.ops, n, P.TC_AXES, 2):
+        pp, layouts, mats = P.plan_tc_pass(p, n)
+        for L, U in zip(layouts, mats):
+            qubits = [pp.axes[a] for a in L.digits]
+            perm = [q for q in range(n) if q not in qubits] + [qubits[2], qubits[1], qubits[0]]
+            X = np.transpose(exact, perm).reshape(-1, 64)
+            exact = np.transpose((X @ U.T).reshape([4] * n), np.argsort(perm))
+            split = _tc_split_round(split, n, qubits, U)
+    err = rec.readouts[0][3]
+    pe = O.ensemble_probabilities(exact.reshape(-1) * 2.0 ** -n, n, 'Z', None, err)
+    ps = O.ensemble_probabilities(split.reshape(-1) * 2.0 ** -n, n, 'Z', None, err)
+    assert 0.5 * np.abs(pe - ps).sum() < 1e-6
+    assert abs(ps.sum() - 1.0) < 1e-6
+
+
 def test_xy_unital_flag_marks_exactly_the_maps_without_i_in_x_and_y():
     """DM_MAP1_XY_UNITAL is set from the composed matrix itself (a product of such maps need not be one)."""
     n = 6
