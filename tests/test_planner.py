@@ -204,6 +204,22 @@ def test_streamed_planning_gives_the_passes_of_the_whole_stream(n, kmax, low, ch
     assert launched_early > len(whole) // 2     # most passes start before the stream ends
 
 
+def test_streamed_planning_edge_cases():
+    """No ops: nothing launched, nothing left; ops that fit one open pass: all of them stay queued."""
+    assert P.plan_passes([], 6, 4, 2, partial=True) == ([], [])
+    ops = [P.Op('map1', (5,), np.eye(4)), P.Op('map1', (4,), np.eye(4))]
+    done, rest = P.plan_passes(ops, 6, 4, 2, partial=True)
+    assert done == [] and rest == ops
+    # a full pass whose resident axes are all blocked by later ops closes before the end of the queue
+    n = 6
+    ops = [P.Op('map1', (q,), np.eye(4)) for q in (5, 4, 3, 2)]
+    ops += [P.Op('map1', (q,), np.eye(4)) for q in (1, 0)]                     # outside the full pass
+    ops += [P.Op('cx', (1, q), np.array(P.cx_coefficients([1.0, 0.0])[0]), True) for q in (5, 4, 3, 2)]
+    done, rest = P.plan_passes(ops, n, 4, 2, partial=True)
+    assert len(done) == 1 and sorted(done[0].axes) == [2, 3, 4, 5]
+    assert rest == ops[4:]
+
+
 @pytest.mark.parametrize('width', [2, 3])
 @pytest.mark.parametrize('n,kmax,low', [(5, 4, 2), (7, 6, 2), (8, 7, 2), (9, 7, 3)])
 def test_register_rounds_equal_program_order(n, kmax, low, width):
