@@ -48,7 +48,7 @@ import __graft_entry__  # noqa: E402
 
 METRIC = 'gate-layers/s at n=16 (random U3+CX brick layers, full noise after every gate): fused FP32 vs plain FP64'
 NOISE = dict(depolarisation=1e-3, decoherence=0.995, decay=0.998, rotation_sigma=1e-3)
-CPU_SAMPLE_N = 11
+CPU_SAMPLE_N = 12      # one layer at 12 qubits: about 7 s of single-core oracle work on the host
 
 
 def parse():
