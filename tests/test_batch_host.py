@@ -198,3 +198,12 @@ def test_mixed_batch_packs_both_parts():
             pos += size
         assert pos == total
     assert T.swept_bytes(4) == sum(2 * 4 ** I.n * 4 * I.npasses for I in T.all_instances())
+
+
+def test_tensor_core_choice_is_rejected_where_it_cannot_run():
+    specs = B.sweep_specs(2, seed=1, n_range=(6, 6), depth_range=(2, 3))
+    with pytest.raises(Exception):
+        B.BatchTables(specs, 'single', kmax={6: B.TC}, workers=1)       # fewer than 7 qubits
+    specs = B.sweep_specs(2, seed=1, n_range=(8, 8), depth_range=(2, 3))
+    with pytest.raises(Exception):
+        B.BatchTables(specs, 'double', kmax={8: B.TC}, workers=1)       # FP64 runs on the CUDA cores

@@ -128,3 +128,14 @@ def test_param_vector_defaults_and_mapping():
     v = TP.param_vector(noise_options(depolarisation=0.01, decoherence=0.99, decay=0.98, thermal=0.9,
                                       rotation_sigma=0.1, tsp=[0.97, 0.02]))
     assert np.allclose(v[:12], [0.99, 0.9, 0.98] + [math.exp(-0.005), 0] * 3 + [0.97, 0.02, 0.99])
+
+
+def test_tensor_core_template_choice_is_rejected_where_it_cannot_run():
+    rng = np.random.default_rng(3)
+    qc = random_layer_circuit(5, 2, seed=2)
+    with pytest.raises(Exception):
+        TP.TemplateProgram(qc.to_experiment(), instance_options(rng), 'single', tensor_cores=True)
+    qc9 = random_layer_circuit(9, 2, seed=2)
+    assert not TP.TemplateProgram(qc9.to_experiment(), instance_options(rng), 'double').tc
+    with pytest.raises(Exception):
+        TP.TemplateProgram(qc9.to_experiment(), instance_options(rng), 'double', tensor_cores=True)
