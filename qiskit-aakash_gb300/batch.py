@@ -109,6 +109,89 @@ def compile_experiment(experiment, options):
     return rec
 
 
+def _error_params(options):
+    """The backend's error parameters for ``options`` (pristine class defaults, as compile_experiment)."""
+    from .dm_simulator import DmSimulatorGPU
+    saved = DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error']
+    DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
+    try:
+        b = DmSimulatorGPU()
+        opts = dict(options)
+        opts['compute_densitymatrix'] = False
+        b._set_options(backend_options=opts)
+        b._initialize_errors()
+    finally:
+        DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = saved
+    return b._error_params, b.MERGE
+
+
+def derive_recording(ref, spec):
+    """The recording of sweep instance ``spec`` from ``ref``, the backend's recording of another
+    instance of the same structure (qubits, depth): the same operations in the same order, with
+    this instance's matrices built by the functions the run loop uses (its merged gates'
+    rotations in program order per qubit, its memory noise, its CX error, its read-out
+    polarisation).  None when the instance does not line up with ``ref``; the caller then
+    records it through the run loop."""
+    from .dm_simulator import _u_decomposition
+    from .scheduler import merge_single_gates
+    exp, opts = instance_experiment(spec)
+    n = ref.n
+    if exp.config.n_qubits != n:
+        return None
+    err, merge = _error_params(opts)
+    gates = [[] for _ in range(n)]
+    for inst in merge_single_gates(exp.instructions, n, merge):
+        if inst.name in ('u1', 'u3'):
+            gates[inst.qubits[0]].append(_u_decomposition(inst.name, inst.params))
+    mem = err['memory']
+    noise = P.noise_ptm(mem['decoherence'], mem['thermalization'], mem['amplitude_decay'])
+    if np.array_equal(noise, P.IDENTITY4):
+        return None                    # the run loop records no memory noise then
+    coef, ideal = P.cx_coefficients(err['two_qubit_gates'])
+    rot_err = err['one_qubit_gates']
+    used = [0] * n
+    ops = []
+    for op in ref.ops:
+        if op.kind == 'map1' and op.tag and op.tag[0] == 'rot':
+            q = op.axes[0]
+            if used[q] >= len(gates[q]):
+                return None
+            gate = gates[q][used[q]]
+            used[q] += 1
+            if [a for a, _ in gate] != [a for a, _ in op.tag[1]]:
+                return None
+            ops.append(P.Op('map1', op.axes, P.rotations_ptm(gate, rot_err),
+                            tag=('rot', tuple((a, float(t)) for a, t in gate))))
+        elif op.kind == 'map1' and op.tag == ('noise',):
+            ops.append(P.Op('map1', op.axes, noise, tag=('noise',)))
+        elif op.kind == 'cx':
+            ops.append(P.Op('cx', op.axes, np.array(coef), ideal, tag=('cx',)))
+        else:
+            return None
+    if used != [len(g) for g in gates]:
+        return None
+    rec = HostRecorder(n)
+    rec.init = ref.init
+    rec.ops = ops
+    kind, pos, mode, _ = ref.readouts[0]
+    rec.readouts = [(kind, pos, list(mode), float(err['measurement']))]
+    return rec
+
+
+def record_group(specs):
+    """Recordings of sweep instances of one structure: the first through the backend's run
+    loop, the others derived from it (``derive_recording``) where they line up."""
+    recs, ref = [], None
+    for spec in specs:
+        rec = derive_recording(ref, spec) if ref is not None else None
+        if rec is None:
+            rec = compile_experiment(*instance_experiment(spec))
+            if ref is None:
+                ref = rec
+        recs.append(rec)
+    return recs
+
+
 def _signature(ops):
     return tuple((op.kind, op.axes, op.ideal) for op in ops)
 
@@ -307,7 +390,7 @@ def compile_group(specs, variants):
     bytes, pass count, coefficient count) and per instance (plan index,
     FP64 coefficient block, measurement polarisation).
     """
-    recs = [compile_experiment(*instance_experiment(s)) for s in specs]
+    recs = record_group(specs)
     out = []
     for precision, k in variants:
         np_dtype = np.float32 if precision == 'single' else np.float64

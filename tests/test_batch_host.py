@@ -207,3 +207,35 @@ def test_tensor_core_choice_is_rejected_where_it_cannot_run():
     specs = B.sweep_specs(2, seed=1, n_range=(8, 8), depth_range=(2, 3))
     with pytest.raises(Exception):
         B.BatchTables(specs, 'double', kmax={8: B.TC}, workers=1)       # FP64 runs on the CUDA cores
+
+
+def test_derived_recordings_equal_the_run_loop():
+    """Instances of one structure after the first are derived from its recording; every op (kind,
+    axes, matrix bit for bit) and the read-out equal the backend's own run loop."""
+    specs = B.sweep_specs(400, seed=5)
+    groups = {}
+    for s in specs:
+        groups.setdefault(B._structure(s), []).append(s)
+    checked = 0
+    for key, gs in list(groups.items())[:12]:
+        if len(gs) < 2:
+            continue
+        ref = B.compile_experiment(*B.instance_experiment(gs[0]))
+        for s in gs[1:4]:
+            d = B.derive_recording(ref, s)
+            f = B.compile_experiment(*B.instance_experiment(s))
+            assert d is not None
+            assert d.readouts == f.readouts and len(d.ops) == len(f.ops)
+            for a, b in zip(d.ops, f.ops):
+                assert (a.kind, tuple(a.axes), a.ideal) == (b.kind, tuple(b.axes), b.ideal)
+                assert np.array_equal(np.asarray(a.data), np.asarray(b.data))
+            checked += 1
+    assert checked >= 10
+
+
+def test_derived_recording_refuses_a_different_structure():
+    a, b = B.sweep_specs(2, seed=6, n_range=(7, 7), depth_range=(4, 4))
+    ref = B.compile_experiment(*B.instance_experiment(a))
+    assert B.derive_recording(ref, dict(b, depth=5)) is None          # one more layer of gates
+    assert B.derive_recording(ref, dict(b, n=8)) is None
+    assert B.derive_recording(ref, dict(b, decoherence=1.0, decay=1.0, depolarisation=0.0)) is None
