@@ -157,16 +157,21 @@ def measured_peaks():
         return 6800.0, 'fallback'
 
 
-def profiled_traffic():
-    """Per-launch DRAM bytes of the pass kernel from the committed ncu summary, if any."""
+def profiled_value(key):
+    """A figure of the pass kernel's committed ncu summary ('key: value' line), if any."""
     path = os.path.join(ROOT, 'profiles', 'pass_tc_kernel_fp16_split_fp32_n14.md')
     try:
         for line in open(path):
-            if line.startswith('traffic_bytes_per_launch:'):
+            if line.startswith(key + ':'):
                 return float(line.split(':', 1)[1])
     except OSError:
         pass
     return None
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of the pass kernel from the committed ncu summary, if any."""
+    return profiled_value('traffic_bytes_per_launch')
 
 
 # ---------------------------------------------------------------------------
@@ -637,6 +642,8 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s', 'frac': achieved / hbm,
                      'traffic': traffic, 'kernel': 'pass_tc_kernel (tcgen05 kind::f16, 3-way FP16 split)', 'launches_per_step': len(durs),
                      'mean_launch_ms': mean_pass_ms,
+                     'tensor_pipe_active': profiled_value('tensor_pipe_active'),
+                     'tensor_pipe_source': 'sm__pipe_tensor_cycles_active of the committed ncu capture at n = 14',
                      'algorithmic_bytes_per_launch': 2 * N4 * 4, 'peak_kind': peak_kind},
         'e2e': {'value': world * layers / e2e_s, 'unit': 'gate-layers/s', 'seconds_per_step': e2e_s,
                 'seconds_each': each, 'copy_out_each': copies,
