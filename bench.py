@@ -48,7 +48,7 @@ import __graft_entry__  # noqa: E402
 
 METRIC = 'gate-layers/s at n=16 (random U3+CX brick layers, full noise after every gate): fused FP32 vs plain FP64'
 NOISE = dict(depolarisation=1e-3, decoherence=0.995, decay=0.998, rotation_sigma=1e-3)
-CPU_SAMPLE_N = 12      # one layer at 12 qubits: about 7 s of single-core oracle work on the host
+CPU_SAMPLE_N = 11      # one noisy layer at 11 qubits: about 7 s of single-core reference work on the host
 
 
 def parse():
@@ -66,11 +66,12 @@ def parse():
     ap.add_argument('--no-gate-kinds', action='store_true', help='skip the per-gate-kind bandwidth table')
     ap.add_argument('--batch', type=int, default=4096,
                     help='instances of the batched noise sweep (0 skips the sweep leg)')
-    ap.add_argument('--surrogate-train', type=int, default=131072,
+    ap.add_argument('--surrogate-train', type=int, default=1048576,
                     help='training points of the noise surrogate (0 skips the surrogate leg)')
-    ap.add_argument('--surrogate-test', type=int, default=16384, help='held-out points of the noise surrogate')
-    ap.add_argument('--surrogate-epochs', type=int, default=40)
-    ap.add_argument('--legs', default='headline,batch,surrogate',
+    ap.add_argument('--surrogate-test', type=int, default=65536, help='held-out points of the noise surrogate')
+    ap.add_argument('--surrogate-epochs', type=int, default=20)
+    ap.add_argument('--c2-layers', type=int, default=40, help='random layers after the QFT in the n=14 leg')
+    ap.add_argument('--legs', default='headline,c2,batch,surrogate',
                     help='comma list of legs to run (the JSON line keeps only what ran)')
     ap.add_argument('--no-autotune', action='store_true',
                     help='batched sweep without timing candidates: tensor cores from 9 qubits, 7 resident axes below')
@@ -178,29 +179,53 @@ def profiled_traffic():
 # CPU baseline (the oracle, a numpy restatement of the reference's algorithm)
 # ---------------------------------------------------------------------------
 
+def cpu_simulator():
+    """(kind, factory) of the CPU implementation timed: the reference's own DmSimulatorPy (unmodified,
+    loaded by oracle/refload.py from the reference tree or its byte-compiled copy in oracle/_ref), else
+    the oracle port (a numpy restatement of the same algorithm)."""
+    from oracle import refload
+    if refload.available():
+        dm = refload.load()
+
+        def make(opts):
+            dm.DmSimulatorPy.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
+            b = dm.DmSimulatorPy()
+            b._set_options(qobj_config=None, backend_options=copy.deepcopy(opts))
+            return b
+        return 'reference', make
+    from oracle import dm_oracle
+    return 'port', lambda opts: dm_oracle.OracleDmSimulator(copy.deepcopy(opts))
+
+
 def cpu_sample(pkg, n_full, seed):
-    """Time one noisy random layer of the oracle at CPU_SAMPLE_N qubits; scale to n_full.
+    """Time one noisy random layer of the reference at CPU_SAMPLE_N qubits; scale to n_full.
 
     The reference's work per level is n full-state sweeps of 4**n
     coefficients and a layer has n U3 levels plus the CX levels, so the
-    per-layer time scales by levels(n) * n * 4**n.
+    per-layer time scales by levels(n) * n * 4**n.  The n = 16 workload
+    itself does not fit the reference on the host (a 34 GB state plus a
+    full copy per rotation).
     """
-    from oracle import dm_oracle
+    kind, make = cpu_simulator()
     n = CPU_SAMPLE_N
     qc = pkg.random_layer_circuit(n, 1, seed, barrier_after_gate=True, measure=False)
     opts = pkg.noise_options(**NOISE)
     opts['compute_densitymatrix'] = False
+    sim = make(opts)
     t0 = time.perf_counter()
-    res = dm_oracle.OracleDmSimulator(copy.deepcopy(opts)).run_experiment(qc.to_experiment())
+    res = sim.run_experiment(qc.to_experiment())
     dt = time.perf_counter() - t0
     lv_small = res['number_of_clock_cycles']
     # levels per layer at n_full: n U3 levels + CX levels (n//2 in even, (n-1)//2 in odd layers)
     lv_full = n_full + ((n_full // 2) + ((n_full - 1) // 2)) / 2.0
     scale = (lv_full * n_full * 4.0 ** n_full) / (lv_small * n * 4.0 ** n)
     sec_per_layer_full = dt * scale
-    return {'value': 1.0 / sec_per_layer_full, 'unit': 'gate-layers/s', 'cores': 1, 'kind': 'port',
-            'sample': ('1 noisy random layer at n=%d (%d levels, %.2f s, numpy FP64, 1 thread), scaled to n=%d '
-                       'by levels*n*4^n (x%.0f)' % (n, lv_small, dt, n_full, scale)),
+    what = ('the reference DmSimulatorPy.run_experiment (dm_simulator.py:950-1196, unmodified)' if kind == 'reference'
+            else 'the oracle port')
+    return {'value': 1.0 / sec_per_layer_full, 'unit': 'gate-layers/s', 'cores': 1, 'kind': kind,
+            'sample': ('1 noisy random layer at n=%d through %s (%d levels, %.2f s, numpy FP64, 1 thread), '
+                       'scaled to n=%d by levels*n*4^n (x%.0f); n=%d itself does not fit the reference on the host'
+                       % (n, what, lv_small, dt, n_full, scale, n_full)),
             'sample_seconds': dt}
 
 
@@ -256,22 +281,33 @@ def time_replays(torch, state, steps):
     return start.elapsed_time(end) / steps
 
 
+PASS_KERNELS = {'dm_apply_pass': 'pass_pipe_kernel', 'dm_apply_pass_tc': 'pass_tc_kernel',
+                'dm_apply_pass_tma': 'pass_tma_kernel'}
+
+
 def pass_kernel_profile(torch, state):
-    """Mean duration of the pass-kernel launches of one replay (events on the launching stream)."""
+    """Durations (ms) of the pass-kernel launches of one replay, by kernel (events on the launching stream)."""
     stream = torch.cuda.current_stream()
     marks = []
 
     def on_call(name, before):
-        if name in ('dm_apply_pass', 'dm_apply_pass_tc'):
+        if name in PASS_KERNELS:
             ev = torch.cuda.Event(enable_timing=True)
             ev.record(stream)
-            marks.append(ev)
+            marks.append((name, ev))
 
     torch.cuda.synchronize()
     state.replay(on_call)
     torch.cuda.synchronize()
-    durs = [marks[i].elapsed_time(marks[i + 1]) for i in range(0, len(marks) - 1, 2)]
-    return durs
+    out = {}
+    for i in range(0, len(marks) - 1, 2):
+        name = PASS_KERNELS[marks[i][0]]
+        out.setdefault(name, []).append(marks[i][1].elapsed_time(marks[i + 1][1]))
+    return out
+
+
+def all_durations(by_kernel):
+    return [d for v in by_kernel.values() for d in v]
 
 
 def device_max_abs_diff(torch, a32, b64, chunk=1 << 28):
@@ -520,12 +556,13 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
     seed = args.seed + rank
     qc, opts = workload(pkg, n, layers, seed)
 
-    def backend_for(precision, tensor_cores=True):
+    def backend_for(precision, tensor_cores=True, tma=True):
         DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
         b = DmSimulatorGPU()
         o = copy.deepcopy(opts)
         o['precision'] = precision
         o['tensor_cores'] = tensor_cores
+        o['tma'] = tma
         o['coefficients_to_host'] = False      # compared on the device below
         b._set_options(backend_options=o)
         return b
@@ -536,8 +573,18 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
     stcc = bcc.recorded_state
     stcc.replay()
     ms_cc = time_replays(torch, stcc, 1)
-    durs_cc = pass_kernel_profile(torch, stcc)
+    durs_cc = all_durations(pass_kernel_profile(torch, stcc))
     del stcc, bcc
+    torch.cuda.empty_cache()
+
+    # --- FP32 tensor cores with cp.async-fed tiles only (the previous form), for comparison ----
+    bca = backend_for('single', tma=False)
+    bca.record_experiment(qc.to_experiment())
+    stca = bca.recorded_state
+    stca.replay()
+    ms_ca = time_replays(torch, stca, 1)
+    durs_ca = all_durations(pass_kernel_profile(torch, stca))
+    del stca, bca
     torch.cuda.empty_cache()
 
     # --- fused FP32: record once, then time replays ---------------------------
@@ -555,7 +602,8 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
     launches = (N.lib().dm_kernel_launch_count() - l0)
     barrier(torch, world)
     value32, ms32 = replica_throughput(torch, world, float(layers), ms32)
-    durs = pass_kernel_profile(torch, st32)     # a full replay: leaves the final FP32 state
+    by_kernel = pass_kernel_profile(torch, st32)     # a full replay: leaves the final FP32 state
+    passes_by_kernel = dict(st32.passes_by_kernel)
     prob32 = np.array(list(r32['data']['ensemble_probability'].values()))
 
     # --- plain FP64 (the parity form) ---------------------------------------
@@ -565,7 +613,7 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
     stats64 = dict(b64.last_run_stats)
     st64.replay()
     ms64 = time_replays(torch, st64, args.fp64_steps)
-    durs64 = pass_kernel_profile(torch, st64)
+    durs64 = all_durations(pass_kernel_profile(torch, st64))
     prob64 = np.array(list(r64['data']['ensemble_probability'].values()))
     max_abs = device_max_abs_diff(torch, st32.state, st64.state) * 2.0 ** n
     prob_l1 = float(np.abs(prob32 - prob64).sum())
@@ -603,8 +651,13 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
         return None
     hbm, peak_kind = measured_peaks()
     N4 = 4.0 ** n
+    # the dominant kernel: the most device time of the step's pass launches
+    top = max(by_kernel, key=lambda k: sum(by_kernel[k]))
+    durs = by_kernel[top]
     mean_pass_ms = float(np.mean(durs)) if durs else float('nan')
     achieved = 2 * N4 * 4 / (mean_pass_ms / 1e3) / 1e9
+    kernels = {k: {'launches': len(v), 'total_ms': float(np.sum(v)), 'mean_ms': float(np.mean(v)),
+                   'achieved_gbs': 2 * N4 * 4 / (float(np.mean(v)) / 1e3) / 1e9} for k, v in by_kernel.items()}
     mean_pass64 = float(np.mean(durs64)) if durs64 else float('nan')
     achieved64 = 2 * N4 * 8 / (mean_pass64 / 1e3) / 1e9
     traffic = profiled_traffic()
@@ -636,11 +689,15 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
                             'kernel': 'pass_pipe_kernel<float,3>',
                             'mean_pass_ms': float(np.mean(durs_cc)) if durs_cc else None,
                             'pass_achieved_gbs': (2 * N4 * 4 / (float(np.mean(durs_cc)) / 1e3) / 1e9) if durs_cc else None},
+        'fp32_tc_cp_async': {'value': world * layers / (ms_ca / 1e3), 'unit': 'gate-layers/s', 'ms_per_step': ms_ca,
+                             'kernel': 'pass_tc_kernel only (tiles by cp.async, two CTAs per SM)',
+                             'mean_pass_ms': float(np.mean(durs_ca)) if durs_ca else None},
         'accuracy': {'max_abs_coeff_err': max_abs, 'prob_l1_err': prob_l1,
                      'against': 'FP64 GPU plain form (itself parity-checked against the reference at n<=14)',
                      'coeff_scale': 'Pauli expectations 2^n * a_s'},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s', 'frac': achieved / hbm,
-                     'traffic': traffic, 'kernel': 'pass_tc_kernel (tcgen05 kind::f16, 3-way FP16 split)', 'launches_per_step': len(durs),
+                     'traffic': traffic, 'kernel': top + ' (tcgen05 kind::f16, 3-way FP16 split)',
+                     'launches_per_step': len(durs), 'pass_kernels': kernels, 'passes_by_form': passes_by_kernel,
                      'mean_launch_ms': mean_pass_ms,
                      'tensor_pipe_active': profiled_value('tensor_pipe_active'),
                      'tensor_pipe_source': 'sm__pipe_tensor_cycles_active of the committed ncu capture at n = 14',
@@ -653,6 +710,56 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
         'clocks': clocks.summary(),
     }
     return line
+
+
+def c2_leg(args, pkg, torch, N, DmSimulatorGPU):
+    """The 14-qubit workload: QFT on all qubits, then random layers, full noise after every gate.
+
+    FP64 (the parity form) and FP32 (tensor cores), each recorded once and
+    then replayed with its program resident on the device (CUDA events);
+    per-pass bandwidth against the algorithmic bytes 2 * 4**14 * s per pass,
+    and the FP32 result against the FP64 one on the device."""
+    n, layers = 14, args.c2_layers
+    qc = pkg.random_layer_circuit(n, layers, args.seed, barrier_after_gate=True, qft=True)
+    opts = pkg.noise_options(**NOISE)
+    opts['compute_densitymatrix'] = False
+    hbm, peak_kind = measured_peaks()
+    out = {'workload': 'QFT on 14 qubits + %d random brick layers, noise after every gate, Ensemble Z' % layers,
+           'noise': NOISE}
+    states, probs = {}, {}
+    for precision, s in (('double', 8), ('single', 4)):
+        DmSimulatorGPU.DEFAULT_OPTIONS['rotation_error'] = {'rx': [1., 0.], 'ry': [1., 0.], 'rz': [1., 0.]}
+        b = DmSimulatorGPU()
+        o = copy.deepcopy(opts)
+        o['precision'] = precision
+        o['coefficients_to_host'] = False
+        b._set_options(backend_options=o)
+        res = b.record_experiment(qc.to_experiment())
+        st = b.recorded_state
+        st.replay()
+        steps = max(1, min(args.steps, 3))
+        ms = time_replays(torch, st, steps)
+        by_kernel = pass_kernel_profile(torch, st)
+        durs = all_durations(by_kernel)
+        mean = float(np.mean(durs))
+        gbs = 2 * 4.0 ** n * s / (mean / 1e3) / 1e9
+        out['fp64' if precision == 'double' else 'fp32'] = {
+            'ms_per_circuit': ms, 'levels': b.last_run_stats['levels'], 'passes': len(durs),
+            'pass_kernels': {k: len(v) for k, v in by_kernel.items()}, 'mean_pass_ms': mean,
+            'pass_achieved_gbs': gbs, 'pass_frac_of_hbm': gbs / hbm, 'gate_layers_per_s': layers / (ms / 1e3)}
+        states[precision] = st
+        probs[precision] = np.array(list(res['data']['ensemble_probability'].values()))
+        del b
+    out['fp32_over_fp64'] = out['fp64']['ms_per_circuit'] / out['fp32']['ms_per_circuit']
+    out['accuracy_fp32'] = {
+        'max_abs_coeff_err': states['single'].max_abs_diff(states['double']) * 2.0 ** n,
+        'prob_l1_err': float(np.abs(probs['single'] - probs['double']).sum()),
+        'against': 'the same circuit in FP64 on the GPU'}
+    out['peak_gbs'] = hbm
+    out['peak_kind'] = peak_kind
+    del states
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_ours(args):
@@ -674,6 +781,8 @@ def run_ours(args):
     if 'headline' in legs and not args.no_gate_kinds:
         line['per_gate_kind_fp64'] = per_gate_kind(torch, N)
         line['per_gate_kind_fp32'] = per_gate_kind(torch, N, dtype=N.DM_F32)
+    if 'c2' in legs:
+        line['qft14_workload'] = c2_leg(args, pkg, torch, N, DmSimulatorGPU)
     if 'batch' in legs and args.batch > 0:
         line['batched_sweep'] = batch_leg(args, pkg, torch, N)
     if 'surrogate' in legs and args.surrogate_train > 0:
@@ -697,8 +806,8 @@ def host_threads():
 
 
 def run_reference(args):
-    """The reference's algorithm (the oracle port) on every host core: each step runs one layer
-    sample per core in parallel worker processes and reports their total work over the wall time."""
+    """The reference's own CPU implementation on every host core: each step runs one layer sample
+    per core in parallel worker processes and reports their total work over the wall time."""
     import multiprocessing
     from concurrent.futures import ProcessPoolExecutor
     world, rank, _ = dist_setup(args)
@@ -721,7 +830,7 @@ def run_reference(args):
                 samples.append({'value': workers / (wall * scale), 'wall': wall, 'first': res[0]})
     value = float(np.mean([s['value'] for s in samples]))
     last = samples[-1]
-    cb = {'value': value, 'unit': 'gate-layers/s', 'cores': workers, 'kind': 'port',
+    cb = {'value': value, 'unit': 'gate-layers/s', 'cores': workers, 'kind': last['first']['kind'],
           'sample': ('%d noisy random layers at n=%d, one per worker process on %d host threads in parallel '
                      '(numpy FP64, 1 thread each, %.2f s wall per step), scaled to n=%d like the single-core '
                      'sample: %s' % (workers, CPU_SAMPLE_N, workers, last['wall'], args.n, last['first']['sample'])),

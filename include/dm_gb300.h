@@ -171,6 +171,27 @@ typedef struct dm_tc_pass {
 int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, const uint16_t *umats_dev, size_t umats_count,
                      int *status_dev, void *stream);
 
+/* The same pass with TMA-fed tiles: one CTA per SM of two thread teams,
+ * each streaming its tiles through its own shared-memory slot by
+ * cp.async.bulk.tensor loads and stores, with the pass's round images
+ * resident in shared memory.  Differences from dm_apply_pass_tc: the
+ * natural-tile tables (natrow / natk, and rowc / kc of the last round) are
+ * plain element offsets (the TMA box is unswizzled); each round's images are
+ * 8192 FP16 values, Uh then Ul = fp16(2**11 (U - Uh)) (no 2**11 Uh image);
+ * at most 6 rounds; the resident axes must fit a 5-dimensional tensor map
+ * (runs of consecutive qubits, at most 4 per dimension).  Returns
+ * DM_ERR_PROGRAM for a pass outside these limits (the caller then uses
+ * dm_apply_pass_tc).  Same role as dm_apply_pass (dm_simulator.py:1005-1177). */
+int dm_apply_pass_tma(void *state_dev, int n, const dm_tc_pass *pass, const uint16_t *umats_dev, size_t umats_count,
+                      int *status_dev, void *stream);
+
+/* out_dev[0] = max |a_s - b_s| over the 4**n coefficients of two device states
+ * (dtypes DM_F32 / DM_F64 each), computed in FP64 on the device.  The error
+ * statement of an FP32 result against the same experiment run in FP64
+ * (no reference counterpart: the reference computes in FP64 only). */
+int dm_max_abs_diff(const void *a_dev, int dtype_a, const void *b_dev, int dtype_b, int n, double *out_dev,
+                    void *stream);
+
 /* ------------------------------------------------------------- batched sweeps */
 
 /* One pass of a batched program (the n-independent part of dm_pass). */
@@ -420,7 +441,9 @@ int dm_nbasis_probs(const void *state_dev, int n, int dtype, const double *nvec3
  * exits, enough for n <= 10.  Larger n returns DM_ERR_RANGE without touching
  * the GPU.  The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress, with that device current), so make that first call
- * before any stream capture.  Every call shares the one array: calls that
+ * before any stream capture; the address is looked up again when the
+ * device's CUDA context has changed since (after cudaDeviceReset the module,
+ * and with it the array, may sit elsewhere).  Every call shares the one array: calls that
  * overlap on the GPU (other streams, other host threads) race on it.  Each
  * call writes every scratch element it reads, so nothing left from a previous
  * call reaches a result.  Allocates nothing (no cudaMalloc / cudaFree). */
@@ -436,7 +459,9 @@ int dm_gather(const void *state_dev, int n, int dtype, const int64_t *idx, int c
 /* Shot counts from 2**m outcome probabilities (FP64, device), no counterpart
  * in the reference (its dm_simulator has max_shots = 1 and reports
  * probabilities only).  counts_dev receives 2**m int64 counts summing to
- * shots; the draws are a deterministic function of seed.  m <= 20;
+ * shots; the draws are a deterministic function of seed.  Negative
+ * probabilities count as 0; when none is positive, no shot is drawn and
+ * every count is 0 (so the counts sum to 0, not shots).  m <= 20;
  * scratch_dev: dm_sample_counts_scratch_bytes(m) bytes. */
 size_t dm_sample_counts_scratch_bytes(int m);
 int dm_sample_counts(const double *probs_dev, int m, int64_t shots, uint64_t seed, int64_t *counts_dev,

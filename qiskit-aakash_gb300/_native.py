@@ -18,7 +18,8 @@ CSRC = os.path.join(PKG_DIR, 'csrc')
 INCLUDE = os.path.join(REPO_DIR, 'include')
 BUILD_DIR = os.path.join(PKG_DIR, '_build')
 LIB_PATH = os.path.join(PKG_DIR, 'libdmgb300.so')
-SOURCES = ['dm_misc.cu', 'dm_pass.cu', 'dm_state.cu', 'dm_measure.cu', 'dm_tc.cu', 'dm_mlp.cu', 'dm_sample.cu']
+SOURCES = ['dm_misc.cu', 'dm_pass.cu', 'dm_state.cu', 'dm_measure.cu', 'dm_tc.cu', 'dm_tma.cu', 'dm_mlp.cu',
+           'dm_sample.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '-Xptxas', '-warn-spills',
               '--expt-relaxed-constexpr']
@@ -176,6 +177,8 @@ SIGNATURES = {
     'dm_apply_memory_noise': (_i, [_vp, _i, _i, _d, _d, _d, _vp]),
     'dm_apply_pass': (_i, [_vp, _i, _i, ctypes.POINTER(DmPass), _vp, _sz, _vp]),
     'dm_apply_pass_tc': (_i, [_vp, _i, ctypes.POINTER(DmTcPass), _vp, _sz, _vp, _vp]),
+    'dm_apply_pass_tma': (_i, [_vp, _i, ctypes.POINTER(DmTcPass), _vp, _sz, _vp, _vp]),
+    'dm_max_abs_diff': (_i, [_vp, _i, _vp, _i, _i, _vp, _vp]),
     'dm_batch_run': (_i, [_i, _vp, _sz, _vp, _sz, _vp, _sz, ctypes.POINTER(DmBatchInstance), _vp, _i,
                           ctypes.POINTER(DmBatchPass), _vp, _i, _vp, _vp, _vp]),
     'dm_batch_tc_scratch_bytes': (_sz, []),

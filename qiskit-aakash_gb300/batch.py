@@ -81,6 +81,9 @@ class HostRecorder:
     def overlap(self, other):
         raise BasicAerError('batched programs do not compare states')
 
+    def trace_error(self):
+        return 0.0
+
     def synchronize(self):
         pass
 
@@ -130,8 +133,10 @@ def derive_recording(ref, spec):
     instance of the same structure (qubits, depth): the same operations in the same order, with
     this instance's matrices built by the functions the run loop uses (its merged gates'
     rotations in program order per qubit, its memory noise, its CX error, its read-out
-    polarisation).  None when the instance does not line up with ``ref``; the caller then
-    records it through the run loop."""
+    polarisation).  None when the instance does not line up with ``ref`` (qubit count,
+    rotation axes per qubit, the (control, target) sequence of its CX gates, or a read-out
+    other than one Ensemble Z measurement of every qubit); the caller then records it
+    through the run loop."""
     from .dm_simulator import _u_decomposition
     from .scheduler import merge_single_gates
     exp, opts = instance_experiment(spec)
@@ -140,9 +145,20 @@ def derive_recording(ref, spec):
         return None
     err, merge = _error_params(opts)
     gates = [[] for _ in range(n)]
+    cxs = []
+    measured = set()
     for inst in merge_single_gates(exp.instructions, n, merge):
         if inst.name in ('u1', 'u3'):
             gates[inst.qubits[0]].append(_u_decomposition(inst.name, inst.params))
+        elif inst.name in ('cx', 'CX'):
+            cxs.append(tuple(int(q) for q in inst.qubits))
+        elif inst.name == 'measure':
+            params = getattr(inst, 'params', None) or []
+            if len(params) != 2 or str(params[0]) != 'Ensemble' or str(params[1]) != 'Z':
+                return None
+            measured.update(int(q) for q in inst.qubits)
+    if measured != set(range(n)) or len(ref.readouts) != 1 or list(ref.readouts[0][2]) != [3] * n:
+        return None
     mem = err['memory']
     noise = P.noise_ptm(mem['decoherence'], mem['thermalization'], mem['amplitude_decay'])
     if np.array_equal(noise, P.IDENTITY4):
@@ -150,6 +166,7 @@ def derive_recording(ref, spec):
     coef, ideal = P.cx_coefficients(err['two_qubit_gates'])
     rot_err = err['one_qubit_gates']
     used = [0] * n
+    used_cx = 0
     ops = []
     for op in ref.ops:
         if op.kind == 'map1' and op.tag and op.tag[0] == 'rot':
@@ -165,10 +182,13 @@ def derive_recording(ref, spec):
         elif op.kind == 'map1' and op.tag == ('noise',):
             ops.append(P.Op('map1', op.axes, noise, tag=('noise',)))
         elif op.kind == 'cx':
+            if used_cx >= len(cxs) or tuple(op.axes) != cxs[used_cx]:
+                return None
+            used_cx += 1
             ops.append(P.Op('cx', op.axes, np.array(coef), ideal, tag=('cx',)))
         else:
             return None
-    if used != [len(g) for g in gates]:
+    if used != [len(g) for g in gates] or used_cx != len(cxs):
         return None
     rec = HostRecorder(n)
     rec.init = ref.init

@@ -27,6 +27,10 @@ inline bool valid_n(int n) { return n >= 1 && n <= DM_MAX_QUBITS; }
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
+// Raise func's dynamic shared-memory limit to `bytes` on the current device
+// (once per kernel and device; the attribute is per device).
+cudaError_t ensure_max_dynamic_smem(const void *func, int bytes);
+
 // Check the launch that was just enqueued.
 inline int launch_status() {
     cudaError_t e = cudaGetLastError();

@@ -11,6 +11,8 @@
 // err**popcount and apply an in-place Walsh-Hadamard transform.
 #include <math.h>
 
+#include <cuda.h>
+
 #include <mutex>
 
 #include "dm_common.cuh"
@@ -241,26 +243,62 @@ static __device__ __align__(256) double g_nbasis_scratch[kNoallocScratchDoubles]
 
 constexpr int kMaxDevices = 64;
 
-// Device address of g_nbasis_scratch, resolved once per device with that
-// device current.  Host code must not pass the symbol itself to a kernel:
-// on the host it names a shadow variable, not device memory.
+// The unique ID of the current CUDA context (driver entry points resolved at
+// run time), or 0 when it cannot be read.  A device's primary context gets a
+// new ID when it is destroyed and created again (cudaDeviceReset), and the
+// module holding g_nbasis_scratch is then loaded again, possibly elsewhere.
+static unsigned long long current_context_id() {
+    using GetCurrent = CUresult (*)(CUcontext *);
+    using GetId = CUresult (*)(CUcontext, unsigned long long *);
+    static std::once_flag once;
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(p);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(p);
+        (void)cudaGetLastError();
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr ||
+        get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
+
+// Device address of g_nbasis_scratch, resolved with the device current, once
+// per device and context: it is looked up again when the device's context
+// has changed since (or when its ID cannot be read).  Host code must not pass
+// the symbol itself to a kernel: on the host it names a shadow variable, not
+// device memory.
 static int noalloc_scratch(double **out) {
     static std::mutex mu;
     static double *addr[kMaxDevices] = {nullptr};
+    static unsigned long long ctx_of[kMaxDevices] = {0};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) {
         (void)cudaGetLastError();
         return DM_ERR_CUDA;
     }
     if (dev < 0 || dev >= kMaxDevices) return DM_ERR_RANGE;
+    // 0 (no context current on this thread yet, or no ID): look the address up, which also makes
+    // the runtime's context current; a later call then records that context's ID
+    const unsigned long long ctx = current_context_id();
     std::lock_guard<std::mutex> lock(mu);
-    if (addr[dev] == nullptr) {
+    if (addr[dev] == nullptr || ctx == 0 || ctx != ctx_of[dev]) {
         void *p = nullptr;
         if (cudaGetSymbolAddress(&p, g_nbasis_scratch) != cudaSuccess) {
             (void)cudaGetLastError();
             return DM_ERR_CUDA;
         }
         addr[dev] = static_cast<double *>(p);
+        ctx_of[dev] = ctx;
     }
     *out = addr[dev];
     return DM_OK;

@@ -1,6 +1,7 @@
 // Library-wide bookkeeping: launch counter, SM count cache, error strings.
 #include <atomic>
 #include <mutex>
+#include <vector>
 
 #include "dm_common.cuh"
 
@@ -23,6 +24,30 @@ int sm_count() {
         cache[dev] = v;
     }
     return cache[dev];
+}
+
+cudaError_t ensure_max_dynamic_smem(const void *func, int bytes) {
+    struct Done {
+        const void *func;
+        int device, bytes;
+    };
+    static std::mutex mu;
+    static std::vector<Done> done;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return cudaErrorInvalidDevice;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    for (const Done &d : done)
+        if (d.func == func && d.device == dev && d.bytes >= bytes) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return e;
+    }
+    done.push_back(Done{func, dev, bytes});
+    return cudaSuccess;
 }
 
 }  // namespace dmg

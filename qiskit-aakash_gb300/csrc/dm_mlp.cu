@@ -368,12 +368,8 @@ __global__ void __launch_bounds__(kRowThreads) ensemble_kernel(const float *__re
 
 template <int EPI>
 static int launch_gemm(const dm_mlp_gemm &g, int *status, cudaStream_t s) {
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [] {
-        attr_err = cudaFuncSetAttribute(gemm_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytes));
-    });
-    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    if (ensure_max_dynamic_smem(reinterpret_cast<const void *>(gemm_kernel<EPI>), int(kSmemBytes)) != cudaSuccess)
+        return DM_ERR_CUDA;
     dim3 grid(g.M / kBM, g.N / kBN, g.members);
     gemm_kernel<EPI><<<grid, kThreads, kSmemBytes, s>>>(g, status);
     count_launch();

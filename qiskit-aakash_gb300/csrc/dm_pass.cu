@@ -474,12 +474,8 @@ static int build_rounds(const dm_pass *in, const PassDev &pd, int R, PassRounds 
 template <typename T, int R>
 static int launch_rounds(T *st, const PassRounds &p, const T *mats, cudaStream_t s) {
     const size_t smem = size_t(kPipeBuffers) * (size_t(1) << (2 * pipe_tile_axes<T>())) * sizeof(T);
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [smem] {
-        attr_err = cudaFuncSetAttribute(pass_pipe_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    });
-    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    if (ensure_max_dynamic_smem(reinterpret_cast<const void *>(pass_pipe_kernel<T, R>), int(smem)) != cudaSuccess)
+        return DM_ERR_CUDA;
     const int64_t ntiles = int64_t(1) << (2 * p.m);
     int64_t grid = sm_count();
     if (grid > ntiles) grid = ntiles;
@@ -491,13 +487,9 @@ static int launch_rounds(T *st, const PassRounds &p, const T *mats, cudaStream_t
 template <typename T>
 static int launch_pass(T *st, const PassDev &p, const T *mats, cudaStream_t s) {
     const size_t smem = (size_t(1) << (2 * p.k)) * sizeof(T);
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [] {
-        attr_err = cudaFuncSetAttribute(pass_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        int((size_t(1) << (2 * DM_MAX_TILE_AXES)) * sizeof(T)));
-    });
-    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    if (ensure_max_dynamic_smem(reinterpret_cast<const void *>(pass_kernel<T>),
+                                int((size_t(1) << (2 * DM_MAX_TILE_AXES)) * sizeof(T))) != cudaSuccess)
+        return DM_ERR_CUDA;
     int per_sm = 0;
     DM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pass_kernel<T>, 256, smem));
     if (per_sm < 1) per_sm = 1;
@@ -712,12 +704,8 @@ template <typename T, int R>
 static int launch_batch(T *states, double *probs, const T *mats, const dm_batch_instance *insts, int ninst,
                         const dm_batch_pass *passes, int *counter, cudaStream_t s) {
     const size_t smem = size_t(kPipeBuffers) * (size_t(1) << (2 * pipe_tile_axes<T>())) * sizeof(T);
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [smem] {
-        attr_err = cudaFuncSetAttribute(batch_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    });
-    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    if (ensure_max_dynamic_smem(reinterpret_cast<const void *>(batch_kernel<T, R>), int(smem)) != cudaSuccess)
+        return DM_ERR_CUDA;
     DM_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), s));
     int grid = sm_count();
     if (grid > ninst) grid = ninst;
@@ -769,13 +757,8 @@ template <typename T, int R>
 static int launch_batch_params(T *states, double *probs, const dm_param_program &P, const double *params,
                                int params_stride, int ninst, int *counter, cudaStream_t s) {
     const size_t smem = size_t(kPipeBuffers) * (size_t(1) << (2 * pipe_tile_axes<T>())) * sizeof(T);
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [smem] {
-        attr_err = cudaFuncSetAttribute(batch_param_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        int(smem));
-    });
-    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    if (ensure_max_dynamic_smem(reinterpret_cast<const void *>(batch_param_kernel<T, R>), int(smem)) != cudaSuccess)
+        return DM_ERR_CUDA;
     DM_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), s));
     int grid = sm_count();
     if (grid > ninst) grid = ninst;

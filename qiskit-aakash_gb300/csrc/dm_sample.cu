@@ -6,7 +6,8 @@
 // totals); every shot draws a counter-based uniform (splitmix64 of the seed
 // and the shot index), finds its outcome by binary search in the CDF and
 // increments that outcome's count.  Negative probabilities (rounding noise
-// of a measurement) count as zero.
+// of a measurement) count as zero; when no probability is positive no shot
+// is drawn and every count stays 0.
 #include "dm_common.cuh"
 
 namespace dmg {
@@ -72,6 +73,7 @@ __global__ void add_offsets(double *__restrict__ cdf, int64_t count, const doubl
 __global__ void draw(const double *__restrict__ cdf, int64_t count, const double *__restrict__ total, int64_t shots,
                      uint64_t seed, unsigned long long *__restrict__ counts) {
     const double tot = *total;
+    if (!(tot > 0.0)) return;   // nothing to draw from: the counts stay 0 (the caller sees their sum)
     for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < shots; i += int64_t(gridDim.x) * blockDim.x) {
         const uint64_t r = splitmix64(seed ^ splitmix64(uint64_t(i)));
         const double u = double(r >> 11) * (1.0 / 9007199254740992.0) * tot;   // [0, tot)

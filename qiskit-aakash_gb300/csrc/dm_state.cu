@@ -106,6 +106,26 @@ __global__ void __launch_bounds__(256) sum_partials_kernel(const double *__restr
     if (threadIdx.x == 0) out[0] = acc * scale;
 }
 
+// max |a - b| over two states (any dtypes), in FP64: one atomicMax per block on
+// the bit pattern, which orders non-negative doubles like their values.
+template <typename TA, typename TB>
+__global__ void __launch_bounds__(256) max_abs_diff_kernel(const TA *__restrict__ a, const TB *__restrict__ b,
+                                                           int64_t total, unsigned long long *__restrict__ out) {
+    double m = 0.0;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total;
+         i += int64_t(gridDim.x) * blockDim.x)
+        m = fmax(m, fabs(double(a[i]) - double(b[i])));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ double part[8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) part[w] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < int(blockDim.x >> 5); ++i) m = fmax(m, part[i]);
+        atomicMax(out, static_cast<unsigned long long>(__double_as_longlong(m)));
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Pauli basis -> matrix basis (dm_simulator.py:1198-1255)
 // Per axis (I,X,Y,Z) -> (e00,e01,e10,e11) = (I+Z, X-iY, X+iY, I-Z); then the
@@ -305,6 +325,30 @@ extern "C" int dm_pauli_to_matrix(const void *state_dev, int n, int dtype, doubl
     }
     const int64_t total = pow4(n);
     deinterleave_kernel<<<grid_for(total, 256), 256, 0, s>>>(buf, n, reinterpret_cast<double2 *>(out_dev));
+    count_launch();
+    return launch_status();
+}
+
+extern "C" int dm_max_abs_diff(const void *a_dev, int dtype_a, const void *b_dev, int dtype_b, int n, double *out_dev,
+                               void *stream) {
+    DM_CHECK_ARG(a_dev && b_dev && out_dev && valid_n(n) && valid_dtype(dtype_a) && valid_dtype(dtype_b));
+    const int64_t total = pow4(n);
+    cudaStream_t s = as_stream(stream);
+    DM_CUDA_TRY(cudaMemsetAsync(out_dev, 0, sizeof(double), s));
+    const int blocks = grid_for(total, 256, 4);
+    auto *out = reinterpret_cast<unsigned long long *>(out_dev);
+    if (dtype_a == DM_F32 && dtype_b == DM_F64)
+        max_abs_diff_kernel<<<blocks, 256, 0, s>>>(static_cast<const float *>(a_dev), static_cast<const double *>(b_dev),
+                                                   total, out);
+    else if (dtype_a == DM_F64 && dtype_b == DM_F64)
+        max_abs_diff_kernel<<<blocks, 256, 0, s>>>(static_cast<const double *>(a_dev),
+                                                   static_cast<const double *>(b_dev), total, out);
+    else if (dtype_a == DM_F32 && dtype_b == DM_F32)
+        max_abs_diff_kernel<<<blocks, 256, 0, s>>>(static_cast<const float *>(a_dev), static_cast<const float *>(b_dev),
+                                                   total, out);
+    else
+        max_abs_diff_kernel<<<blocks, 256, 0, s>>>(static_cast<const double *>(a_dev),
+                                                   static_cast<const float *>(b_dev), total, out);
     count_launch();
     return launch_status();
 }

@@ -40,6 +40,7 @@
 #include "dm_batch.cuh"
 #include "dm_common.cuh"
 #include "dm_rounds.cuh"
+#include "dm_tc_tile.cuh"
 #include "dm_tcgen05.cuh"
 
 namespace dmg {
@@ -49,47 +50,13 @@ namespace tc {
 constexpr int kThreads = 256;                  // two CTAs per SM
 constexpr int kCtasPerSm = 2;
 constexpr int kBlocksPerThread = 256 / kThreads;   // M = 128 blocks in one thread's epilogue
-constexpr int kAxes = 7;                       // resident axes per tile
-constexpr int kTile = 1 << (2 * kAxes);        // 16384 coefficients
-constexpr int kGroups = kTile / 64;            // 256 rows per round
-constexpr uint32_t kABytes = kGroups * 64 * 2; // 32 KB per FP16 operand image
-constexpr uint32_t kBImage = 64 * 64 * 2;      // 8 KB per FP16 matrix image
 constexpr uint32_t kBBytes = 3 * kBImage;      // 24 KB
 constexpr uint32_t kSmemBytes = 2 * kABytes + kBBytes;   // 88 KB: two CTAs per SM
 constexpr int kUHalves = 3 * 64 * 64;          // FP16 values per round image
-constexpr float kLoScale = 2048.0f, kLoUnscale = 1.0f / 2048.0f;
 constexpr uint32_t kTmemCols = 256;            // two M = 128 blocks x N = 128 (D1 | D2)
-
-// K-major core-matrix layout (no swizzle) of a rows x 64 FP16 operand: element
-// (row, k) lives at byte (row%8)*16 + (k%8)*2 + (k/8)*128 + (row/8)*1024.
-// LBO (next 16-byte core matrix along K) = 128 B, SBO (next 8 rows) = 1024 B.
-constexpr uint32_t kLBO = 128, kSBO = 1024;
-
-__device__ __forceinline__ uint32_t row_off(int row) { return (row & 7) * 16 + (row >> 3) * kSBO; }
-__device__ __forceinline__ uint32_t k_off(int k) { return (k & 7) * 2 + (k >> 3) * kLBO; }
-
-using tcg::cp_async16;
-using tcg::cp_async_commit;
-using tcg::cp_async_wait_all;
-using tcg::mbar_wait;
-using tcg::smem_u32;
-
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) { return tcg::smem_desc(saddr, kLBO, kSBO); }
-
-// kind::f16, D = F32 (bits 4-5 = 1), A = B = F16 (bits 7-9, 10-12 = 0), both K-major, M = 128, N = 128 / 64.
-constexpr uint32_t kIdesc128 = (1u << 4) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
-constexpr uint32_t kIdesc64 = (1u << 4) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
 
 // Natural-layout swizzle of the tile (16-byte chunks intact), as in dm_pass.cu.
 __device__ __forceinline__ int nat_swz(int e) { return e ^ ((((e >> 5) ^ (e >> 8)) & 7) << 2); }
-
-struct Round {
-    int8_t digits[3];
-    int8_t vec;
-    int32_t umoff;
-    uint32_t rowc[8];
-    uint32_t kc[6];
-};
 
 struct Pass {
     int n, m, low, nrounds;
@@ -105,110 +72,6 @@ __device__ __forceinline__ int64_t tile_offset(const Pass &p, int e) {
     int64_t off = e & ((1 << (2 * p.low)) - 1);
     for (int r = p.low; r < kAxes; ++r) off += int64_t((e >> (2 * r)) & 3) * p.res_stride[r];
     return off;
-}
-
-// XOR-combination of the offsets of the set bits of x (nbits of them).
-template <int NB>
-__device__ __forceinline__ uint32_t xor_bits(uint32_t x, const uint32_t *c) {
-    uint32_t o = 0;
-#pragma unroll
-    for (int i = 0; i < NB; ++i)
-        if ((x >> i) & 1) o ^= c[i];
-    return o;
-}
-
-// Per-digit XOR tables of the 64 K indices: k -> t0[d0] ^ t1[d1] ^ t2[d2].
-__device__ __forceinline__ void digit_tables(const uint32_t *kc, uint32_t (&t)[3][4]) {
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        t[d][0] = 0;
-        t[d][1] = kc[2 * d];
-        t[d][2] = kc[2 * d + 1];
-        t[d][3] = kc[2 * d] ^ kc[2 * d + 1];
-    }
-}
-
-// x -> (h, l): h = fp16(x), l = fp16(2**11 (x - h)), two values at once with packed conversions
-// (h2 = (fp16(a), fp16(b)) as FP16 bit patterns, l2 likewise)
-__device__ __forceinline__ void split2(float a, float b, uint32_t &h2, uint32_t &l2) {
-    const __half2 hh = __floats2half2_rn(a, b);
-    const float2 hf = __half22float2(hh);
-    const __half2 ll = __floats2half2_rn((a - hf.x) * kLoScale, (b - hf.y) * kLoScale);
-    h2 = *reinterpret_cast<const uint32_t *>(&hh);
-    l2 = *reinterpret_cast<const uint32_t *>(&ll);
-}
-
-// The same split of accumulator values a = 2**11 x: h = fp16(2**-11 a) and
-// l = fp16(a - 2**11 h), one FMA, exact (a - 2**11 h = 2**11 (x - h) is an
-// FP32 number), so the result equals split2(2**-11 a, 2**-11 b) bit for bit.
-__device__ __forceinline__ void split2_acc(float a, float b, uint32_t &h2, uint32_t &l2) {
-    const __half2 hh = __floats2half2_rn(a * kLoUnscale, b * kLoUnscale);
-    const float2 hf = __half22float2(hh);
-    const __half2 ll = __floats2half2_rn(fmaf(-kLoScale, hf.x, a), fmaf(-kLoScale, hf.y, b));
-    h2 = *reinterpret_cast<const uint32_t *>(&hh);
-    l2 = *reinterpret_cast<const uint32_t *>(&ll);
-}
-
-// four accumulator values adjacent in K: one 64-bit store into each image
-__device__ __forceinline__ void put_split4(unsigned char *AH, unsigned char *AL, uint32_t o, float a, float b,
-                                           float c, float d) {
-    uint32_t h0, l0, h1, l1;
-    split2_acc(a, b, h0, l0);
-    split2_acc(c, d, h1, l1);
-    *reinterpret_cast<uint2 *>(AH + o) = make_uint2(h0, h1);
-    *reinterpret_cast<uint2 *>(AL + o) = make_uint2(l0, l1);
-}
-
-// Epilogue stores of one thread's 64 values (K index j = d0 + 4 d1 + 16 d2)
-// at base ^ t[0][d0] ^ t[1][d1] ^ t[2][d2].  With a vector digit D the four
-// values along D are adjacent in the destination: one 64-bit store per
-// FP16 image (SPLIT), or one 128-bit FP32 store into the natural tile.
-template <int D, bool SPLIT>
-__device__ __forceinline__ void store_vec(const float (&v)[64], uint32_t base, const uint32_t (&t)[3][4],
-                                          unsigned char *AH, unsigned char *AL) {
-    constexpr int S = 1 << (2 * D);
-    constexpr int X = D == 0 ? 1 : 0, Y = D == 2 ? 1 : 2;   // the two other digits
-#pragma unroll
-    for (int x = 0; x < 4; ++x)
-#pragma unroll
-        for (int y = 0; y < 4; ++y) {
-            const int j0 = (x << (2 * X)) | (y << (2 * Y));
-            const uint32_t o = base ^ t[X][x] ^ t[Y][y];
-            if (SPLIT)
-                put_split4(AH, AL, o, v[j0], v[j0 + S], v[j0 + 2 * S], v[j0 + 3 * S]);
-            else
-                *reinterpret_cast<float4 *>(AH + 4 * o) = make_float4(v[j0], v[j0 + S], v[j0 + 2 * S], v[j0 + 3 * S]);
-        }
-}
-
-template <bool SPLIT>
-__device__ __forceinline__ void store_all(const float (&v)[64], int vec, uint32_t base, const uint32_t (&t)[3][4],
-                                          unsigned char *AH, unsigned char *AL) {
-    if (vec == 0) {
-        store_vec<0, SPLIT>(v, base, t, AH, AL);
-    } else if (vec == 1) {
-        store_vec<1, SPLIT>(v, base, t, AH, AL);
-    } else if (vec == 2) {
-        store_vec<2, SPLIT>(v, base, t, AH, AL);
-    } else if (SPLIT) {
-#pragma unroll
-        for (int j = 0; j < 64; j += 2) {   // conversions in pairs, 16-bit stores
-            uint32_t h2, l2;
-            split2_acc(v[j], v[j + 1], h2, l2);
-            const uint32_t o0 = base ^ t[0][j & 3] ^ t[1][(j >> 2) & 3] ^ t[2][j >> 4];
-            const uint32_t o1 = o0 ^ t[0][(j & 3) ^ 1] ^ t[0][j & 3];
-            *reinterpret_cast<unsigned short *>(AH + o0) = (unsigned short)(h2 & 0xFFFFu);
-            *reinterpret_cast<unsigned short *>(AL + o0) = (unsigned short)(l2 & 0xFFFFu);
-            *reinterpret_cast<unsigned short *>(AH + o1) = (unsigned short)(h2 >> 16);
-            *reinterpret_cast<unsigned short *>(AL + o1) = (unsigned short)(l2 >> 16);
-        }
-    } else {
-#pragma unroll
-        for (int j = 0; j < 64; ++j) {
-            const uint32_t o = base ^ t[0][j & 3] ^ t[1][(j >> 2) & 3] ^ t[2][j >> 4];
-            reinterpret_cast<float *>(AH)[o] = v[j];
-        }
-    }
 }
 
 // Per-CTA tensor-core state shared by the single-state and the batched kernels.
@@ -756,13 +619,9 @@ extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, 
         if (in.umoff < 0 || (in.umoff & 7) || size_t(in.umoff) + tc::kUHalves > umats_count) return DM_ERR_PROGRAM;
         o.umoff = in.umoff;
     }
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [] {
-        attr_err = cudaFuncSetAttribute(tc::pass_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        int(tc::kSmemBytes));
-    });
-    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    if (ensure_max_dynamic_smem(reinterpret_cast<const void *>(tc::pass_tc_kernel), int(tc::kSmemBytes)) !=
+        cudaSuccess)
+        return DM_ERR_CUDA;
     const int64_t ntiles = int64_t(1) << (2 * p.m);
     // 88 KB of shared memory, <= 128 registers per thread and 256 TMEM columns per CTA: two CTAs per SM
     int64_t grid = int64_t(sm_count()) * tc::kCtasPerSm;
@@ -842,13 +701,9 @@ extern "C" int dm_batch_run_tc(float *states_dev, size_t states_count, double *p
         }
     }
     if (scratch_bytes < dm_batch_tc_scratch_bytes()) return DM_ERR_ARG;
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [] {
-        attr_err = cudaFuncSetAttribute(tc::batch_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        int(tc::kSmemBytes));
-    });
-    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    if (ensure_max_dynamic_smem(reinterpret_cast<const void *>(tc::batch_tc_kernel), int(tc::kSmemBytes)) !=
+        cudaSuccess)
+        return DM_ERR_CUDA;
     cudaStream_t s = as_stream(stream);
     DM_CUDA_TRY(cudaMemsetAsync(counter_dev, 0, sizeof(int), s));
     const int grid = sm_count() * tc::kCtasPerSm;
@@ -888,13 +743,9 @@ extern "C" int dm_batch_run_params_tc(const dm_param_program *host, const dm_par
     if (size_t(ninst) * (size_t(1) << (2 * P.n)) > states_count) return DM_ERR_ARG;
     if (size_t(ninst) * (size_t(1) << P.n) > probs_count) return DM_ERR_ARG;
     if (scratch_bytes < dm_batch_tc_scratch_bytes()) return DM_ERR_ARG;
-    static std::once_flag once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(once, [] {
-        attr_err = cudaFuncSetAttribute(tc::batch_param_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        int(tc::kSmemBytes));
-    });
-    if (attr_err != cudaSuccess) return DM_ERR_CUDA;
+    if (ensure_max_dynamic_smem(reinterpret_cast<const void *>(tc::batch_param_tc_kernel), int(tc::kSmemBytes)) !=
+        cudaSuccess)
+        return DM_ERR_CUDA;
     cudaStream_t s = as_stream(stream);
     DM_CUDA_TRY(cudaMemsetAsync(counter_dev, 0, sizeof(int), s));
     const int grid = sm_count() * tc::kCtasPerSm;

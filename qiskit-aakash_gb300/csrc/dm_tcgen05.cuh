@@ -6,10 +6,19 @@
 namespace dmg {
 namespace tcg {
 
-constexpr int kSpinLimit = 1 << 24;   // bounded mbarrier waits (about a second)
+// Bounded mbarrier waits: a wait gives up after kWaitLimitNs of wall-clock time
+// (%globaltimer), or after kWaitPollCap polls should the timer not advance.
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+constexpr uint32_t kWaitPollCap = 1u << 30;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
 }
 
 // Shared-memory matrix descriptor of a K-major operand without swizzle:
@@ -29,18 +38,43 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// Wait for an mbarrier phase; gives up (returns false) after kSpinLimit polls.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-    for (int it = 0; it < kSpinLimit; ++it) {
-        uint32_t ok;
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(ok)
-            : "r"(mbar), "r"(parity)
-            : "memory");
-        if (ok) return true;
+__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Wait for an mbarrier phase; gives up (returns false) after limit_ns.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint64_t limit_ns = kWaitLimitNs) {
+    if (mbar_try(mbar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t it = 1; it < kWaitPollCap; ++it) {
+        if (mbar_try(mbar, parity)) return true;
+        if ((it & 15) == 0 && global_ns() - t0 > limit_ns) return false;
     }
     return false;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+
+// Arrive once and add `bytes` to the transaction count that the phase waits for.
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+// Bulk copy (TMA without a tensor map) of `bytes` (a multiple of 16, both
+// addresses 16-byte aligned) from global memory into this CTA's shared memory,
+// completing on mbar.
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
 }
 
 // 64 consecutive FP32 accumulator columns of this thread's TMEM lane.
@@ -65,32 +99,38 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
     for (int j = 0; j < 64; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-// Two runs of 32 consecutive FP32 accumulator columns of this thread's TMEM
-// lane (at taddr0 and taddr1), added: both loads are in flight before the wait.
-__device__ __forceinline__ void tmem_ld32_pair_add(uint32_t taddr0, uint32_t taddr1, float *v) {
-    uint32_t a[32], b[32];
 #define DM_R32(x)                                                                                                   \
     "=r"(x[0]), "=r"(x[1]), "=r"(x[2]), "=r"(x[3]), "=r"(x[4]), "=r"(x[5]), "=r"(x[6]), "=r"(x[7]), "=r"(x[8]),     \
         "=r"(x[9]), "=r"(x[10]), "=r"(x[11]), "=r"(x[12]), "=r"(x[13]), "=r"(x[14]), "=r"(x[15]), "=r"(x[16]),      \
         "=r"(x[17]), "=r"(x[18]), "=r"(x[19]), "=r"(x[20]), "=r"(x[21]), "=r"(x[22]), "=r"(x[23]), "=r"(x[24]),     \
         "=r"(x[25]), "=r"(x[26]), "=r"(x[27]), "=r"(x[28]), "=r"(x[29]), "=r"(x[30]), "=r"(x[31])
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,"
-        "%28,%29,%30,%31}, [%32];"
-        : DM_R32(a)
-        : "r"(taddr0));
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,"
-        "%28,%29,%30,%31}, [%32];"
-        : DM_R32(b)
-        : "r"(taddr1));
-#undef DM_R32
+#define DM_LD32 \
+    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18," \
+    "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+
+// Two runs of 32 consecutive FP32 accumulator columns of this thread's TMEM
+// lane (at taddr0 and taddr1), added: both loads are in flight before the wait.
+__device__ __forceinline__ void tmem_ld32_pair_add(uint32_t taddr0, uint32_t taddr1, float *v) {
+    uint32_t a[32], b[32];
+    asm volatile(DM_LD32 : DM_R32(a) : "r"(taddr0));
+    asm volatile(DM_LD32 : DM_R32(b) : "r"(taddr1));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(a[j]) + __uint_as_float(b[j]);
 }
+
+// The same two runs combined as v = a * scale + b.
+__device__ __forceinline__ void tmem_ld32_pair_fma(uint32_t taddr0, uint32_t taddr1, float scale, float *v) {
+    uint32_t a[32], b[32];
+    asm volatile(DM_LD32 : DM_R32(a) : "r"(taddr0));
+    asm volatile(DM_LD32 : DM_R32(b) : "r"(taddr1));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = fmaf(__uint_as_float(a[j]), scale, __uint_as_float(b[j]));
+}
+
+#undef DM_LD32
+#undef DM_R32
 
 }  // namespace tcg
 }  // namespace dmg

@@ -1,0 +1,514 @@
+// Tensor-core fused pass fed by TMA (FP32 state, 3-way FP16 split on tcgen05).
+//
+// Same arithmetic as pass_tc_kernel (dm_tc.cu): a pass holds 7 resident
+// qubit axes; each tile of 4**7 = 16,384 coefficients runs the pass's rounds,
+// each round a 64x64 real transfer matrix U on 3 of the tile's axes, issued
+// as tcgen05.mma.kind::f16 over a 3-way FP16 split (tile in units of 2**-n,
+// x = h + 2**-11 l; U = Uh + 2**-11 Ul):
+//     D1 = h Uh^T,   D2 = h Ul^T + l Uh^T,   2**11 x U^T = 2**11 D1 + D2 + O(2**-22 |x|),
+// D1 and D2 in separate FP32 accumulators (TMEM), combined by one FMA in the
+// epilogue, which writes the next round's h / l operand (or, after the last
+// round, the natural FP32 tile).
+//
+// What differs is how the work is fed and overlapped:
+// * one persistent CTA per SM with two teams of 256 threads; each team owns
+//   one 64 KB tile slot and 256 TMEM columns and streams its own tiles, so
+//   one team's MMAs, loads and stores overlap the other team's epilogues;
+// * tiles move by TMA (cp.async.bulk.tensor): one thread of the team issues
+//   the load of its next tile (completing on an mbarrier) as soon as the TMA
+//   store of its current tile has read the slot, and the store is
+//   asynchronous (bulk group); no thread computes a global address;
+// * the pass's round images ([Uh ; Ul], 16 KB per round) are loaded once per
+//   CTA by bulk copies and stay in shared memory for the whole pass (up to
+//   kMaxRounds rounds; longer passes run on pass_tc_kernel).
+//
+// Tensor map.  The state is a 4**n vector whose flat index is the base-4
+// number of the qubits' Pauli labels (qubit n-1 the lowest digit).  The 7
+// resident digits form runs of consecutive positions; each run is split into
+// chunks of at most 4 digits (a box dimension of <= 256 elements), and each
+// chunk is one tensor-map dimension with stride 4**start elements, box
+// 4**len and extent 4**(len + gap), where gap counts the non-resident digits
+// directly above the chunk.  Tile t (its non-resident digits in increasing
+// position order) has coordinate ((t >> 2 g) & (4**gap - 1)) * 4**len in that
+// dimension, g being the number of non-resident digits below the gap.  The box
+// lands in shared memory densely in dimension order, which is the tile's
+// natural order (local axis r = the r-th lowest resident digit), unswizzled.
+// The lowest digit is always resident, so every coordinate of dimension 0 is
+// a multiple of 4 elements (16 bytes), as TMA requires.
+//
+// Shared memory (dynamic, 1024-byte aligned): slot 0 | slot 1 (64 KB each:
+// AH | AL, 32 KB per FP16 operand image; the natural FP32 tile on load and
+// store) | round images (16 KB per round).  Every mbarrier wait is bounded in
+// time; a wait that gives up sets *status, the team stops, drains what it has
+// in flight (MMA, tile load, tile store) and the kernel returns.
+#include <cuda.h>
+#include <cuda_fp16.h>
+
+#include <mutex>
+
+#include "dm_common.cuh"
+#include "dm_tc_tile.cuh"
+#include "dm_tcgen05.cuh"
+
+namespace dmg {
+
+namespace tma {
+
+using namespace tc;
+using tcg::mbar_wait;
+using tcg::smem_u32;
+
+constexpr int kTeams = 2;
+constexpr int kTeamThreads = 256;
+constexpr int kThreads = kTeams * kTeamThreads;
+constexpr int kMaxRounds = 6;                                // round images resident in shared memory
+constexpr int kMaxDims = 5;                                  // tensor-map rank
+constexpr uint32_t kSlotBytes = 2 * kABytes;                 // 64 KB: AH | AL, or the FP32 tile
+constexpr uint32_t kUBytes = 2 * kBImage;                    // 16 KB per round: Uh | Ul (one 128-row operand)
+constexpr uint32_t kUHalves = kUBytes / 2;
+constexpr uint32_t kSmemBytes = kTeams * kSlotBytes + kMaxRounds * kUBytes + 1024;   // + alignment slack
+constexpr uint32_t kTmemCols = 512;                          // per team: two M = 128 blocks x (D1 | D2)
+
+struct TmaPass {
+    int nrounds, vec0, ndims;
+    float up, down;                  // 2**n, 2**-n
+    int64_t ntiles;
+    int8_t gap_first[kMaxDims];      // tile-index digit of the first non-resident digit above dimension i
+    int8_t gap_len[kMaxDims];        // non-resident digits above dimension i
+    int8_t box_log4[kMaxDims];       // resident digits of dimension i
+    int32_t uoff[kMaxRounds];        // FP16-value offset of round r's images
+    uint32_t natrow[8], natk[6];
+    Round rounds[kMaxRounds];
+};
+
+__device__ __forceinline__ void tile_coords(const TmaPass &p, int64_t t, int (&c)[kMaxDims]) {
+#pragma unroll
+    for (int i = 0; i < kMaxDims; ++i) {
+        const int64_t g = (t >> (2 * p.gap_first[i])) & ((int64_t(1) << (2 * p.gap_len[i])) - 1);
+        c[i] = int(g << (2 * p.box_log4[i]));
+    }
+}
+
+// TMA tile load of tile coordinates c into shared memory at dst, completing on mbar.
+__device__ __forceinline__ void tma_load(const CUtensorMap *map, int nd, const int (&c)[kMaxDims], uint32_t dst,
+                                         uint32_t mbar) {
+    const uint64_t m = reinterpret_cast<uint64_t>(map);
+    switch (nd) {
+    case 1:
+        asm volatile("cp.async.bulk.tensor.1d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2}], [%3];"
+                     ::"r"(dst), "l"(m), "r"(c[0]), "r"(mbar) : "memory");
+        break;
+    case 2:
+        asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+                     "[%4];" ::"r"(dst), "l"(m), "r"(c[0]), "r"(c[1]), "r"(mbar) : "memory");
+        break;
+    case 3:
+        asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                     "%4}], [%5];" ::"r"(dst), "l"(m), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(mbar) : "memory");
+        break;
+    case 4:
+        asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                     "%4, %5}], [%6];" ::"r"(dst), "l"(m), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(mbar)
+                     : "memory");
+        break;
+    default:
+        asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                     "%4, %5, %6}], [%7];" ::"r"(dst), "l"(m), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]),
+                     "r"(mbar) : "memory");
+        break;
+    }
+}
+
+// TMA tile store of the shared-memory box at src to tile coordinates c (bulk group of this thread).
+__device__ __forceinline__ void tma_store(const CUtensorMap *map, int nd, const int (&c)[kMaxDims], uint32_t src) {
+    const uint64_t m = reinterpret_cast<uint64_t>(map);
+    switch (nd) {
+    case 1:
+        asm volatile("cp.async.bulk.tensor.1d.global.shared::cta.bulk_group [%0, {%2}], [%1];" ::"l"(m), "r"(src),
+                     "r"(c[0]) : "memory");
+        break;
+    case 2:
+        asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(m), "r"(src),
+                     "r"(c[0]), "r"(c[1]) : "memory");
+        break;
+    case 3:
+        asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(m),
+                     "r"(src), "r"(c[0]), "r"(c[1]), "r"(c[2]) : "memory");
+        break;
+    case 4:
+        asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%2, %3, %4, %5}], [%1];" ::"l"(m),
+                     "r"(src), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]) : "memory");
+        break;
+    default:
+        asm volatile("cp.async.bulk.tensor.5d.global.shared::cta.bulk_group [%0, {%2, %3, %4, %5, %6}], [%1];" ::"l"(m),
+                     "r"(src), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]) : "memory");
+        break;
+    }
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void team_sync(int team) {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + team), "n"(kTeamThreads) : "memory");
+}
+
+// Barrier of the team that also ANDs `ok` over its threads: every thread of the
+// team gets the same answer, so a failed wait anywhere sends the whole team
+// down the same path (its barrier sequence stays matched).
+__device__ __forceinline__ bool team_and(bool ok, int team) {
+    uint32_t r;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.u32 p, %1, 0;\nbar.red.and.pred q, %2, %3, p;\nselp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"(uint32_t(ok)), "r"(1 + team), "n"(kTeamThreads)
+        : "memory");
+    return r != 0;
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    pass_tma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ TmaPass p,
+                    const uint16_t *__restrict__ umats, int *status) {
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t load_bar[kTeams];
+    __shared__ __align__(8) uint64_t mma_bar[kTeams];
+    __shared__ __align__(8) uint64_t u_bar;
+    __shared__ uint32_t tmem_base_s;
+    unsigned char *smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int team = tid / kTeamThreads, ttid = tid % kTeamThreads;
+    const bool leader = ttid == 0;
+    unsigned char *AH = smem + team * kSlotBytes, *AL = AH + kABytes;
+    unsigned char *U = smem + kTeams * kSlotBytes;
+    const uint32_t lbar = smem_u32(&load_bar[team]), mbar = smem_u32(&mma_bar[team]), ubar = smem_u32(&u_bar);
+
+    if (tid == 0) {
+        for (int i = 0; i < kTeams; ++i) {
+            tcg::mbar_init(smem_u32(&load_bar[i]), 1);
+            tcg::mbar_init(smem_u32(&mma_bar[i]), 1);
+        }
+        tcg::mbar_init(ubar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                     "n"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base_s + uint32_t(team * 256);
+
+    const int64_t stride = int64_t(gridDim.x) * kTeams;
+    int64_t t = int64_t(blockIdx.x) * kTeams + team;
+    if (tid == 0) {   // the pass's round images, once per CTA
+        tcg::mbar_expect_tx(ubar, uint32_t(p.nrounds) * kUBytes);
+        for (int r = 0; r < p.nrounds; ++r)
+            tcg::bulk_load(smem_u32(U + r * kUBytes), umats + p.uoff[r], kUBytes, ubar);
+    }
+    if (leader && t < p.ntiles) {
+        int c[kMaxDims];
+        tile_coords(p, t, c);
+        tcg::mbar_expect_tx(lbar, kSlotBytes);
+        tma_load(&tmap, p.ndims, c, smem_u32(AH), lbar);
+    }
+    bool load_pending = t < p.ntiles;
+    bool mma_pending = false;
+    uint32_t lphase = 0, mphase = 0;
+    const bool u_ok = team_and(mbar_wait(ubar, 0), team);
+    if (!u_ok && ttid == 0) atomicExch(status, 1);
+
+    // epilogue geometry: the thread holds row ttid of the 256-row operand, i.e. row ttid % 128 of
+    // M block ttid / 128, in TMEM lane quadrant warp % 4
+    const int mb_own = ttid >> 7;
+    const uint32_t taddr = tmem + (uint32_t(32 * (warp & 3)) << 16) + uint32_t(mb_own * 128);
+
+    for (; u_ok && t < p.ntiles; t += stride) {
+        if (!team_and(mbar_wait(lbar, lphase), team)) {
+            if (ttid == 0) atomicExch(status, 1);
+            break;
+        }
+        lphase ^= 1;
+        load_pending = false;
+        // ---- natural tile -> round 0's operand (h / l), in place ----
+        {
+            constexpr int kItems = kGroups * 8 / kTeamThreads;   // 8
+            const float *nat = reinterpret_cast<const float *>(AH);
+            const float up = p.up;
+            float x[kItems][8];
+#pragma unroll
+            for (int q = 0; q < kItems; ++q) {
+                const int i = ttid + kTeamThreads * q;
+                const int crow = ((i >> 6) << 3) | (i & 7), c = (i >> 3) & 7;
+                const uint32_t nb = xor_bits<8>(uint32_t(crow), p.natrow) ^ ((c & 1) ? p.natk[3] : 0u) ^
+                                    ((c & 2) ? p.natk[4] : 0u) ^ ((c & 4) ? p.natk[5] : 0u);
+                if (p.vec0 == 0) {
+                    const float4 a4 = *reinterpret_cast<const float4 *>(nat + nb);
+                    const float4 b4 = *reinterpret_cast<const float4 *>(nat + (nb ^ p.natk[2]));
+                    x[q][0] = a4.x; x[q][1] = a4.y; x[q][2] = a4.z; x[q][3] = a4.w;
+                    x[q][4] = b4.x; x[q][5] = b4.y; x[q][6] = b4.z; x[q][7] = b4.w;
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                        x[q][e] = nat[nb ^ ((e & 1) ? p.natk[0] : 0u) ^ ((e & 2) ? p.natk[1] : 0u) ^
+                                      ((e & 4) ? p.natk[2] : 0u)];
+                }
+            }
+            team_sync(team);
+#pragma unroll
+            for (int q = 0; q < kItems; ++q) {
+                const int i = ttid + kTeamThreads * q;
+                const int crow = ((i >> 6) << 3) | (i & 7), c = (i >> 3) & 7;
+                uint32_t hw[4], lw[4];
+#pragma unroll
+                for (int e = 0; e < 8; e += 2) split2(x[q][e] * up, x[q][e + 1] * up, hw[e >> 1], lw[e >> 1]);
+                const uint32_t o = row_off(crow) + uint32_t(c) * kLBO;
+                *reinterpret_cast<uint4 *>(AH + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(AL + o) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            }
+        }
+        bool alive = true;
+        for (int r = 0; r < p.nrounds; ++r) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            team_sync(team);
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (leader) {
+                // D[:, 0:64] = h Uh^T and D[:, 64:128] = h Ul^T (one N = 128 chain over [Uh ; Ul]),
+                // then D[:, 64:128] += l Uh^T (N = 64), for both M = 128 blocks
+                const uint32_t ah = smem_u32(AH), al = smem_u32(AL), ub = smem_u32(U + r * kUBytes);
+#pragma unroll
+                for (int mb = 0; mb < 2; ++mb) {
+                    const uint32_t aoff = mb * (kABytes / 2);
+                    const uint32_t d = tmem + mb * 128;
+#pragma unroll
+                    for (int term = 0; term < 2; ++term) {
+                        const uint32_t dd = d + (term == 0 ? 0u : 64u);
+                        const uint32_t a = (term == 0 ? ah : al) + aoff;
+                        const uint32_t idesc = term == 0 ? kIdesc128 : kIdesc64;
+#pragma unroll
+                        for (int ks = 0; ks < 4; ++ks) {
+                            const uint64_t da = smem_desc(a + ks * 2 * kLBO);
+                            const uint64_t db = smem_desc(ub + ks * 2 * kLBO);
+                            const uint32_t acc = (term | ks) ? 1u : 0u;
+                            asm volatile(
+                                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dd),
+                                "l"(da), "l"(db), "r"(idesc), "r"(acc));
+                        }
+                    }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
+            }
+            mma_pending = true;
+            if (!team_and(mbar_wait(mbar, mphase), team)) {
+                if (ttid == 0) atomicExch(status, 1);
+                alive = false;
+                break;
+            }
+            mphase ^= 1;
+            mma_pending = false;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            // ---- epilogue: D -> next operand (h / l), or the natural FP32 tile after the last round ----
+            const Round &R = p.rounds[r];
+            uint32_t tk[3][4];
+            digit_tables(R.kc, tk);
+            float v[64];
+            tcg::tmem_ld32_pair_fma(taddr, taddr + 64, kLoScale, v);        // 2**11 x = 2**11 D1 + D2
+            tcg::tmem_ld32_pair_fma(taddr + 32, taddr + 96, kLoScale, v + 32);
+            const uint32_t base = xor_bits<8>(uint32_t(ttid), R.rowc);
+            if (r + 1 < p.nrounds) {
+                store_all<true>(v, R.vec, base, tk, AH, AL);
+            } else {
+                const float down = p.down * kLoUnscale;
+#pragma unroll
+                for (int j = 0; j < 64; ++j) v[j] *= down;
+                store_all<false>(v, R.vec, base, tk, AH, AL);
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        }
+        if (!alive) break;
+        // ---- store the tile (TMA), then load the team's next tile into the slot ----
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        team_sync(team);
+        const int64_t tn = t + stride;
+        if (leader) {
+            int c[kMaxDims];
+            tile_coords(p, t, c);
+            tma_store(&tmap, p.ndims, c, smem_u32(AH));
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");   // the slot has been read
+            if (tn < p.ntiles) {
+                tile_coords(p, tn, c);
+                tcg::mbar_expect_tx(lbar, kSlotBytes);
+                tma_load(&tmap, p.ndims, c, smem_u32(AH), lbar);
+            }
+        }
+        load_pending = tn < p.ntiles;
+    }
+    // ---- drain: the team's MMA, tile load and tile stores in flight ----
+    if (mma_pending) mbar_wait(mbar, mphase);
+    if (load_pending) mbar_wait(lbar, lphase);
+    if (!u_ok) mbar_wait(ubar, 0);
+    if (leader) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base_s), "n"(kTmemCols));
+}
+
+}  // namespace tma
+
+}  // namespace dmg
+
+using namespace dmg;
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+namespace {
+
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+    static std::once_flag once;
+    static EncodeTiled fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+        (void)cudaGetLastError();
+    });
+    return fn;
+}
+
+}  // namespace
+
+// Tensor-map dimensions of a pass (see the file comment); false when the
+// resident digits need more than kMaxDims dimensions.
+static bool tma_dims(int n, const int32_t *axes, tma::TmaPass &p, cuuint64_t *gdim, cuuint64_t *gstride_bytes,
+                     cuuint32_t *box) {
+    bool res[DM_MAX_QUBITS * 2] = {false};
+    for (int r = 0; r < tc::kAxes; ++r) res[n - 1 - axes[r]] = true;   // digit position of each resident qubit
+    int nd = 0, gap_first = 0;
+    int pos = 0;
+    while (pos < n) {
+        if (!res[pos]) return false;   // only reached for position 0 (a chunk is always followed by its gap)
+        int len = 0;
+        while (pos + len < n && res[pos + len] && len < 4) ++len;
+        int gap = 0;
+        while (pos + len + gap < n && !res[pos + len + gap]) ++gap;
+        if (nd == tma::kMaxDims) return false;
+        p.box_log4[nd] = int8_t(len);
+        p.gap_len[nd] = int8_t(gap);
+        p.gap_first[nd] = int8_t(gap_first);
+        gdim[nd] = cuuint64_t(1) << (2 * (len + gap));
+        box[nd] = cuuint32_t(1) << (2 * len);
+        if (nd > 0) gstride_bytes[nd - 1] = (cuuint64_t(1) << (2 * pos)) * sizeof(float);
+        gap_first += gap;
+        pos += len + gap;
+        ++nd;
+    }
+    for (int i = nd; i < tma::kMaxDims; ++i) p.box_log4[i] = p.gap_len[i] = p.gap_first[i] = 0;
+    p.ndims = nd;
+    return gap_first == n - tc::kAxes;
+}
+
+// Natural-tile tables: element offsets below 4**7, each a power of two (the TMA box is unswizzled).
+static bool linear_tables(const uint32_t *rowc, const uint32_t *kc, int vec) {
+    uint32_t seen = 0;
+    for (int i = 0; i < 14; ++i) {
+        const uint32_t c = i < 8 ? rowc[i] : kc[i - 8];
+        if (c == 0 || (c & (c - 1)) || c >= uint32_t(tc::kTile) || (seen & c)) return false;
+        seen |= c;
+    }
+    if (vec >= 0) {
+        if (vec > 2 || kc[2 * vec] != 1 || kc[2 * vec + 1] != 2) return false;
+    }
+    return true;
+}
+
+// Operand tables: distinct powers of two inside one 32 KB image, 8-byte aligned
+// apart from the vector digit's two bits.
+static bool operand_tables(const uint32_t *rowc, const uint32_t *kc, int vec) {
+    uint32_t seen = 0;
+    for (int i = 0; i < 14; ++i) {
+        const uint32_t c = i < 8 ? rowc[i] : kc[i - 8];
+        if (c == 0 || (c & (c - 1)) || c >= tc::kABytes || (seen & c)) return false;
+        seen |= c;
+    }
+    if (vec >= 0) {
+        if (vec > 2 || kc[2 * vec] != 2 || kc[2 * vec + 1] != 4) return false;
+        for (int i = 0; i < 14; ++i) {
+            if (i >= 8 && (i - 8) / 2 == vec) continue;
+            const uint32_t c = i < 8 ? rowc[i] : kc[i - 8];
+            if (c % 8) return false;
+        }
+    }
+    return true;
+}
+
+extern "C" int dm_apply_pass_tma(void *state_dev, int n, const dm_tc_pass *pass, const uint16_t *umats_dev,
+                                 size_t umats_count, int *status_dev, void *stream) {
+    DM_CHECK_ARG(state_dev && pass && umats_dev && status_dev && valid_n(n));
+    if (reinterpret_cast<uintptr_t>(state_dev) & 15 || reinterpret_cast<uintptr_t>(umats_dev) & 15) return DM_ERR_ARG;
+    if (n < tc::kAxes) return DM_ERR_PROGRAM;
+    const int nr = pass->nrounds;
+    if (nr < 1 || nr > tma::kMaxRounds) return DM_ERR_PROGRAM;
+    for (int r = 0; r < tc::kAxes; ++r) {
+        const int q = pass->axes[r];
+        if (q < 0 || q >= n || (r > 0 && q >= pass->axes[r - 1])) return DM_ERR_PROGRAM;
+    }
+    if (pass->axes[0] != n - 1) return DM_ERR_PROGRAM;   // the contiguous axis is resident
+    tma::TmaPass p{};
+    cuuint64_t gdim[tma::kMaxDims], gstride[tma::kMaxDims];
+    cuuint32_t box[tma::kMaxDims], estride[tma::kMaxDims];
+    if (!tma_dims(n, pass->axes, p, gdim, gstride, box)) return DM_ERR_PROGRAM;
+    p.nrounds = nr;
+    p.vec0 = pass->vec0 == 0 ? 0 : -1;
+    p.up = float(ldexp(1.0, n));
+    p.down = float(ldexp(1.0, -n));
+    p.ntiles = int64_t(1) << (2 * (n - tc::kAxes));
+    if (p.vec0 == 0 && (pass->natk[0] != 1 || pass->natk[1] != 2)) return DM_ERR_PROGRAM;
+    if (!linear_tables(pass->natrow, pass->natk, -1)) return DM_ERR_PROGRAM;
+    for (int i = 0; i < 8; ++i) p.natrow[i] = pass->natrow[i];
+    for (int i = 0; i < 6; ++i) p.natk[i] = pass->natk[i];
+    for (int r = 0; r < nr; ++r) {
+        const dm_tc_round &in = pass->rounds[r];
+        tc::Round &o = p.rounds[r];
+        for (int i = 0; i < 3; ++i) {
+            if (in.digits[i] < 0 || in.digits[i] >= tc::kAxes) return DM_ERR_PROGRAM;
+            o.digits[i] = in.digits[i];
+        }
+        o.vec = in.vec;
+        const bool ok = r + 1 == nr ? linear_tables(in.rowc, in.kc, in.vec) : operand_tables(in.rowc, in.kc, in.vec);
+        if (!ok) return DM_ERR_PROGRAM;
+        for (int i = 0; i < 8; ++i) o.rowc[i] = in.rowc[i];
+        for (int i = 0; i < 6; ++i) o.kc[i] = in.kc[i];
+        if (in.umoff < 0 || (in.umoff & 7) || size_t(in.umoff) + tma::kUHalves > umats_count) return DM_ERR_PROGRAM;
+        o.umoff = in.umoff;
+        p.uoff[r] = in.umoff;
+    }
+    EncodeTiled enc = encode_fn();
+    if (!enc) return DM_ERR_CUDA;
+    for (int i = 0; i < tma::kMaxDims; ++i) estride[i] = 1;
+    CUtensorMap map;
+    if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, cuuint32_t(p.ndims), state_dev, gdim, gstride, box, estride,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return DM_ERR_CUDA;
+    if (ensure_max_dynamic_smem(reinterpret_cast<const void *>(tma::pass_tma_kernel), int(tma::kSmemBytes)) !=
+        cudaSuccess)
+        return DM_ERR_CUDA;
+    int64_t grid = sm_count();
+    const int64_t want = (p.ntiles + tma::kTeams - 1) / tma::kTeams;
+    if (grid > want) grid = want;
+    tma::pass_tma_kernel<<<int(grid), tma::kThreads, tma::kSmemBytes, as_stream(stream)>>>(map, p, umats_dev,
+                                                                                           status_dev);
+    count_launch();
+    return launch_status();
+}

@@ -31,13 +31,22 @@ GB300 options (absent from the reference): ``precision`` ('double', the
 default and the parity form, or 'single'), ``fusion`` (fused tile passes,
 default True), ``tile_axes`` (resident axes per tile), ``register_rounds``
 (apply a pass's operations in register rounds, default True), ``tensor_cores``
-(FP32 passes on tcgen05 as 64x64 transfer matrices in a 3-way FP16 split, default True) and
+(FP32 passes on tcgen05 as 64x64 transfer matrices in a 3-way FP16 split, default True), ``tma``
+(tensor-core passes with TMA-fed tiles where a pass fits them, default True) and
 ``coefficients_to_host`` (default True; False leaves ``coeffmatrix`` /
 ``densitymatrix`` out of the result, for callers that only need the
 measurement data of a large register) and ``counts_shots`` / ``counts_seed``
 (default 0: off; with shots > 0 every ensemble measurement also reports
 ``counts``, {bit string: count} of that many shots drawn on the device from
-its outcome probabilities; the reference reports probabilities only).
+its outcome probabilities; the reference reports probabilities only) and
+``fp64_check`` (default False; with precision 'single' the experiment is run
+a second time in FP64 on the device and the result's data gains
+``max_abs_coeff_err`` (max |2**n (a32 - a64)| over the final state),
+``prob_l1_err`` (the largest L1 distance of its probability outputs) and
+``trace_err``).  Every run ends with a trace-preservation check: 2**n a_0,
+read from the device in FP64, must be 1 within TRACE_TOL of the precision,
+else BasicAerError (the reference checks a_0 = 2**-n on the initial state
+only, dm_simulator.py:363).
 """
 import copy
 import logging
@@ -232,6 +241,8 @@ class DmSimulatorGPU(_Base):
         self._counts_seed = 0
         self._register_rounds = True
         self._tensor_cores = True
+        self._tma = True
+        self._fp64_check = False
         self.last_run_stats = {}
         self._record_next = False
         self.recorded_state = None
@@ -351,6 +362,8 @@ class DmSimulatorGPU(_Base):
             self._tile_axes = int(backend_options['tile_axes'])
         if 'tensor_cores' in backend_options:
             self._tensor_cores = bool(backend_options['tensor_cores'])
+        if 'tma' in backend_options:
+            self._tma = bool(backend_options['tma'])
         if 'register_rounds' in backend_options:
             self._register_rounds = bool(backend_options['register_rounds'])
         if 'coefficients_to_host' in backend_options:
@@ -362,6 +375,8 @@ class DmSimulatorGPU(_Base):
             self._counts_shots = shots
         if 'counts_seed' in backend_options:
             self._counts_seed = int(backend_options['counts_seed'])
+        if 'fp64_check' in backend_options:
+            self._fp64_check = bool(backend_options['fp64_check'])
 
     def _initialize_errors(self):
         """dm_simulator.py:273-282."""
@@ -593,11 +608,12 @@ class DmSimulatorGPU(_Base):
         self._classical_memory = 0
         self._classical_register = 0
         data = {}
+        shadow_exp = copy.deepcopy(experiment) if self._fp64_check and self._precision == 'single' else None
         if any(op.name == 'bfunc' for op in experiment.instructions):
             raise BasicAerError('dm_simulator does not support conditional (bfunc) operations')
         self._dev = self._state_factory(n, precision=self._precision, fusion=self._fusion,
                                         tile_axes=self._tile_axes, rounds=self._register_rounds,
-                                        tensor_cores=self._tensor_cores)
+                                        tensor_cores=self._tensor_cores, tma=self._tma)
         if self._record_next:
             self._dev.record()
         launches0 = N.lib().dm_kernel_launch_count()
@@ -718,6 +734,7 @@ class DmSimulatorGPU(_Base):
                     raise BasicAerError(err_msg.format(self.name(), name))
             self._add_decoherence_and_amp_decay(clock, f=mem['decoherence'], p=mem['thermalization'],
                                                 g=mem['amplitude_decay'])
+        trace_err = self._check_trace()
         if self.SHOW_FINAL_STATE and self._coefficients_to_host:
             if self._get_den_mat:
                 data['coeffmatrix'], data['densitymatrix'] = self._get_densitymatrix()
@@ -725,6 +742,9 @@ class DmSimulatorGPU(_Base):
                 data['coeffmatrix'] = self._get_densitymatrix()
             if self._fidelity is not None:
                 data['fidelity'] = self._fidelity
+        if shadow_exp is not None:
+            data.update(self._fp64_statement(shadow_exp, data))
+            data['trace_err'] = trace_err
         self._dev.synchronize()
         end_runtime = time.time()
         self.last_run_stats = {'passes': self._dev.passes_run, 'levels': levels,
@@ -743,6 +763,50 @@ class DmSimulatorGPU(_Base):
                 'processing_time_taken': -start_processing + end_processing,
                 'running_time_taken': -start_runtime + end_runtime,
                 'header': experiment.header.as_dict()}
+
+    # ------------------------------------------------------- result checks
+    TRACE_TOL = {'double': 1e-12, 'single': 1e-6}
+
+    def _check_trace(self):
+        """Trace preservation after the run: |2**n a_0 - 1| (a_0 read in FP64 on the device).
+
+        The maps of every gate, channel and measurement keep a_0 = 2**-n
+        (their I row is (1, 0, 0, 0)); a departure means the state was
+        corrupted.  Same test as the reference's initial-state check
+        (dm_simulator.py:363), applied to the final state."""
+        err = self._dev.trace_error()
+        if not err <= self.TRACE_TOL[self._precision]:
+            raise BasicAerError('Trace of densitymatrix is not one after the run: |2^n a_0 - 1| = %.3g (> %g)'
+                                % (err, self.TRACE_TOL[self._precision]))
+        return err
+
+    def _fp64_statement(self, experiment, data):
+        """Error statement of an FP32 result: the same experiment run in FP64 on the device.
+
+        Returns max_abs_coeff_err = max |2**n (a32 - a64)| over the final
+        states (compared on the device) and prob_l1_err = the largest L1
+        distance between a probability output of this run and the FP64 run's."""
+        shadow = copy.copy(self)
+        shadow._precision = 'double'
+        shadow._fp64_check = False
+        shadow._coefficients_to_host = False
+        shadow._counts_shots = 0
+        shadow._record_next = True
+        shadow._dev = None
+        ref = shadow.run_experiment(experiment)
+        st64 = shadow.recorded_state
+        n = self._number_of_qubits
+        max_abs = self._dev.max_abs_diff(st64) * 2.0 ** n
+        del st64
+        shadow.recorded_state = None
+        l1 = 0.0
+        for k, v in ref['data'].items():
+            g = data.get(k)
+            if isinstance(v, dict) and isinstance(g, dict) and list(g.keys()) == list(v.keys()):
+                a = np.array([float(x) for x in g.values()])
+                b = np.array([float(x) for x in v.values()])
+                l1 = max(l1, float(np.abs(a - b).sum()))
+        return {'max_abs_coeff_err': max_abs, 'prob_l1_err': l1}
 
     # ---------------------------------------------------------------- outputs
     def _compute_densitymatrix(self, dmpauli=None):

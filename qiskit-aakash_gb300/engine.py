@@ -14,7 +14,8 @@ import numpy as np
 
 from . import _native as N
 from .exceptions import BasicAerError
-from .program import TC_AXES, Op, TcPlanError, cx_coefficients, encode_pass, encode_pass_tc, plan_passes
+from .program import (TC_AXES, Op, TcPlanError, cx_coefficients, encode_pass, encode_pass_tc, encode_pass_tma,
+                      plan_passes)
 
 # Tile sizes of the fused pass: 4**6 FP64 = 32 KB and 4**7 FP32 = 64 KB of
 # shared memory per tile; the two lowest qubit axes (16 contiguous
@@ -138,7 +139,7 @@ class DeviceState:
     """An n-qubit Pauli-coefficient vector on a CUDA device."""
 
     def __init__(self, n, precision='double', fusion=True, tile_axes=None, low_axes=DEFAULT_LOW_AXES,
-                 device=None, rounds=True, tensor_cores=True):
+                 device=None, rounds=True, tensor_cores=True, tma=True):
         torch = _torch()
         if not torch.cuda.is_available():
             raise BasicAerError('dm_simulator (GB300) needs a CUDA device; none is visible')
@@ -158,6 +159,8 @@ class DeviceState:
         self.rounds = rounds
         # FP32 passes of 7 resident axes run on the tensor cores (3-way FP16 split)
         self.tensor_cores = bool(tensor_cores) and precision == 'single' and n >= TC_AXES
+        self.tma = bool(tma)      # TMA-fed tensor-core passes where a pass fits them
+        self.passes_by_kernel = {'tma': 0, 'tc': 0, 'cuda_cores': 0}
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device) if self.tensor_cores else None
         self.kmax = min(tile_axes or DEFAULT_TILE_AXES[precision], N.DM_MAX_TILE_AXES)
         self.low = low_axes
@@ -271,23 +274,42 @@ class DeviceState:
         else:
             self._run_passes(passes)
 
+    def _encode_tc(self, p):
+        """(entry point, descriptor, FP16 images) of a pass on the tensor cores, or None.
+
+        The TMA-fed kernel takes passes of up to 6 rounds whose resident axes
+        fit a 5-dimensional tensor map; other passes run on the cp.async-fed
+        kernel; a pass with more rounds than a descriptor holds, on neither."""
+        if self.tma:
+            umats = []
+            try:
+                return 'dm_apply_pass_tma', encode_pass_tma(p, self.n, umats), umats
+            except TcPlanError:
+                pass
+        umats = []
+        try:
+            return 'dm_apply_pass_tc', encode_pass_tc(p, self.n, umats), umats
+        except TcPlanError:
+            return None
+
     def _run_passes_tc(self, passes):
         """Encode and launch pass by pass: the host plans pass i+1 while the GPU runs pass i."""
         torch = _torch()
         sp = ctypes.c_void_p(self.status.data_ptr())
         keep = []
         for p in passes:
-            umats = []
-            try:
-                d = encode_pass_tc(p, self.n, umats)
-            except TcPlanError:
+            enc = self._encode_tc(p)
+            if enc is None:
                 self._run_passes([p])     # more rounds than a descriptor holds: the CUDA-core pass
+                self.passes_by_kernel['cuda_cores'] += 1
                 continue
+            name, d, umats = enc
+            self.passes_by_kernel['tma' if name == 'dm_apply_pass_tma' else 'tc'] += 1
             host = np.concatenate(umats).view(np.int16)      # FP16 bit patterns
             h = torch.from_numpy(host).pin_memory()
             dev = h.to(self.device, non_blocking=True)
             self.h2d_bytes += host.nbytes
-            self._call('dm_apply_pass_tc', self.ptr, self.n, ctypes.byref(d), ctypes.c_void_p(dev.data_ptr()),
+            self._call(name, self.ptr, self.n, ctypes.byref(d), ctypes.c_void_p(dev.data_ptr()),
                        ctypes.c_size_t(host.size), sp, self.stream, keep=(d, dev))
             keep.append((h, dev, d))
         self.passes_run += len(keep)
@@ -359,7 +381,10 @@ class DeviceState:
         self._call('dm_sample_counts', ctypes.c_void_p(probs.data_ptr()), m, ctypes.c_int64(int(shots)),
                    ctypes.c_uint64(int(seed) & (2 ** 64 - 1)), ctypes.c_void_p(counts.data_ptr()),
                    ctypes.c_void_p(scratch.data_ptr()), self.stream, keep=(counts, scratch))
-        return self._to_host(counts)
+        out = self._to_host(counts)
+        if shots > 0 and int(out.sum()) != int(shots):
+            raise BasicAerError('cannot draw counts: no outcome has a positive probability')
+        return out
 
     def gather(self, indices):
         self.flush()
@@ -464,6 +489,25 @@ class DeviceState:
         N.call('dm_overlap', self.ptr, ctypes.c_void_p(b.data_ptr()), self.n, self.dtype,
                ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(scratch.data_ptr()), self.stream)
         return float(self._to_host(out)[0])
+
+    def max_abs_diff(self, other):
+        """max |a_s - b_s| against another device state of the same size (FP64, on the device)."""
+        self.flush()
+        other.flush()
+        if other.n != self.n:
+            raise BasicAerError('states of %d and %d qubits cannot be compared' % (self.n, other.n))
+        out = _torch().empty(1, dtype=_torch().float64, device=self.device)
+        N.call('dm_max_abs_diff', self.ptr, self.dtype, other.ptr, other.dtype, self.n,
+               ctypes.c_void_p(out.data_ptr()), self.stream)
+        return float(self._to_host(out)[0])
+
+    def trace_error(self):
+        """|2**n a_0 - 1| of the current state, a_0 read from the device in FP64 (not recorded)."""
+        self.flush()
+        o = _torch().empty(1, dtype=_torch().float64, device=self.device)
+        idx = (ctypes.c_int64 * 1)(0)
+        N.call('dm_gather', self.ptr, self.n, self.dtype, idx, 1, ctypes.c_void_p(o.data_ptr()), self.stream)
+        return abs(float(self._to_host(o)[0]) * 2.0 ** self.n - 1.0)
 
     def synchronize(self):
         _torch().cuda.synchronize(self.device)

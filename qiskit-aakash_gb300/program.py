@@ -501,6 +501,15 @@ def nat_swz(e):
     return e ^ ((((e >> 5) ^ (e >> 8)) & 7) << 2)
 
 
+def nat_linear(e):
+    """Element position of tile element e in a TMA box (dense, unswizzled)."""
+    return e
+
+
+# natural-tile layouts: 'xor' for the cp.async-fed pass (dm_apply_pass_tc), 'linear' for the TMA-fed pass
+NAT_MAPS = {'xor': nat_swz, 'linear': nat_linear}
+
+
 class TcLayout:
     """Digit order (3 local axes) and row-bit order (8 tile bits) of one round's operand."""
 
@@ -549,22 +558,24 @@ def _transition_cost(src, dst_off, vec):
     return n * w + n // 4
 
 
-def _conversion_cost(layout):
+def _conversion_cost(layout, nat='xor'):
     """Shared-memory load wavefronts of one warp converting the natural tile into round 0 (layout).
 
     A warp's lanes are (row bits 0-2, chunk bits = K bits 3-4) of 8-value
     chunks; with local axis 0 as digit 0 the 8 values are two 16-byte loads,
     otherwise eight 4-byte loads."""
-    offs = tuple(4 * nat_swz(1 << tb) for tb in layout.rowbits[:3]) + \
-        tuple(4 * nat_swz(1 << tb) for tb in layout.kbits[3:5])
+    f = NAT_MAPS[nat]
+    offs = tuple(4 * f(1 << tb) for tb in layout.rowbits[:3]) + \
+        tuple(4 * f(1 << tb) for tb in layout.kbits[3:5])
     vec = layout.digits[0] == 0
     w = _store_wavefronts(offs, 16 if vec else 4)
     return (2 if vec else 8) * w
 
 
-def _natural_cost(layout):
+def _natural_cost(layout, nat='xor'):
     vec = 16 if _vec_digit(layout, 0) >= 0 else 0
-    return _transition_cost(layout, lambda tb: 4 * nat_swz(1 << tb), vec)
+    f = NAT_MAPS[nat]
+    return _transition_cost(layout, lambda tb: 4 * f(1 << tb), vec)
 
 
 def _fill_rows(first, lanes, keep, nonround):
@@ -592,7 +603,7 @@ def _best_next_cost(cand, next_axes):
 
 
 @functools.lru_cache(maxsize=4096)
-def _choose_layouts_cached(rounds_axes):
+def _choose_layouts_cached(rounds_axes, nat='xor'):
     import itertools
     layouts = []
     prev = None
@@ -609,8 +620,8 @@ def _choose_layouts_cached(rounds_axes):
             for digits in orders:
                 for tri in itertools.combinations(nonround, 3):
                     cand = TcLayout(list(digits), _fill_rows(list(tri), [], [], nonround))
-                    cost = _conversion_cost(cand)
-                    cost += _best_next_cost(cand, nxt_axes) if nxt_axes else _natural_cost(cand)
+                    cost = _conversion_cost(cand, nat)
+                    cost += _best_next_cost(cand, nxt_axes) if nxt_axes else _natural_cost(cand, nat)
                     if best is None or cost < best[0]:
                         best = (cost, cand)
             layouts.append(best[1])
@@ -632,7 +643,7 @@ def _choose_layouts_cached(rounds_axes):
                                                              lanes, keep, nonround))
                     vec = 8 if _vec_digit(prev, cand.digits[0]) >= 0 else None
                     cost = _transition_cost(prev, cand.byte_of_bit, vec)
-                    cost += _natural_cost(cand) if ri == nlast else _best_next_cost(cand, nxt_axes)
+                    cost += _natural_cost(cand, nat) if ri == nlast else _best_next_cost(cand, nxt_axes)
                     if best is None or cost < best[0]:
                         best = (cost, cand)
         layouts.append(best[1])
@@ -640,7 +651,7 @@ def _choose_layouts_cached(rounds_axes):
     return tuple(layouts)
 
 
-def _choose_layouts(rounds_axes):
+def _choose_layouts(rounds_axes, nat='xor'):
     """Pick each round's digit order and row-bit order (greedy along the rounds, one round of lookahead).
 
     The epilogue of round r (one source row per thread) writes round r+1's
@@ -650,9 +661,10 @@ def _choose_layouts(rounds_axes):
     axes (8-byte vector stores).  Each candidate (digit order, which source
     lane bits become row bits 0-2, which bit becomes row 3) is scored by the
     exact wavefront count of its incoming epilogue plus the cheapest
-    outgoing one; the last round pays for its stores into the natural tile.
+    outgoing one; the last round pays for its stores into the natural tile
+    (``nat`` names that tile's layout, see NAT_MAPS).
     """
-    return list(_choose_layouts_cached(tuple(tuple(sorted(a)) for a in rounds_axes)))
+    return list(_choose_layouts_cached(tuple(tuple(sorted(a)) for a in rounds_axes), nat))
 
 
 def _vec_digit(src, dst_first_axis):
@@ -701,11 +713,11 @@ def epilogue_wavefronts(src, dst, natural=False):
     return total
 
 
-def plan_tc_pass(p, n):
+def plan_tc_pass(p, n, nat='xor'):
     """Pad a pass to 7 axes, plan its rounds and their layouts, compose each round's U (FP64)."""
     pp = pad_pass(p, n)
     rounds = plan_rounds(pp, 3, pad='neighbors')
-    layouts = _choose_layouts([axes for axes, _ in rounds])
+    layouts = _choose_layouts([axes for axes, _ in rounds], nat)
     mats = []
     for (axes, rops), lay in zip(rounds, layouts):
         U = np.eye(64)
@@ -715,10 +727,11 @@ def plan_tc_pass(p, n):
     return pp, layouts, mats
 
 
-def tc_tables(layouts):
+def tc_tables(layouts, nat='xor'):
     """Conversion and per-round epilogue tables of a tensor-core pass (see dm_tc_pass)."""
+    f = NAT_MAPS[nat]
     L0 = layouts[0]
-    conv = {'natrow': [nat_swz(1 << tb) for tb in L0.rowbits], 'natk': [nat_swz(1 << tb) for tb in L0.kbits],
+    conv = {'natrow': [f(1 << tb) for tb in L0.rowbits], 'natk': [f(1 << tb) for tb in L0.kbits],
             'vec0': 0 if L0.digits[0] == 0 else -1}
     rounds = []
     for r, L in enumerate(layouts):
@@ -728,19 +741,17 @@ def tc_tables(layouts):
             kc = [nxt.byte_of_bit(tb) for tb in L.kbits]
             vec = _vec_digit(L, nxt.digits[0])
         else:
-            rowc = [nat_swz(1 << tb) for tb in L.rowbits]
-            kc = [nat_swz(1 << tb) for tb in L.kbits]
+            rowc = [f(1 << tb) for tb in L.rowbits]
+            kc = [f(1 << tb) for tb in L.kbits]
             vec = _vec_digit(L, 0)
         rounds.append({'digits': L.digits, 'rowc': rowc, 'kc': kc, 'vec': vec})
     return conv, rounds
 
 
-def encode_pass_tc(p, n, umats):
-    """DmTcPass for dm_apply_pass_tc; appends the rounds' FP16 matrix images (uint16) to ``umats``."""
-    pp, layouts, mats = plan_tc_pass(p, n)
+def _encode_tc(pp, layouts, mats, nat, image, umats):
     if len(layouts) > N.DM_MAX_ROUNDS:
         raise TcPlanError('pass needs %d rounds (> %d)' % (len(layouts), N.DM_MAX_ROUNDS))
-    conv, rounds = tc_tables(layouts)
+    conv, rounds = tc_tables(layouts, nat)
     dp = N.DmTcPass()
     for r, q in enumerate(pp.axes):
         dp.axes[r] = q
@@ -761,7 +772,76 @@ def encode_pass_tc(p, n, umats):
         for i in range(6):
             o.kc[i] = rd['kc'][i]
         o.umoff = off
-        img = tc_round_image(U)
+        img = image(U)
         umats.append(img)
         off += img.size
     return dp
+
+
+def encode_pass_tc(p, n, umats):
+    """DmTcPass for dm_apply_pass_tc; appends the rounds' FP16 matrix images (uint16) to ``umats``."""
+    pp, layouts, mats = plan_tc_pass(p, n)
+    return _encode_tc(pp, layouts, mats, 'xor', tc_round_image, umats)
+
+
+# ---------------------------------------------------------------------------
+# TMA-fed tensor-core pass (dm_apply_pass_tma)
+# ---------------------------------------------------------------------------
+
+TMA_MAX_ROUNDS = 6        # round images resident in shared memory
+TMA_MAX_DIMS = 5          # tensor-map rank
+TMA_IMAGE_HALVES = 2 * 4096
+
+
+def tc_round_image_tma(U):
+    """8192 uint16 (FP16 bits) of U (64x64, FP64), each K-major: Uh, then Ul = fp16(2**11 (U - Uh)).
+
+    Adjacent, so that [Uh ; Ul] is one 128-row operand (h x [Uh ; Ul]) and
+    its first half the operand of l x Uh."""
+    U = np.asarray(U, dtype=np.float64)
+    uh = U.astype(np.float16)
+    parts = [uh, ((U - uh.astype(np.float64)) * TC_LO_SCALE).astype(np.float16)]
+    img = np.zeros(TMA_IMAGE_HALVES, dtype=np.uint16)
+    for i, part in enumerate(parts):
+        img[4096 * i + _KMAJOR] = part.view(np.uint16).reshape(-1)
+    return img
+
+
+def tma_box_dims(n, axes):
+    """Tensor-map dimensions of a tile of resident qubits ``axes``: [(start digit, length, gap above)].
+
+    Runs of consecutive resident digit positions (qubit q has position
+    n-1-q), split into chunks of at most 4 digits; gap counts the
+    non-resident digits between a chunk and the next one (or the top).
+    Mirrors tma_dims() in csrc/dm_tma.cu."""
+    res = set(n - 1 - q for q in axes)
+    dims, pos = [], 0
+    if 0 not in res:
+        return None
+    while pos < n:
+        length = 0
+        while pos + length < n and pos + length in res and length < 4:
+            length += 1
+        gap = 0
+        while pos + length + gap < n and pos + length + gap not in res:
+            gap += 1
+        dims.append((pos, length, gap))
+        pos += length + gap
+    return dims
+
+
+def tma_eligible(pp, n, nrounds):
+    dims = tma_box_dims(n, pp.axes)
+    return dims is not None and len(dims) <= TMA_MAX_DIMS and nrounds <= TMA_MAX_ROUNDS
+
+
+def encode_pass_tma(p, n, umats):
+    """DmTcPass for dm_apply_pass_tma (natural tile unswizzled, [Uh ; Ul] images).
+
+    Raises TcPlanError when the pass has more rounds than stay resident or
+    its resident digits need more tensor-map dimensions than TMA has."""
+    pp, layouts, mats = plan_tc_pass(p, n, nat='linear')
+    if not tma_eligible(pp, n, len(layouts)):
+        raise TcPlanError('pass does not fit the TMA-fed kernel (%d rounds, dims %s)'
+                          % (len(layouts), tma_box_dims(n, pp.axes)))
+    return _encode_tc(pp, layouts, mats, 'linear', tc_round_image_tma, umats)

@@ -1,12 +1,12 @@
 """Generate the golden fixtures by running the reference's own dm_simulator.
 
-Run once in a container that has the reference tree at /root/reference
-(or DM_REFERENCE_ROOT)::
+Run once where the reference tree is checked out, with ``DM_REFERENCE_ROOT``
+pointing at it::
 
-    python tests/golden/make_golden.py
+    DM_REFERENCE_ROOT=<reference tree> python tests/golden/make_golden.py
 
 It loads the unmodified ``dm_simulator.py`` / ``basicaertools.py`` through
-``refload.py`` and records, for every case:
+``oracle/refload.py`` and records, for every case:
 
 * the input (instructions, qubit count, backend options) in ``cases.json``;
 * the reference's level structure (``single_gate_merge`` + ``partition``)
@@ -36,8 +36,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, HERE)
 sys.path.insert(0, REPO)
 
-import refload  # noqa: E402
-from oracle import dm_oracle  # noqa: E402
+from oracle import dm_oracle, refload  # noqa: E402
 
 
 def _load_pkg():

@@ -66,7 +66,7 @@ def oracle_probs(spec):
 def test_batch_tables_replay_equals_oracle(precision):
     specs = B.sweep_specs(12, seed=3, n_range=(3, 6), depth_range=(2, 9))
     T = B.BatchTables(specs, precision)
-    tol = 1e-12 if precision == 'double' else 2e-5
+    tol = 1e-12 if precision == 'double' else 1e-6
     for i, spec in enumerate(specs):
         got = emulate_instance(T, i)
         assert np.max(np.abs(got - oracle_probs(spec))) < tol, (i, spec)
@@ -239,3 +239,20 @@ def test_derived_recording_refuses_a_different_structure():
     assert B.derive_recording(ref, dict(b, depth=5)) is None          # one more layer of gates
     assert B.derive_recording(ref, dict(b, n=8)) is None
     assert B.derive_recording(ref, dict(b, decoherence=1.0, decay=1.0, depolarisation=0.0)) is None
+
+
+def test_derived_recording_refuses_other_cx_pairs_or_read_out():
+    """The CX (control, target) sequence and the Z read-out of every qubit are compared with the
+    reference recording, not copied from it."""
+    import copy
+    a, b = B.sweep_specs(2, seed=6, n_range=(7, 7), depth_range=(4, 4))
+    ref = B.compile_experiment(*B.instance_experiment(a))
+    assert B.derive_recording(ref, b) is not None
+    swapped = copy.deepcopy(ref)
+    i = next(k for k, op in enumerate(swapped.ops) if op.kind == 'cx')
+    swapped.ops[i].axes = tuple(reversed(swapped.ops[i].axes))        # control and target exchanged
+    assert B.derive_recording(swapped, b) is None
+    other = copy.deepcopy(ref)
+    kind, pos, mode, err = other.readouts[0]
+    other.readouts = [(kind, pos, [1] * len(mode), err)]                # an X read-out
+    assert B.derive_recording(other, b) is None

@@ -115,6 +115,50 @@ def test_malformed_pass_is_rejected_on_host(lib):
     assert rc == N.DM_ERR_PROGRAM
 
 
+def test_malformed_tma_pass_is_rejected_on_host(lib):
+    """dm_apply_pass_tma checks its descriptor before any CUDA call (here there is no GPU)."""
+    import numpy as np
+    from qiskit_aakash_gb300 import program as P
+    n = 10
+    ops = [P.Op('map1', (q,), np.eye(4)) for q in range(n)]
+    passes = P.plan_passes(ops, n, 7, 2)
+    umats = []
+    good = P.encode_pass_tma(passes[0], n, umats)
+    count = sum(m.size for m in umats)
+    dev = ctypes.c_void_p(1 << 20)
+
+    def run(d, cnt=count, state=dev):
+        return lib.dm_apply_pass_tma(state, n, ctypes.byref(d), dev, ctypes.c_size_t(cnt), dev, None)
+
+    def copy():
+        return N.DmTcPass.from_buffer_copy(bytes(good))
+
+    assert run(copy(), state=ctypes.c_void_p(None)) == N.DM_ERR_ARG
+    assert run(copy(), state=ctypes.c_void_p((1 << 20) + 4)) == N.DM_ERR_ARG     # unaligned state
+    assert run(copy(), cnt=count - 8) == N.DM_ERR_PROGRAM                         # images beyond the buffer
+    bad = copy()
+    bad.nrounds = P.TMA_MAX_ROUNDS + 1
+    assert run(bad) == N.DM_ERR_PROGRAM
+    bad = copy()
+    bad.axes[0] = n - 2                                                           # lowest axis not resident
+    assert run(bad) == N.DM_ERR_PROGRAM
+    bad = copy()
+    bad.natrow[0] = 3                                                             # not a power of two
+    assert run(bad) == N.DM_ERR_PROGRAM
+    bad = copy()
+    bad.rounds[bad.nrounds - 1].kc[0] = 1 << 14                                   # beyond the natural tile
+    assert run(bad) == N.DM_ERR_PROGRAM
+    bad = copy()
+    bad.rounds[0].umoff = 4                                                       # images not 16-byte aligned
+    assert run(bad) == N.DM_ERR_PROGRAM
+    # seven isolated resident qubits need seven tensor-map dimensions
+    bad = copy()
+    for r, q in enumerate([16, 14, 12, 10, 8, 6, 4]):
+        bad.axes[r] = q
+    assert lib.dm_apply_pass_tma(dev, 17, ctypes.byref(bad), dev, ctypes.c_size_t(count), dev, None) \
+        == N.DM_ERR_PROGRAM
+
+
 def test_malformed_tensor_core_batch_tables_are_rejected_on_host(lib):
     """dm_batch_run_tc / dm_batch_run_params_tc validate every table before any CUDA call."""
     from qiskit_aakash_gb300 import batch as B

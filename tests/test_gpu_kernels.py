@@ -228,6 +228,67 @@ def test_tensor_core_pass_equals_program_order(torch, n):
     assert np.max(np.abs(got - ref)) * 2.0 ** n < 2e-6
 
 
+def _physical_ops(rng, n, count):
+    """Random ops made trace-preserving and contractive (see test_tensor_core_pass_equals_program_order)."""
+    from test_planner import random_ops
+    ops = random_ops(rng, n, count)
+    for op in ops:
+        if op.kind == 'map1':
+            m = op.data / np.abs(op.data).sum(axis=1, keepdims=True)
+            m[0] = (1.0, 0.0, 0.0, 0.0)
+            op.data = m
+        elif op.kind == 'diag2':
+            op.data = np.clip(op.data, -1, 1)
+            op.data[0] = 1.0
+        elif op.kind == 'map2':
+            m = op.data / np.abs(op.data).sum(axis=1, keepdims=True)
+            m[0] = 0.0
+            m[0, 0] = 1.0
+            op.data = m
+    return ops
+
+
+@pytest.mark.parametrize('n', [7, 8, 10, 12])
+def test_tma_pass_equals_program_order(torch, n):
+    """dm_apply_pass_tma (TMA-fed tiles, resident round images) against the ops applied in FP64,
+    and against dm_apply_pass_tc on the same passes (same split arithmetic)."""
+    from test_planner import apply_op
+    rng = np.random.default_rng(4000 + n)
+    ops = _physical_ops(rng, n, 80)
+    st = rng.uniform(-1, 1, size=4 ** n) * 2.0 ** -n
+    st[0] = 2.0 ** -n
+    ref = st.copy()
+    for op in ops:
+        ref = apply_op(ref, n, op)
+    passes = P.plan_passes(ops, n, 7, 2)
+    status = torch.zeros(1, dtype=torch.int32, device='cuda')
+    t_tma = dev(torch, st, np.float32)
+    t_tc = dev(torch, st, np.float32)
+    used = 0
+    for p in passes:
+        for name, enc, t in (('dm_apply_pass_tma', P.encode_pass_tma, t_tma), ('dm_apply_pass_tc', P.encode_pass_tc, t_tc)):
+            umats = []
+            try:
+                d = enc(p, n, umats)
+            except P.TcPlanError:
+                d = None
+            if d is None:     # a pass the TMA kernel does not take: the cp.async kernel for both
+                umats = []
+                d, name = P.encode_pass_tc(p, n, umats), 'dm_apply_pass_tc'
+            elif name == 'dm_apply_pass_tma':
+                used += 1
+            m = np.concatenate(umats)
+            md = torch.from_numpy(m.view(np.int16)).cuda()
+            N.call(name, vp(t), n, ctypes.byref(d), vp(md), ctypes.c_size_t(m.size), vp(status), stream(torch))
+            torch.cuda.synchronize()
+    assert used > 0
+    assert status.item() == 0
+    got = t_tma.double().cpu().numpy()
+    other = t_tc.double().cpu().numpy()
+    assert np.max(np.abs(got - ref)) * 2.0 ** n < 2e-6
+    assert np.max(np.abs(got - other)) * 2.0 ** n < 1e-6
+
+
 def test_tensor_core_pass_rejects_bad_programs(torch):
     """Malformed tensor-core descriptors are refused on the host (no launch)."""
     n = 8

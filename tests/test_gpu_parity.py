@@ -8,7 +8,9 @@
   size-independent properties.
 
 Tolerances: FP64 paths agree with the reference to 1e-12 on the Pauli
-expectations 2**n a_s and on probabilities; FP32 paths to 2e-5.
+expectations 2**n a_s and on probabilities; FP32 paths (CUDA cores and the
+tensor-core FP16 split) to FP32_TOL = 1e-6 on the same values, and the L1
+distance of every probability distribution to 1e-6 as well.
 """
 import copy
 
@@ -23,6 +25,7 @@ from test_oracle import compare_outputs
 pytestmark = pytest.mark.gpu
 
 CASES = [c for c in G.cases() if 'error' not in c]
+FP32_TOL = 1e-6      # max-abs of 2**n a_s and of probabilities, and probability L1, for FP32 results
 
 
 @pytest.fixture(scope='module', autouse=True)
@@ -60,7 +63,7 @@ def test_golden_fp64_one_sweep_per_op(c):
 @pytest.mark.parametrize('c', CASES[::2], ids=lambda c: c['name'])
 def test_golden_fp32_fused(c):
     res, _ = run_gpu(G.experiment(c), G.options(c), precision='single')
-    compare_outputs(c, res['data'], rel=2e-5)
+    compare_outputs(c, res['data'], rel=FP32_TOL, l1=FP32_TOL)
 
 
 def _oracle(exp, opts):
@@ -73,6 +76,8 @@ def _assert_close(a, b, n, rel):
         if isinstance(v, dict):
             assert list(g.keys()) == list(v.keys())
             np.testing.assert_allclose(list(g.values()), list(v.values()), rtol=0, atol=rel)
+            l1 = np.abs(np.array(list(g.values()), dtype=float) - np.array(list(v.values()), dtype=float)).sum()
+            assert l1 <= max(rel, 1e-12 * len(v)), (k, l1)
         elif k == 'coeffmatrix':
             np.testing.assert_allclose(np.asarray(g) * 2 ** n, np.asarray(v) * 2 ** n, rtol=0, atol=rel)
         else:
@@ -91,9 +96,10 @@ def test_workloads_match_oracle(n, layers, seed, every_gate, qft):
     opts['compute_densitymatrix'] = False
     ref = _oracle(qc.to_experiment(), opts)
     for kw, tol in (({}, 1e-12), ({'tile_axes': 7}, 1e-12), ({'tile_axes': 4}, 1e-12),
-                    ({'register_rounds': False}, 1e-12), ({'precision': 'single'}, 2e-5),
-                    ({'precision': 'single', 'tensor_cores': False}, 2e-5),
-                    ({'precision': 'single', 'tensor_cores': False, 'register_rounds': False}, 2e-5)):
+                    ({'register_rounds': False}, 1e-12), ({'precision': 'single'}, FP32_TOL),
+                    ({'precision': 'single', 'tma': False}, FP32_TOL),
+                    ({'precision': 'single', 'tensor_cores': False}, FP32_TOL),
+                    ({'precision': 'single', 'tensor_cores': False, 'register_rounds': False}, FP32_TOL)):
         got, b = run_gpu(qc.to_experiment(), opts, **kw)
         assert got['number_of_clock_cycles'] == ref['number_of_clock_cycles']
         _assert_close(got, ref, n, tol)
@@ -112,9 +118,12 @@ def test_fourteen_qubit_properties():
     assert abs(p.sum() - 1.0) < 1e-12 and p.min() > -1e-12
     assert b.last_run_stats['passes'] < fused['number_of_clock_cycles']
     single, _ = run_gpu(qc.to_experiment(), opts, precision='single')
-    np.testing.assert_allclose(single['data']['coeffmatrix'] * 2 ** n, a * 2 ** n, rtol=0, atol=2e-5)
+    np.testing.assert_allclose(single['data']['coeffmatrix'] * 2 ** n, a * 2 ** n, rtol=0, atol=FP32_TOL)
     cuda_cores, _ = run_gpu(qc.to_experiment(), opts, precision='single', tensor_cores=False)
-    np.testing.assert_allclose(cuda_cores['data']['coeffmatrix'] * 2 ** n, a * 2 ** n, rtol=0, atol=2e-5)
+    np.testing.assert_allclose(cuda_cores['data']['coeffmatrix'] * 2 ** n, a * 2 ** n, rtol=0, atol=FP32_TOL)
+    for r in (single, cuda_cores):
+        p32 = np.array(list(r['data']['ensemble_probability'].values()))
+        assert np.abs(p32 - p).sum() <= FP32_TOL
     unfused, _ = run_gpu(qc.to_experiment(), opts, fusion=False)
     np.testing.assert_allclose(unfused['data']['coeffmatrix'] * 2 ** n, a * 2 ** n, rtol=0, atol=1e-12)
 
@@ -162,7 +171,7 @@ def test_tensor_core_round_overflow_falls_back_to_the_cuda_core_pass():
     opts['compute_densitymatrix'] = False
     ref = _oracle(qc.to_experiment(), opts)
     got, _ = run_gpu(qc.to_experiment(), opts, precision='single')
-    _assert_close(got, ref, n, 2e-5)
+    _assert_close(got, ref, n, FP32_TOL)
 
 
 @pytest.mark.parametrize('precision', ['double', 'single'])
@@ -182,4 +191,74 @@ def test_streamed_launches_equal_one_flush(precision, monkeypatch):
     assert b1.last_run_stats['passes'] == b2.last_run_stats['passes']
     assert np.array_equal(whole['data']['coeffmatrix'], streamed['data']['coeffmatrix'])
     ref = _oracle(qc.to_experiment(), opts)
-    _assert_close(streamed, ref, n, 1e-12 if precision == 'double' else 2e-5)
+    _assert_close(streamed, ref, n, 1e-12 if precision == 'double' else FP32_TOL)
+
+
+def test_tensor_core_fp32_against_fp64_twelve_qubits_twenty_layers():
+    """12 qubits, 20 noisy layers, noise after every gate: the tensor-core FP32 form (TMA-fed and
+    cp.async-fed) against the FP64 form on the GPU, at the 1e-6 bound on 2**n a_s and probability L1."""
+    n = 12
+    qc = dmg.random_layer_circuit(n, 20, 31, barrier_after_gate=True)
+    opts = dmg.noise_options(depolarisation=1e-3, decoherence=0.995, decay=0.998, rotation_sigma=1e-3)
+    opts['compute_densitymatrix'] = False
+    ref, _ = run_gpu(qc.to_experiment(), opts)
+    a = ref['data']['coeffmatrix']
+    p = np.array(list(ref['data']['ensemble_probability'].values()))
+    for kw in ({}, {'tma': False}):
+        got, b = run_gpu(qc.to_experiment(), opts, precision='single', **kw)
+        assert b.last_run_stats['passes'] > 0
+        err = np.abs(got['data']['coeffmatrix'] - a).max() * 2 ** n
+        p32 = np.array(list(got['data']['ensemble_probability'].values()))
+        assert err <= FP32_TOL, (kw, err)
+        assert np.abs(p32 - p).sum() <= FP32_TOL, kw
+
+
+def test_fp64_check_states_the_fp32_error():
+    """precision='single' with fp64_check: the result states its max-abs coefficient error and
+    probability L1 error against the same experiment in FP64 (and both are within 1e-6)."""
+    n = 9
+    qc = dmg.random_layer_circuit(n, 6, 41, barrier_after_gate=True)
+    qc.measure([0, 3], [0, 3], basis='Ensemble', add_param='X')
+    opts = dmg.noise_options(depolarisation=1e-3, decoherence=0.995, decay=0.998, rotation_sigma=1e-3)
+    opts['compute_densitymatrix'] = False
+    got, _ = run_gpu(qc.to_experiment(), opts, precision='single', fp64_check=True)
+    ref, _ = run_gpu(qc.to_experiment(), opts)
+    d = got['data']
+    assert 0 < d['max_abs_coeff_err'] <= FP32_TOL
+    assert 0 <= d['prob_l1_err'] <= FP32_TOL
+    assert d['trace_err'] <= FP32_TOL
+    host_err = np.abs(d['coeffmatrix'] - ref['data']['coeffmatrix']).max() * 2 ** n
+    assert abs(host_err - d['max_abs_coeff_err']) <= 1e-9
+    p32 = np.array(list(d['ensemble_probability'].values()))
+    p64 = np.array(list(ref['data']['ensemble_probability'].values()))
+    assert np.abs(p32 - p64).sum() <= d['prob_l1_err'] + 1e-15
+    plain, _ = run_gpu(qc.to_experiment(), opts, precision='single')
+    assert 'max_abs_coeff_err' not in plain['data'] and 'trace_err' not in plain['data']
+
+
+@pytest.mark.parametrize('precision', ['double', 'single'])
+def test_trace_violation_raises(precision, monkeypatch):
+    """A state whose trace coefficient left 2**-n is reported as an error after the run.
+
+    The corruption is made on the host: before the final check reads a_0,
+    the state is read back, a_0 is halved and the vector is loaded again
+    through dm_load_state."""
+    from qiskit_aakash_gb300 import engine
+    from qiskit_aakash_gb300.exceptions import BasicAerError
+    n = 8
+    qc = dmg.random_layer_circuit(n, 2, 43)
+    opts = dmg.noise_options(decoherence=0.99, decay=0.99)
+    opts['compute_densitymatrix'] = False
+    ok, _ = run_gpu(qc.to_experiment(), opts, precision=precision)
+    assert ok['success']
+    original = engine.DeviceState.trace_error
+
+    def corrupted(self):
+        a = self.raw_coefficients().astype(np.float64)
+        a[0] *= 0.5
+        self.load(a)
+        return original(self)
+
+    monkeypatch.setattr(engine.DeviceState, 'trace_error', corrupted)
+    with pytest.raises(BasicAerError, match='Trace of densitymatrix is not one after the run'):
+        run_gpu(qc.to_experiment(), opts, precision=precision)

@@ -51,3 +51,12 @@ def test_backend_counts_option():
         assert abs(c - 1e5 * probs[k]) <= 6 * np.sqrt(1e5 * probs[k]) + 2
     res2 = execute(qc, BasicAer.get_backend('dm_simulator'), **copy.deepcopy(opts)).result()['results'][0]['data']
     assert 'counts' not in res2
+
+
+def test_no_positive_probability_draws_nothing():
+    """All-zero (or negative) probabilities: no shot is drawn, every count is 0."""
+    import torch
+    p = np.zeros(16)
+    p[3] = -1e-18
+    c = draw(torch, p, 1000, 5)
+    assert c.sum() == 0

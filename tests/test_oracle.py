@@ -43,8 +43,11 @@ def test_levelling_matches_reference(c):
     _same_levels(sig, c['levels'])
 
 
-def compare_outputs(c, data, rel=1e-12):
-    """Compare a result 'data' dict with the golden outputs of case c."""
+def compare_outputs(c, data, rel=1e-12, l1=None):
+    """Compare a result 'data' dict with the golden outputs of case c.
+
+    rel bounds every value (Pauli expectations 2**n a_s, probabilities);
+    l1, when given, also bounds the L1 distance of each probability dictionary."""
     n = c['n']
     scale = 2.0 ** n          # coefficients are Pauli expectations / 2**n
     for k, key in c['outputs'].items():
@@ -54,6 +57,8 @@ def compare_outputs(c, data, rel=1e-12):
         if isinstance(got, dict):
             assert list(got.keys()) == c['dict_keys'][k]
             got = np.array([float(v) for v in got.values()])
+            if l1 is not None:
+                assert np.abs(got - ref).sum() <= l1, (k, np.abs(got - ref).sum())
         got = np.asarray(got)
         if k == 'coeffmatrix':
             np.testing.assert_allclose(got * scale, ref * scale, rtol=0, atol=rel)

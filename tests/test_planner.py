@@ -308,6 +308,146 @@ def test_tensor_core_tables_emulated():
     np.testing.assert_allclose(got, ref, rtol=0, atol=1e-10 * np.abs(ref).max())
 
 
+def _tma_tile_index(n, dims, t):
+    """Global element of each shared-memory position of tile t, as the TMA box delivers it.
+
+    Dimension i: stride 4**start, box 4**len, coordinate ((t >> 2 g) & (4**gap - 1)) * 4**len
+    with g the non-resident digits below its gap (tile_coords in csrc/dm_tma.cu); the box
+    lands densely in dimension order."""
+    idx = np.zeros(1, dtype=np.int64)
+    g = 0
+    for start, length, gap in dims:
+        c = ((t >> (2 * g)) & ((1 << (2 * gap)) - 1)) << (2 * length)
+        x = np.arange(4 ** length, dtype=np.int64)
+        idx = (idx[None, :] + ((c + x) * 4 ** start)[:, None]).reshape(-1)
+        g += gap
+    return idx
+
+
+def _emulate_tma_pass(st, n, p):
+    """numpy model of dm_apply_pass_tma: TMA box addressing, linear natural tables, exact arithmetic."""
+    pp, layouts, mats = P.plan_tc_pass(p, n, nat='linear')
+    conv, rounds = P.tc_tables(layouts, 'linear')
+    dims = P.tma_box_dims(n, pp.axes)
+    out = st.copy()
+    seen = np.zeros(4 ** n, dtype=np.int64)
+
+    def xor_bits(x, c):
+        o = 0
+        for i, ci in enumerate(c):
+            if (x >> i) & 1:
+                o ^= ci
+        return o
+
+    for t in range(4 ** (n - 7)):
+        idx = _tma_tile_index(n, dims, t)
+        seen[idx] += 1
+        nat = st[idx]
+        A = np.zeros(16384)
+        for row in range(256):
+            nb = xor_bits(row, conv['natrow'])
+            for j in range(64):
+                A[(P._row_off(row) + P._k_off(j)) // 2] = nat[nb ^ xor_bits(j, conv['natk'])]
+        for r, (rd, U) in enumerate(zip(rounds, mats)):
+            X = np.array([[A[(P._row_off(row) + P._k_off(j)) // 2] for j in range(64)] for row in range(256)])
+            D = X @ U.T
+            last = r + 1 == len(rounds)
+            newA = np.zeros(16384)
+            natout = np.zeros(4 ** 7)
+            for row in range(256):
+                b = xor_bits(row, rd['rowc'])
+                for j in range(64):
+                    o = b ^ xor_bits(j, rd['kc'])
+                    if last:
+                        natout[o] = D[row, j]
+                    else:
+                        newA[o // 2] = D[row, j]
+            A = newA
+        out[idx] = natout
+    assert np.all(seen == 1)          # the tiles' boxes cover the state exactly once
+    return out
+
+
+def test_tma_tables_emulated():
+    """The TMA-fed pass's tensor-map boxes and linear tables, replayed in numpy, equal program order."""
+    n = 9
+    rng = np.random.default_rng(23)
+    ops = random_ops(rng, n, 50)
+    st0 = rng.normal(size=4 ** n)
+    ref = st0.copy()
+    for op in ops:
+        ref = apply_op(ref, n, op)
+    got = st0.copy()
+    used = 0
+    for p in P.plan_passes(ops, n, 7, 2):
+        pp, layouts, _ = P.plan_tc_pass(p, n, nat='linear')
+        if P.tma_eligible(pp, n, len(layouts)):
+            got = _emulate_tma_pass(got, n, p)
+            used += 1
+        else:
+            got = _emulate_tc_pass(got, n, p)
+    assert used > 0
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-10 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize('axes_pos', [(0, 1, 2, 3, 4, 5, 6), (0, 1, 4, 5, 6, 9, 10), (0, 3, 5, 7, 9, 11, 13),
+                                      (0, 2, 3, 4, 5, 6, 7), (0, 1, 2, 3, 4, 5, 13)])
+def test_tma_box_dims(axes_pos):
+    """Box dimensions: chunks of <= 4 resident digits, the gaps above them, every tile covered once."""
+    n = 14
+    axes = sorted((n - 1 - x for x in axes_pos), reverse=True)
+    dims = P.tma_box_dims(n, axes)
+    assert sum(length for _, length, _ in dims) == 7
+    assert sum(gap for _, _, gap in dims) == n - 7
+    assert all(1 <= length <= 4 for _, length, _ in dims)
+    if len(dims) <= P.TMA_MAX_DIMS and n <= 10:
+        seen = np.zeros(4 ** n, dtype=np.int64)
+        for t in range(4 ** (n - 7)):
+            seen[_tma_tile_index(n, dims, t)] += 1
+        assert np.all(seen == 1)
+    # shared-memory position e holds the tile's natural element e (local axis r = r-th lowest resident digit)
+    idx = _tma_tile_index(n, dims, 0) if len(dims) <= P.TMA_MAX_DIMS else None
+    if idx is not None:
+        pos = sorted(axes_pos)
+        want = np.array([sum(((e >> (2 * r)) & 3) * 4 ** pos[r] for r in range(7)) for e in range(4 ** 7)])
+        assert np.array_equal(idx, want)
+
+
+def test_tma_tables_are_valid():
+    """TMA-pass tables obey dm_apply_pass_tma's checks (linear natural offsets, operand alignment)."""
+    n = 16
+    rng = np.random.default_rng(5)
+    ops = random_ops(rng, n, 300)
+    for p in P.plan_passes(ops, n, 7, 2):
+        _, layouts, _ = P.plan_tc_pass(p, n, nat='linear')
+        conv, rounds = P.tc_tables(layouts, 'linear')
+        assert all(x > 0 and x & (x - 1) == 0 and x < 16384 for x in conv['natrow'] + conv['natk'])
+        if conv['vec0'] == 0:
+            assert conv['natk'][:2] == [1, 2]
+        for r, rd in enumerate(rounds):
+            c = rd['rowc'] + rd['kc']
+            assert len(set(c)) == 14
+            if r + 1 < len(rounds):
+                assert all(x > 0 and x & (x - 1) == 0 and x < P.TC_A_BYTES for x in c)
+            else:
+                assert all(x > 0 and x & (x - 1) == 0 and x < 16384 for x in c)
+                if rd['vec'] >= 0:
+                    assert rd['kc'][2 * rd['vec']:2 * rd['vec'] + 2] == [1, 2]
+
+
+def test_tma_image_layout_and_split():
+    U = np.random.default_rng(3).normal(size=(64, 64)) / 8
+    img = P.tc_round_image_tma(U)
+    assert img.dtype == np.uint16 and img.size == P.TMA_IMAGE_HALVES
+    uh, ul = (img[4096 * i + P._KMAJOR].view(np.float16).astype(np.float64).reshape(64, 64) for i in range(2))
+    assert np.array_equal(uh, U.astype(np.float16).astype(np.float64))
+    np.testing.assert_allclose(uh + ul / P.TC_LO_SCALE, U, rtol=0, atol=2.0 ** -21 * np.abs(U).max())
+    # the TMA form's first two products equal the cp.async form's up to the power-of-two scale of Uh
+    old = P.tc_round_image(U)
+    assert np.array_equal(old[4096:8192], img[4096:8192])
+    assert np.array_equal(old[8192:], img[:4096])
+
+
 def test_tensor_core_tables_are_valid():
     """Every table entry obeys the kernel's checks (distinct power-of-two operand offsets, alignment)."""
     n = 16
