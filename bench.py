@@ -310,13 +310,64 @@ def all_durations(by_kernel):
     return [d for v in by_kernel.values() for d in v]
 
 
-def device_max_abs_diff(torch, a32, b64, chunk=1 << 28):
-    """max |a - b| over two device vectors (FP32 vs FP64), in chunks (measurement only)."""
-    m = 0.0
-    for s in range(0, a32.numel(), chunk):
-        d = (a32[s:s + chunk].double() - b64[s:s + chunk]).abs().max().item()
-        m = max(m, d)
-    return m
+def fp64_peak(torch, N, seconds=0.5):
+    """Measured FP64 FMA throughput of this GPU (dm_fp64_fma_probe, CUDA events, clocks sampled)."""
+    import ctypes
+    L = N.lib()
+    threads = L.dm_fp64_fma_probe_threads()
+    out = torch.empty(threads, dtype=torch.float64, device='cuda')
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def run(iters):
+        N.call('dm_fp64_fma_probe', ctypes.c_void_p(out.data_ptr()), ctypes.c_int64(iters), sp)
+
+    run(1000)
+    iters = 1000
+    while True:     # grow the launch to about `seconds`
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        run(iters)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        if ms > 1e3 * seconds / 4 or iters > 1 << 30:
+            break
+        iters *= 4
+    with ClockSampler(gpu_uuid(torch)) as clocks:
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(4):
+            run(iters)
+        b.record(stream)
+        torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / 4
+    flops = 2.0 * 8 * iters * threads
+    return {'tflops': flops / (ms / 1e3) / 1e12, 'ms': ms, 'fmas_per_launch': flops / 2,
+            'kernel': 'fp64_fma_probe: 8 independent FMA chains per thread, %d threads' % threads,
+            'clocks': clocks.summary()}
+
+
+def fp64_flops(pkg, qc, opts, tile_axes=6, low=2):
+    """FP64 FLOPs of one run of the circuit as the fused FP64 passes apply it: the circuit's operations
+    planned into passes (consecutive maps on one axis of a pass composed into one), and per planned
+    operation 2 * its matrix's nonzeros / its dimension per coefficient (a dense 4x4 map: 8; an ideal
+    CX: 0, a signed permutation), times 4**n."""
+    from qiskit_aakash_gb300 import batch as B
+    from qiskit_aakash_gb300 import program as P
+    rec = B.compile_experiment(qc.to_experiment(), opts)
+    per = 0.0
+    for op in (o for p in P.plan_passes(rec.ops, rec.n, tile_axes, low) for o in p.ops):
+        if op.kind == 'map1':
+            per += 2.0 * np.count_nonzero(np.asarray(op.data)) / 4
+        elif op.kind == 'cx':
+            per += 0.0 if op.ideal else 2.0 * np.count_nonzero(P.cx_matrix16(op.data, op.ideal)) / 16
+        elif op.kind == 'diag2':
+            per += np.count_nonzero(np.asarray(op.data) != 1.0) / 16
+        else:
+            per += 2.0 * np.count_nonzero(np.asarray(op.data)) / 16
+    return per * 4.0 ** rec.n
 
 
 def per_gate_kind(torch, N, n=14, reps=3, dtype=None):
@@ -615,7 +666,9 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
     ms64 = time_replays(torch, st64, args.fp64_steps)
     durs64 = all_durations(pass_kernel_profile(torch, st64))
     prob64 = np.array(list(r64['data']['ensemble_probability'].values()))
-    max_abs = device_max_abs_diff(torch, st32.state, st64.state) * 2.0 ** n
+    max_abs = st32.max_abs_diff(st64) * 2.0 ** n
+    peak64 = fp64_peak(torch, N)
+    flops64 = fp64_flops(pkg, qc, opts)
     prob_l1 = float(np.abs(prob32 - prob64).sum())
     del st64, b64, r64, st32, b32, r32
     torch.cuda.empty_cache()
@@ -683,7 +736,11 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
                    'parallelism': 'replicas' if world > 1 else 'single GPU'},
         'plain_fp64': {'value': world * layers / (ms64 / 1e3), 'unit': 'gate-layers/s', 'ms_per_step': ms64,
                        'fused_passes': stats64['passes'], 'mean_pass_ms': mean_pass64,
-                       'pass_achieved_gbs': achieved64, 'pass_frac_of_hbm': achieved64 / hbm},
+                       'pass_achieved_gbs': achieved64, 'pass_frac_of_hbm': achieved64 / hbm,
+                       'fp64_flops_per_step': flops64,
+                       'achieved_fp64_tflops': flops64 / (ms64 / 1e3) / 1e12,
+                       'frac_of_fp64_peak': flops64 / (ms64 / 1e3) / 1e12 / peak64['tflops'],
+                       'fp64_peak': peak64},
         'fp32_over_fp64': ms64 / ms32,
         'fp32_cuda_cores': {'value': world * layers / (ms_cc / 1e3), 'unit': 'gate-layers/s', 'ms_per_step': ms_cc,
                             'kernel': 'pass_pipe_kernel<float,3>',

@@ -192,6 +192,40 @@ int dm_apply_pass_tma(void *state_dev, int n, const dm_tc_pass *pass, const uint
 int dm_max_abs_diff(const void *a_dev, int dtype_a, const void *b_dev, int dtype_b, int n, double *out_dev,
                     void *stream);
 
+/* FP64 FMA throughput probe (measurement only, no reference counterpart):
+ * dm_fp64_fma_probe_threads() threads each run 8 independent chains of
+ * `iters` FMAs and write one double each into out_dev (that many doubles).
+ * FP64 FLOPs of one launch: 2 * 8 * iters * threads.  bench.py times it to
+ * state the FP64 pipe's measured peak beside the FP64 pass's throughput. */
+int dm_fp64_fma_probe_threads(void);
+int dm_fp64_fma_probe(double *out_dev, int64_t iters, void *stream);
+
+/* ------------------------------------------------------------------ levelling */
+
+/* Instruction kinds for dm_levelize. */
+#define DM_SCHED_GATE1 1      /* u1 / u3 on one qubit (after the single-gate merge) */
+#define DM_SCHED_CX 2
+#define DM_SCHED_MEASURE 3
+#define DM_SCHED_RESET 4
+#define DM_SCHED_BARRIER 5
+#define DM_SCHED_OTHER 6      /* anything else: cannot be placed (DM_ERR_PROGRAM) */
+
+/* Levels (clock cycles) of a merged instruction list, host code: replaces
+ * partition / partition_helper / qubit_stack, basicaertools.py:536-749.
+ * Instruction i has kind[i] and qubits qubits[qoff[i] .. qoff[i+1]-1]
+ * (qoff has count + 1 entries, qoff[0] = 0).  Every instruction other than
+ * a barrier is placed once: placed_inst[k] (instruction index) goes to entry
+ * placed_pos[k] of the level table, in placement order (the order the
+ * reference appends them); *placed_count placements.  *table_len is the
+ * length of the concatenated per-piece tables (unused trailing entries
+ * included) and *levels the number of executed levels (the reference's
+ * number_of_clock_cycles): the first *levels entries run.  placed_inst and
+ * placed_pos hold count entries each.  DM_ERR_PROGRAM when an instruction can
+ * never be placed. */
+int dm_levelize(int n, int count, const int32_t *kind, const int32_t *qoff, const int32_t *qubits,
+                int32_t *placed_inst, int32_t *placed_pos, int32_t *placed_count, int32_t *table_len,
+                int32_t *levels);
+
 /* ------------------------------------------------------------- batched sweeps */
 
 /* One pass of a batched program (the n-independent part of dm_pass). */

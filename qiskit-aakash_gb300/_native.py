@@ -19,7 +19,7 @@ INCLUDE = os.path.join(REPO_DIR, 'include')
 BUILD_DIR = os.path.join(PKG_DIR, '_build')
 LIB_PATH = os.path.join(PKG_DIR, 'libdmgb300.so')
 SOURCES = ['dm_misc.cu', 'dm_pass.cu', 'dm_state.cu', 'dm_measure.cu', 'dm_tc.cu', 'dm_tma.cu', 'dm_mlp.cu',
-           'dm_sample.cu']
+           'dm_sample.cu', 'dm_sched.cpp']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '-Xptxas', '-warn-spills',
               '--expt-relaxed-constexpr']
@@ -35,6 +35,7 @@ DM_OP_MAP1, DM_OP_MAP2, DM_OP_DIAG2, DM_OP_CX = 1, 2, 3, 4
 DM_MAP1_ROW0_IDENTITY = 1
 DM_MAP1_XY_UNITAL = 2
 DM_CX_IDEAL = 1
+DM_SCHED_GATE1, DM_SCHED_CX, DM_SCHED_MEASURE, DM_SCHED_RESET, DM_SCHED_BARRIER, DM_SCHED_OTHER = 1, 2, 3, 4, 5, 6
 
 
 class NativeError(RuntimeError):
@@ -179,6 +180,9 @@ SIGNATURES = {
     'dm_apply_pass_tc': (_i, [_vp, _i, ctypes.POINTER(DmTcPass), _vp, _sz, _vp, _vp]),
     'dm_apply_pass_tma': (_i, [_vp, _i, ctypes.POINTER(DmTcPass), _vp, _sz, _vp, _vp]),
     'dm_max_abs_diff': (_i, [_vp, _i, _vp, _i, _i, _vp, _vp]),
+    'dm_fp64_fma_probe_threads': (_i, []),
+    'dm_fp64_fma_probe': (_i, [_vp, ctypes.c_int64, _vp]),
+    'dm_levelize': (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     'dm_batch_run': (_i, [_i, _vp, _sz, _vp, _sz, _vp, _sz, ctypes.POINTER(DmBatchInstance), _vp, _i,
                           ctypes.POINTER(DmBatchPass), _vp, _i, _vp, _vp, _vp]),
     'dm_batch_tc_scratch_bytes': (_sz, []),

@@ -50,7 +50,36 @@ cudaError_t ensure_max_dynamic_smem(const void *func, int bytes) {
     return cudaSuccess;
 }
 
+// FP64 FMA throughput probe: every thread runs kChains independent FMA chains
+// of `iters` steps (x = x * a + b, a slightly below 1 so nothing overflows)
+// and writes their sum, so no FMA can be dropped.
+constexpr int kFmaChains = 8;
+
+__global__ void __launch_bounds__(256) fp64_fma_probe(double *out, int64_t iters, double a, double b) {
+    double x[kFmaChains];
+#pragma unroll
+    for (int c = 0; c < kFmaChains; ++c) x[c] = double(threadIdx.x + c);
+    for (int64_t i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < kFmaChains; ++c) x[c] = fma(x[c], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < kFmaChains; ++c) s += x[c];
+    out[blockIdx.x * int64_t(blockDim.x) + threadIdx.x] = s;
+}
+
 }  // namespace dmg
+
+extern "C" int dm_fp64_fma_probe_threads(void) { return dmg::sm_count() * 8 * 256; }
+
+extern "C" int dm_fp64_fma_probe(double *out_dev, int64_t iters, void *stream) {
+    if (!out_dev || iters < 1) return DM_ERR_ARG;
+    const int blocks = dmg::sm_count() * 8;
+    dmg::fp64_fma_probe<<<blocks, 256, 0, dmg::as_stream(stream)>>>(out_dev, iters, 0.999999, 1e-7);
+    dmg::count_launch();
+    return dmg::launch_status();
+}
 
 extern "C" const char *dm_error_string(int code) {
     switch (code) {

@@ -10,7 +10,8 @@ reference's levels exactly.
   with the pair merge of :181-228 (mergeU) and the Euler-angle conversion
   of :129-178 (U3_merge).
 * ``levelize``            -- basicaertools.py:714-749 (partition), built on
-  :536-591 (qubit_stack) and :594-712 (partition_helper).
+  :536-591 (qubit_stack) and :594-712 (partition_helper); the levelling itself
+  runs in the library (dm_levelize, csrc/dm_sched.cpp).
 
 Both keep the reference's observable behaviour: merged instructions are
 emitted at each separator in qubit order, a merged run keeps the position
@@ -124,130 +125,46 @@ def merge_single_gates(insts, n, merge=True):
 
 
 # ---------------------------------------------------------------------------
-# levelling
+# levelling (compiled: dm_levelize in csrc/dm_sched.cpp)
 # ---------------------------------------------------------------------------
 
-class _Placeholder:
-    """Stands on a qubit's stack for a measurement / reset on another qubit."""
-    __slots__ = ('kind',)
-
-    def __init__(self, kind):
-        self.kind = kind
-
-
-def _stacks(piece, n):
-    stacks = [[] for _ in range(n)]
-    for op in piece:
-        kind = op.name
-        if kind not in ('measure', 'reset'):
-            for q in op.qubits:
-                stacks[q].append(op)
-            continue
-        q0 = op.qubits[0]
-        top = stacks[q0][-1] if stacks[q0] else None
-        if isinstance(top, _Placeholder) and top.kind == kind:
-            stacks[q0][-1] = op           # joins the pending simultaneous group
-            continue
-        stacks[q0].append(op)
-        ph = _Placeholder(kind)
-        for q in range(n):
-            if q not in op.qubits:
-                stacks[q].append(ph)
-    return stacks
-
-
-def _level_piece(piece, n):
-    stacks = _stacks(piece, n)
-    heads = [0] * n
-    table = [[] for _ in range(max(len(s) for s in stacks))]
-    remaining = len(piece)
-    level = 0
-
-    def top(q):
-        return stacks[q][heads[q]] if heads[q] < len(stacks[q]) else None
-
-    while remaining:
-        busy = set()
-        placed_before = remaining
-        if level == len(table):
-            table.append([])
-        for q in range(n):
-            g = top(q)
-            if g is None or isinstance(g, _Placeholder):
-                continue
-            name = g.name
-            if name in ('u3', 'u1'):
-                if q in busy:
-                    continue
-                table[level].append(g)
-                busy.add(q)
-                heads[q] += 1
-                remaining -= 1
-            elif name in ('cx', 'CX'):
-                other = [x for x in g.qubits if x != q][0]
-                partner = top(other)
-                if q in busy or other in busy or partner is not g:
-                    continue
-                busy.update((q, other))
-                table[level].append(g)
-                heads[q] += 1
-                heads[other] += 1
-                remaining -= 1
-            elif name in ('measure', 'reset'):
-                ready = all(t is None or (isinstance(t, _Placeholder) and t.kind == name)
-                            or (not isinstance(t, _Placeholder) and t.name == name)
-                            for t in (top(x) for x in range(n)))
-                if not ready:
-                    if not remaining:
-                        break
-                    continue
-                if table[level]:
-                    busy = set()
-                    level += 1
-                    if level == len(table):
-                        table.append([])
-                for x in range(n):
-                    t = top(x)
-                    if t is None:
-                        continue
-                    if not isinstance(t, _Placeholder):
-                        busy.add(x)
-                        table[level].append(t)
-                        remaining -= 1
-                    heads[x] += 1
-                break
-            if not remaining:
-                break
-        if remaining == placed_before:
-            raise QiskitError('levelling cannot place the remaining instructions')
-        level += 1
-    return table, level
+_KINDS = {'u1': 1, 'u3': 1, 'cx': 2, 'CX': 2, 'measure': 3, 'reset': 4, 'barrier': 5}
 
 
 def levelize(insts, n):
-    """Split on barriers and level each piece; returns (level table, number of levels)."""
-    pieces, cur = [], []
-    for op in insts:
-        if op.name == 'barrier':
-            pieces.append(cur)
-            cur = []
-        else:
-            cur.append(op)
-    if cur:
-        pieces.append(cur)
-    table, levels = [], 0
-    for piece in pieces:
-        if not piece:
-            continue
-        head = piece[0]
-        prm = getattr(head, 'params', None)
-        if head.name == 'measure' and prm and isinstance(prm[0], str) \
-                and prm[0] in ('Bell', 'Expect', 'Ensemble'):
-            # Plain-string parameters (never produced by qiskit's assembler,
-            # which makes them sympy Symbols) send the reference down a path
-            # that fails (basicaertools.py:740-747); level them like Symbols.
-            pass
-        t, lv = _level_piece(piece, n)
-        table.extend(t)
-        levels += lv
+    """Split on barriers and level each piece; returns (level table, number of levels).
+
+    The levels are computed by the library's dm_levelize (the reference's
+    partition, basicaertools.py:536-749, in C++); the table lists the
+    instruction objects of each level in the order the reference appends them.
+    """
+    import ctypes
+    from . import _native as N
+    count = len(insts)
+    kind = np.empty(count, dtype=np.int32)
+    qoff = np.zeros(count + 1, dtype=np.int32)
+    qubits = []
+    for i, op in enumerate(insts):
+        kind[i] = _KINDS.get(op.name, N.DM_SCHED_OTHER)
+        qs = [] if op.name == 'barrier' else [int(q) for q in op.qubits]
+        qubits.extend(qs)
+        qoff[i + 1] = qoff[i] + len(qs)
+    qarr = np.asarray(qubits if qubits else [0], dtype=np.int32)
+    placed_inst = np.empty(max(count, 1), dtype=np.int32)
+    placed_pos = np.empty(max(count, 1), dtype=np.int32)
+    out = np.zeros(3, dtype=np.int32)
+
+    def ptr(a, k=0):
+        return ctypes.c_void_p(a.ctypes.data + 4 * k)
+
+    rc = N.lib().dm_levelize(n, count, ptr(kind), ptr(qoff), ptr(qarr), ptr(placed_inst), ptr(placed_pos),
+                             ptr(out, 0), ptr(out, 1), ptr(out, 2))
+    if rc == N.DM_ERR_PROGRAM:
+        raise QiskitError('levelling cannot place the remaining instructions')
+    if rc != N.DM_OK:
+        raise QiskitError('levelling failed: %s' % N.lib().dm_error_string(rc).decode())
+    placed, table_len, levels = (int(x) for x in out)
+    table = [[] for _ in range(table_len)]
+    for k in range(placed):
+        table[placed_pos[k]].append(insts[placed_inst[k]])
     return table, levels

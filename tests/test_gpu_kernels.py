@@ -254,7 +254,7 @@ def test_tma_pass_equals_program_order(torch, n):
     and against dm_apply_pass_tc on the same passes (same split arithmetic)."""
     from test_planner import apply_op
     rng = np.random.default_rng(4000 + n)
-    ops = _physical_ops(rng, n, 80)
+    ops = _physical_ops(rng, n, 20 if n == 7 else 80)     # 80 ops on 7 qubits need more than 6 rounds
     st = rng.uniform(-1, 1, size=4 ** n) * 2.0 ** -n
     st[0] = 2.0 ** -n
     ref = st.copy()

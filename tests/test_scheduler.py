@@ -38,3 +38,24 @@ def test_euler_conversion_is_a_rotation_identity():
         rhs = rz(alpha) @ ry(beta) @ rz(gamma)
         # equal up to a global sign
         assert min(np.abs(lhs - rhs).max(), np.abs(lhs + rhs).max()) < 1e-9
+
+
+def test_compiled_levelling_rejects_what_the_reference_cannot_level():
+    """dm_levelize: an instruction that can never be placed, and malformed arrays."""
+    import ctypes
+    from qiskit_aakash_gb300 import _native as N
+    from qiskit_aakash_gb300.circuit import QobjInstruction
+    from qiskit_aakash_gb300.exceptions import QiskitError
+    with pytest.raises(QiskitError, match='cannot place'):
+        S.levelize([QobjInstruction('u3', [0], [0.1, 0.2, 0.3]), QobjInstruction('unitary', [1], [])], 2)
+    kind = np.array([N.DM_SCHED_GATE1], dtype=np.int32)
+    qoff = np.array([0, 1], dtype=np.int32)
+    bad_q = np.array([5], dtype=np.int32)                 # qubit beyond n
+    out = np.zeros(8, dtype=np.int32)
+
+    def p(a):
+        return ctypes.c_void_p(a.ctypes.data)
+
+    rc = N.lib().dm_levelize(2, 1, p(kind), p(qoff), p(bad_q), p(out), p(out), p(out), p(out), p(out))
+    assert rc == N.DM_ERR_ARG
+    assert S.levelize([], 3) == ([], 0)
