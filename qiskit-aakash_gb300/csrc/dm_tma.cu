@@ -70,14 +70,16 @@ constexpr uint32_t kSmemBytes = kTeams * kSlotBytes + kMaxRounds * kUBytes + 102
 constexpr uint32_t kTmemCols = 512;                          // per team: two M = 128 blocks x (D1 | D2)
 
 struct TmaPass {
-    int nrounds, vec0, ndims;
+    int nrounds, ndims;
     float up, down;                  // 2**n, 2**-n
     int64_t ntiles;
     int8_t gap_first[kMaxDims];      // tile-index digit of the first non-resident digit above dimension i
     int8_t gap_len[kMaxDims];        // non-resident digits above dimension i
     int8_t box_log4[kMaxDims];       // resident digits of dimension i
+    int8_t start[kMaxDims];          // digit position of dimension i (its stride is 4**start elements)
     int32_t uoff[kMaxRounds];        // FP16-value offset of round r's images
-    uint32_t natrow[8], natk[6];
+    uint32_t natrow[8], natk[6];     // round 0: natural-tile element offsets of its row and K bits
+    int64_t lastg[14];               // last round: global element offsets of its row bits 0-7 and K bits 0-5
     Round rounds[kMaxRounds];
 };
 
@@ -86,6 +88,40 @@ __device__ __forceinline__ void tile_coords(const TmaPass &p, int64_t t, int (&c
     for (int i = 0; i < kMaxDims; ++i) {
         const int64_t g = (t >> (2 * p.gap_first[i])) & ((int64_t(1) << (2 * p.gap_len[i])) - 1);
         c[i] = int(g << (2 * p.box_log4[i]));
+    }
+}
+
+// Global element offset of tile t's first coefficient (its non-resident digits).
+__device__ __forceinline__ int64_t tile_base(const TmaPass &p, const int (&c)[kMaxDims]) {
+    int64_t b = 0;
+#pragma unroll
+    for (int i = 0; i < kMaxDims; ++i) b += int64_t(c[i]) << (2 * p.start[i]);
+    return b;
+}
+
+// TMA prefetch of tile coordinates c into L2 (no shared memory, no completion).
+__device__ __forceinline__ void tma_prefetch_l2(const CUtensorMap *map, int nd, const int (&c)[kMaxDims]) {
+    const uint64_t m = reinterpret_cast<uint64_t>(map);
+    switch (nd) {
+    case 1:
+        asm volatile("cp.async.bulk.prefetch.tensor.1d.L2.global [%0, {%1}];" ::"l"(m), "r"(c[0]) : "memory");
+        break;
+    case 2:
+        asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global [%0, {%1, %2}];" ::"l"(m), "r"(c[0]), "r"(c[1])
+                     : "memory");
+        break;
+    case 3:
+        asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global [%0, {%1, %2, %3}];" ::"l"(m), "r"(c[0]),
+                     "r"(c[1]), "r"(c[2]) : "memory");
+        break;
+    case 4:
+        asm volatile("cp.async.bulk.prefetch.tensor.4d.L2.global [%0, {%1, %2, %3, %4}];" ::"l"(m), "r"(c[0]),
+                     "r"(c[1]), "r"(c[2]), "r"(c[3]) : "memory");
+        break;
+    default:
+        asm volatile("cp.async.bulk.prefetch.tensor.5d.L2.global [%0, {%1, %2, %3, %4, %5}];" ::"l"(m), "r"(c[0]),
+                     "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]) : "memory");
+        break;
     }
 }
 
@@ -119,34 +155,6 @@ __device__ __forceinline__ void tma_load(const CUtensorMap *map, int nd, const i
     }
 }
 
-// TMA tile store of the shared-memory box at src to tile coordinates c (bulk group of this thread).
-__device__ __forceinline__ void tma_store(const CUtensorMap *map, int nd, const int (&c)[kMaxDims], uint32_t src) {
-    const uint64_t m = reinterpret_cast<uint64_t>(map);
-    switch (nd) {
-    case 1:
-        asm volatile("cp.async.bulk.tensor.1d.global.shared::cta.bulk_group [%0, {%2}], [%1];" ::"l"(m), "r"(src),
-                     "r"(c[0]) : "memory");
-        break;
-    case 2:
-        asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(m), "r"(src),
-                     "r"(c[0]), "r"(c[1]) : "memory");
-        break;
-    case 3:
-        asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(m),
-                     "r"(src), "r"(c[0]), "r"(c[1]), "r"(c[2]) : "memory");
-        break;
-    case 4:
-        asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%2, %3, %4, %5}], [%1];" ::"l"(m),
-                     "r"(src), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]) : "memory");
-        break;
-    default:
-        asm volatile("cp.async.bulk.tensor.5d.global.shared::cta.bulk_group [%0, {%2, %3, %4, %5, %6}], [%1];" ::"l"(m),
-                     "r"(src), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]) : "memory");
-        break;
-    }
-    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-}
-
 __device__ __forceinline__ void team_sync(int team) {
     asm volatile("bar.sync %0, %1;" ::"r"(1 + team), "n"(kTeamThreads) : "memory");
 }
@@ -166,7 +174,7 @@ __device__ __forceinline__ bool team_and(bool ok, int team) {
 
 __global__ void __launch_bounds__(kThreads, 1)
     pass_tma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ TmaPass p,
-                    const uint16_t *__restrict__ umats, int *status) {
+                    float *__restrict__ st, const uint16_t *__restrict__ umats, int *status) {
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t load_bar[kTeams];
     __shared__ __align__(8) uint64_t mma_bar[kTeams];
@@ -230,41 +238,34 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         lphase ^= 1;
         load_pending = false;
-        // ---- natural tile -> round 0's operand (h / l), in place ----
+        const int64_t tn = t + stride;
+        if (leader && tn < p.ntiles) {   // the team's next tile heads for L2 while this one runs
+            int c[kMaxDims];
+            tile_coords(p, tn, c);
+            tma_prefetch_l2(&tmap, p.ndims, c);
+        }
+        // ---- natural tile -> round 0's operand (h / l), in place: one operand row per thread ----
+        // lanes hold rows 0-4, whose tile bits 0-3 are the 16 contiguous coefficients of the tile:
+        // the word loads of a warp hit distinct banks, the 16-byte chunk stores whole core matrices
         {
-            constexpr int kItems = kGroups * 8 / kTeamThreads;   // 8
             const float *nat = reinterpret_cast<const float *>(AH);
             const float up = p.up;
-            float x[kItems][8];
+            uint32_t tn0[3][4];
+            digit_tables(p.natk, tn0);
+            const uint32_t nb = xor_bits<8>(uint32_t(ttid), p.natrow);
+            float x[64];
 #pragma unroll
-            for (int q = 0; q < kItems; ++q) {
-                const int i = ttid + kTeamThreads * q;
-                const int crow = ((i >> 6) << 3) | (i & 7), c = (i >> 3) & 7;
-                const uint32_t nb = xor_bits<8>(uint32_t(crow), p.natrow) ^ ((c & 1) ? p.natk[3] : 0u) ^
-                                    ((c & 2) ? p.natk[4] : 0u) ^ ((c & 4) ? p.natk[5] : 0u);
-                if (p.vec0 == 0) {
-                    const float4 a4 = *reinterpret_cast<const float4 *>(nat + nb);
-                    const float4 b4 = *reinterpret_cast<const float4 *>(nat + (nb ^ p.natk[2]));
-                    x[q][0] = a4.x; x[q][1] = a4.y; x[q][2] = a4.z; x[q][3] = a4.w;
-                    x[q][4] = b4.x; x[q][5] = b4.y; x[q][6] = b4.z; x[q][7] = b4.w;
-                } else {
-#pragma unroll
-                    for (int e = 0; e < 8; ++e)
-                        x[q][e] = nat[nb ^ ((e & 1) ? p.natk[0] : 0u) ^ ((e & 2) ? p.natk[1] : 0u) ^
-                                      ((e & 4) ? p.natk[2] : 0u)];
-                }
-            }
+            for (int j = 0; j < 64; ++j) x[j] = nat[nb ^ tn0[0][j & 3] ^ tn0[1][(j >> 2) & 3] ^ tn0[2][j >> 4]];
             team_sync(team);
+            const uint32_t o = row_off(ttid);
 #pragma unroll
-            for (int q = 0; q < kItems; ++q) {
-                const int i = ttid + kTeamThreads * q;
-                const int crow = ((i >> 6) << 3) | (i & 7), c = (i >> 3) & 7;
+            for (int c = 0; c < 8; ++c) {
                 uint32_t hw[4], lw[4];
 #pragma unroll
-                for (int e = 0; e < 8; e += 2) split2(x[q][e] * up, x[q][e + 1] * up, hw[e >> 1], lw[e >> 1]);
-                const uint32_t o = row_off(crow) + uint32_t(c) * kLBO;
-                *reinterpret_cast<uint4 *>(AH + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-                *reinterpret_cast<uint4 *>(AL + o) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+                for (int e = 0; e < 8; e += 2)
+                    split2(x[8 * c + e] * up, x[8 * c + e + 1] * up, hw[e >> 1], lw[e >> 1]);
+                *reinterpret_cast<uint4 *>(AH + o + uint32_t(c) * kLBO) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4 *>(AL + o + uint32_t(c) * kLBO) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
             }
         }
         bool alive = true;
@@ -308,47 +309,57 @@ __global__ void __launch_bounds__(kThreads, 1)
             mphase ^= 1;
             mma_pending = false;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            // ---- epilogue: D -> next operand (h / l), or the natural FP32 tile after the last round ----
-            const Round &R = p.rounds[r];
-            uint32_t tk[3][4];
-            digit_tables(R.kc, tk);
-            float v[64];
-            tcg::tmem_ld32_pair_fma(taddr, taddr + 64, kLoScale, v);        // 2**11 x = 2**11 D1 + D2
-            tcg::tmem_ld32_pair_fma(taddr + 32, taddr + 96, kLoScale, v + 32);
-            const uint32_t base = xor_bits<8>(uint32_t(ttid), R.rowc);
-            if (r + 1 < p.nrounds) {
-                store_all<true>(v, R.vec, base, tk, AH, AL);
-            } else {
-                const float down = p.down * kLoUnscale;
-#pragma unroll
-                for (int j = 0; j < 64; ++j) v[j] *= down;
-                store_all<false>(v, R.vec, base, tk, AH, AL);
-            }
-            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        }
-        if (!alive) break;
-        // ---- store the tile (TMA), then load the team's next tile into the slot ----
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        team_sync(team);
-        const int64_t tn = t + stride;
-        if (leader) {
-            int c[kMaxDims];
-            tile_coords(p, t, c);
-            tma_store(&tmap, p.ndims, c, smem_u32(AH));
-            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");   // the slot has been read
-            if (tn < p.ntiles) {
+            const bool last = r + 1 == p.nrounds;
+            if (last && leader && tn < p.ntiles) {
+                // the slot's operands are consumed: the next tile's load (from L2) overlaps this epilogue
+                int c[kMaxDims];
                 tile_coords(p, tn, c);
                 tcg::mbar_expect_tx(lbar, kSlotBytes);
                 tma_load(&tmap, p.ndims, c, smem_u32(AH), lbar);
             }
+            float v[64];
+            tcg::tmem_ld32_pair_fma(taddr, taddr + 64, kLoScale, v);        // 2**11 x = 2**11 D1 + D2
+            tcg::tmem_ld32_pair_fma(taddr + 32, taddr + 96, kLoScale, v + 32);
+            if (!last) {
+                // ---- epilogue: D -> the next round's operand (h / l) ----
+                const Round &R = p.rounds[r];
+                uint32_t tk[3][4];
+                digit_tables(R.kc, tk);
+                const uint32_t base = xor_bits<8>(uint32_t(ttid), R.rowc);
+                store_all<true>(v, R.vec, base, tk, AH, AL);
+            } else {
+                // ---- last round: the row straight to global memory; lanes 0-15 cover 64 contiguous bytes ----
+                int c[kMaxDims];
+                tile_coords(p, t, c);
+                int64_t rowg = tile_base(p, c);
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if ((ttid >> i) & 1) rowg += p.lastg[i];
+                float *row = st + rowg;
+                const float down = p.down * kLoUnscale;
+#pragma unroll
+                for (int d2 = 0; d2 < 4; ++d2) {
+                    const int64_t o2 = (d2 & 1 ? p.lastg[12] : 0) + (d2 & 2 ? p.lastg[13] : 0);
+#pragma unroll
+                    for (int d1 = 0; d1 < 4; ++d1) {
+                        float *q = row + o2 + (d1 & 1 ? p.lastg[10] : 0) + (d1 & 2 ? p.lastg[11] : 0);
+                        const int j = 4 * d1 + 16 * d2;
+                        q[0] = v[j] * down;
+                        q[p.lastg[8]] = v[j + 1] * down;
+                        q[p.lastg[9]] = v[j + 2] * down;
+                        q[p.lastg[8] + p.lastg[9]] = v[j + 3] * down;
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         }
+        if (!alive) break;
         load_pending = tn < p.ntiles;
     }
-    // ---- drain: the team's MMA, tile load and tile stores in flight ----
+    // ---- drain: the team's MMA and tile load in flight ----
     if (mma_pending) mbar_wait(mbar, mphase);
     if (load_pending) mbar_wait(lbar, lphase);
     if (!u_ok) mbar_wait(ubar, 0);
-    if (leader) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
@@ -406,6 +417,7 @@ static bool tma_dims(int n, const int32_t *axes, tma::TmaPass &p, cuuint64_t *gd
         p.box_log4[nd] = int8_t(len);
         p.gap_len[nd] = int8_t(gap);
         p.gap_first[nd] = int8_t(gap_first);
+        p.start[nd] = int8_t(pos);
         gdim[nd] = cuuint64_t(1) << (2 * (len + gap));
         box[nd] = cuuint32_t(1) << (2 * len);
         if (nd > 0) gstride_bytes[nd - 1] = (cuuint64_t(1) << (2 * pos)) * sizeof(float);
@@ -413,7 +425,7 @@ static bool tma_dims(int n, const int32_t *axes, tma::TmaPass &p, cuuint64_t *gd
         pos += len + gap;
         ++nd;
     }
-    for (int i = nd; i < tma::kMaxDims; ++i) p.box_log4[i] = p.gap_len[i] = p.gap_first[i] = 0;
+    for (int i = nd; i < tma::kMaxDims; ++i) p.box_log4[i] = p.gap_len[i] = p.gap_first[i] = p.start[i] = 0;
     p.ndims = nd;
     return gap_first == n - tc::kAxes;
 }
@@ -469,11 +481,9 @@ extern "C" int dm_apply_pass_tma(void *state_dev, int n, const dm_tc_pass *pass,
     cuuint32_t box[tma::kMaxDims], estride[tma::kMaxDims];
     if (!tma_dims(n, pass->axes, p, gdim, gstride, box)) return DM_ERR_PROGRAM;
     p.nrounds = nr;
-    p.vec0 = pass->vec0 == 0 ? 0 : -1;
     p.up = float(ldexp(1.0, n));
     p.down = float(ldexp(1.0, -n));
     p.ntiles = int64_t(1) << (2 * (n - tc::kAxes));
-    if (p.vec0 == 0 && (pass->natk[0] != 1 || pass->natk[1] != 2)) return DM_ERR_PROGRAM;
     if (!linear_tables(pass->natrow, pass->natk, -1)) return DM_ERR_PROGRAM;
     for (int i = 0; i < 8; ++i) p.natrow[i] = pass->natrow[i];
     for (int i = 0; i < 6; ++i) p.natk[i] = pass->natk[i];
@@ -485,8 +495,18 @@ extern "C" int dm_apply_pass_tma(void *state_dev, int n, const dm_tc_pass *pass,
             o.digits[i] = in.digits[i];
         }
         o.vec = in.vec;
-        const bool ok = r + 1 == nr ? linear_tables(in.rowc, in.kc, in.vec) : operand_tables(in.rowc, in.kc, in.vec);
+        const bool ok = r + 1 == nr ? linear_tables(in.rowc, in.kc, -1) : operand_tables(in.rowc, in.kc, in.vec);
         if (!ok) return DM_ERR_PROGRAM;
+        if (r + 1 == nr) {
+            // the last round stores to global memory: tile bit b = bit b % 2 of local axis b / 2's digit
+            for (int i = 0; i < 14; ++i) {
+                const uint32_t c = i < 8 ? in.rowc[i] : in.kc[i - 8];
+                int b = 0;
+                while ((1u << b) != c) ++b;
+                const int pos = n - 1 - pass->axes[b >> 1];
+                p.lastg[i] = (int64_t(1) << (b & 1)) << (2 * pos);
+            }
+        }
         for (int i = 0; i < 8; ++i) o.rowc[i] = in.rowc[i];
         for (int i = 0; i < 6; ++i) o.kc[i] = in.kc[i];
         if (in.umoff < 0 || (in.umoff & 7) || size_t(in.umoff) + tma::kUHalves > umats_count) return DM_ERR_PROGRAM;
@@ -507,8 +527,8 @@ extern "C" int dm_apply_pass_tma(void *state_dev, int n, const dm_tc_pass *pass,
     int64_t grid = sm_count();
     const int64_t want = (p.ntiles + tma::kTeams - 1) / tma::kTeams;
     if (grid > want) grid = want;
-    tma::pass_tma_kernel<<<int(grid), tma::kThreads, tma::kSmemBytes, as_stream(stream)>>>(map, p, umats_dev,
-                                                                                           status_dev);
+    tma::pass_tma_kernel<<<int(grid), tma::kThreads, tma::kSmemBytes, as_stream(stream)>>>(
+        map, p, static_cast<float *>(state_dev), umats_dev, status_dev);
     count_launch();
     return launch_status();
 }

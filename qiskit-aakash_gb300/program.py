@@ -651,6 +651,72 @@ def _choose_layouts_cached(rounds_axes, nat='xor'):
     return tuple(layouts)
 
 
+# Layouts of the TMA-fed pass (dm_apply_pass_tma).  Its first round converts
+# the natural tile with one thread per operand row and its last round stores
+# one row per thread straight to global memory; both keep tile bits 0-3
+# (local axes 0 and 1, the 16 contiguous coefficients of a tile) as row bits
+# 0-3, so the 32 lanes of a warp read and write runs of 16 consecutive
+# coefficients.
+TMA_FIXED_ROWS = [0, 1, 2, 3]
+
+
+def _tma_conversion_cost(layout):
+    """Shared-memory load wavefronts of one warp converting the natural tile: 64 word loads, lanes = rows 0-4."""
+    return 64 * _store_wavefronts(tuple(4 * (1 << tb) for tb in layout.rowbits[:5]), 4)
+
+
+@functools.lru_cache(maxsize=4096)
+def _choose_layouts_tma_cached(rounds_axes):
+    import itertools
+    nlast = len(rounds_axes) - 1
+    if any(a in rounds_axes[0] or a in rounds_axes[nlast] for a in (0, 1)):
+        return None
+    layouts = []
+    prev = None
+    for ri, axes in enumerate(rounds_axes):
+        axes = sorted(axes)
+        nonround = [tb for tb in range(2 * TC_AXES) if tb // 2 not in axes]
+        nxt_axes = set(rounds_axes[ri + 1]) if ri < nlast else None
+        cands = []
+        if ri == 0 or ri == nlast:
+            rest = [tb for tb in nonround if tb not in TMA_FIXED_ROWS]
+            fifth = ([4] if 4 in rest else []) + [tb for tb in rest if tb != 4][:2]
+            for digits in itertools.permutations(axes):
+                for f in fifth:
+                    cands.append(TcLayout(list(digits), TMA_FIXED_ROWS + [f] + [tb for tb in rest if tb != f]))
+        else:
+            lanes = [tb for tb in prev.rowbits[:5] if tb in nonround]
+            keep = [tb for tb in prev.rowbits if tb in nonround]
+            triples = list(itertools.combinations(lanes, 3)) if len(lanes) >= 3 else [tuple(lanes)]
+            fourth = [None] + ([tb for tb in nonround if tb % 2 == 0 and tb // 2 in nxt_axes] if nxt_axes else [])
+            for digits in itertools.permutations(axes):
+                for tri in triples:
+                    for f in fourth:
+                        if f in tri:
+                            continue
+                        cands.append(TcLayout(list(digits), _fill_rows(list(tri) + ([f] if f is not None else []),
+                                                                       lanes, keep, nonround)))
+        best = None
+        for cand in cands:
+            cost = _tma_conversion_cost(cand) if ri == 0 else 0
+            if prev is not None:
+                vec = 8 if _vec_digit(prev, cand.digits[0]) >= 0 else None
+                cost += _transition_cost(prev, cand.byte_of_bit, vec)
+            if ri < nlast:
+                if ri + 1 == nlast:      # the next round's rows are fixed: its exact incoming cost
+                    cost += min(_transition_cost(cand, TcLayout(list(d), TMA_FIXED_ROWS + [
+                        tb for tb in range(2 * TC_AXES) if tb // 2 not in nxt_axes and tb not in TMA_FIXED_ROWS
+                    ]).byte_of_bit, 8 if _vec_digit(cand, d[0]) >= 0 else None)
+                        for d in itertools.permutations(sorted(nxt_axes)))
+                else:
+                    cost += _best_next_cost(cand, nxt_axes)
+            if best is None or cost < best[0]:
+                best = (cost, cand)
+        layouts.append(best[1])
+        prev = best[1]
+    return tuple(layouts)
+
+
 def _choose_layouts(rounds_axes, nat='xor'):
     """Pick each round's digit order and row-bit order (greedy along the rounds, one round of lookahead).
 
@@ -714,10 +780,20 @@ def epilogue_wavefronts(src, dst, natural=False):
 
 
 def plan_tc_pass(p, n, nat='xor'):
-    """Pad a pass to 7 axes, plan its rounds and their layouts, compose each round's U (FP64)."""
+    """Pad a pass to 7 axes, plan its rounds and their layouts, compose each round's U (FP64).
+
+    nat='tma' plans for the TMA-fed kernel (first and last rounds with local
+    axes 0 and 1 on rows 0-3); its layouts are None when a first or last
+    round has axis 0 or 1 among its K axes."""
     pp = pad_pass(p, n)
     rounds = plan_rounds(pp, 3, pad='neighbors')
-    layouts = _choose_layouts([axes for axes, _ in rounds], nat)
+    if nat == 'tma':
+        lay = _choose_layouts_tma_cached(tuple(tuple(sorted(a)) for a, _ in rounds))
+        layouts = list(lay) if lay is not None else None
+        if layouts is None:
+            return pp, None, None
+    else:
+        layouts = _choose_layouts([axes for axes, _ in rounds], nat)
     mats = []
     for (axes, rops), lay in zip(rounds, layouts):
         U = np.eye(64)
@@ -830,18 +906,23 @@ def tma_box_dims(n, axes):
     return dims
 
 
-def tma_eligible(pp, n, nrounds):
+def tma_eligible(pp, n, layouts):
+    """True when dm_apply_pass_tma takes the pass planned as ``layouts`` (plan_tc_pass(..., nat='tma'))."""
     dims = tma_box_dims(n, pp.axes)
-    return dims is not None and len(dims) <= TMA_MAX_DIMS and nrounds <= TMA_MAX_ROUNDS
+    return layouts is not None and dims is not None and len(dims) <= TMA_MAX_DIMS \
+        and len(layouts) <= TMA_MAX_ROUNDS
 
 
 def encode_pass_tma(p, n, umats):
-    """DmTcPass for dm_apply_pass_tma (natural tile unswizzled, [Uh ; Ul] images).
+    """DmTcPass for dm_apply_pass_tma: natural-tile tables as plain element offsets (the TMA box is
+    unswizzled; the last round's are turned into global offsets by the library), [Uh ; Ul] images.
 
-    Raises TcPlanError when the pass has more rounds than stay resident or
-    its resident digits need more tensor-map dimensions than TMA has."""
-    pp, layouts, mats = plan_tc_pass(p, n, nat='linear')
-    if not tma_eligible(pp, n, len(layouts)):
-        raise TcPlanError('pass does not fit the TMA-fed kernel (%d rounds, dims %s)'
-                          % (len(layouts), tma_box_dims(n, pp.axes)))
+    Raises TcPlanError when the pass has more rounds than stay resident, its
+    resident digits need more tensor-map dimensions than TMA has, or its first
+    or last round acts on local axis 0 or 1."""
+    pp, layouts, mats = plan_tc_pass(p, n, nat='tma')
+    if not tma_eligible(pp, n, layouts):
+        raise TcPlanError('pass does not fit the TMA-fed kernel (%s rounds, dims %s)'
+                          % (len(layouts) if layouts else 'first/last round on axis 0 or 1',
+                             tma_box_dims(n, pp.axes)))
     return _encode_tc(pp, layouts, mats, 'linear', tc_round_image_tma, umats)

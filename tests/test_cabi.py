@@ -120,7 +120,7 @@ def test_malformed_tma_pass_is_rejected_on_host(lib):
     import numpy as np
     from qiskit_aakash_gb300 import program as P
     n = 10
-    ops = [P.Op('map1', (q,), np.eye(4)) for q in range(n)]
+    ops = [P.Op('map1', (q,), np.eye(4)) for q in range(n - 2)]     # off the two lowest-stride qubits
     passes = P.plan_passes(ops, n, 7, 2)
     umats = []
     good = P.encode_pass_tma(passes[0], n, umats)

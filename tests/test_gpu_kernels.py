@@ -248,15 +248,29 @@ def _physical_ops(rng, n, count):
     return ops
 
 
-@pytest.mark.parametrize('n', [7, 8, 10, 12])
-def test_tma_pass_equals_program_order(torch, n):
-    """dm_apply_pass_tma (TMA-fed tiles, resident round images) against the ops applied in FP64,
-    and against dm_apply_pass_tc on the same passes (same split arithmetic)."""
-    from test_planner import apply_op
+def _tma_case(kind, n):
+    """(ops, state) for the TMA-pass test: random physical ops off the two lowest-stride qubits, or the
+    recorded operations of a noisy layered circuit."""
     rng = np.random.default_rng(4000 + n)
-    ops = _physical_ops(rng, n, 20 if n == 7 else 80)     # 80 ops on 7 qubits need more than 6 rounds
+    if kind == 'random':
+        ops = [op for op in _physical_ops(rng, n, 60) if all(q < n - 2 for q in op.axes)]
+    else:
+        from qiskit_aakash_gb300 import batch as B
+        import qiskit_aakash_gb300 as dmg
+        qc = dmg.random_layer_circuit(n, 4, 5, barrier_after_gate=(n < 10))
+        opts = dmg.noise_options(depolarisation=1e-3, decoherence=0.995, decay=0.998, rotation_sigma=1e-3)
+        ops = B.compile_experiment(qc.to_experiment(), opts).ops
     st = rng.uniform(-1, 1, size=4 ** n) * 2.0 ** -n
     st[0] = 2.0 ** -n
+    return ops, st
+
+
+@pytest.mark.parametrize('kind,n', [('random', 7), ('random', 9), ('layered', 8), ('layered', 9), ('layered', 10)])
+def test_tma_pass_equals_program_order(torch, kind, n):
+    """dm_apply_pass_tma (TMA-fed tiles, resident round images, last round straight to global memory)
+    against the ops applied in FP64, and against dm_apply_pass_tc on the same passes."""
+    from test_planner import apply_op
+    ops, st = _tma_case(kind, n)
     ref = st.copy()
     for op in ops:
         ref = apply_op(ref, n, op)

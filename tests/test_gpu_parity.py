@@ -262,3 +262,40 @@ def test_trace_violation_raises(precision, monkeypatch):
     monkeypatch.setattr(engine.DeviceState, 'trace_error', corrupted)
     with pytest.raises(BasicAerError, match='Trace of densitymatrix is not one after the run'):
         run_gpu(qc.to_experiment(), opts, precision=precision)
+
+
+@pytest.mark.parametrize('n', [13, 14])
+def test_qft_workload_matches_reference_fixture(n):
+    """QFT + 2 random layers with the full noise model after every gate, against the reference itself.
+
+    tests/golden/make_c2_fixture.py ran the unmodified DmSimulatorPy on this
+    circuit (a few CPU-hours at n = 14) and kept its clock cycles, all 2**n
+    ensemble probabilities, every coefficient on the Z sublattice, 65,536
+    coefficients at seeded random indices and checksums of the whole vector.
+    FP64 on the GPU must match at 1e-12 (Pauli expectations 2**n a_s and
+    probabilities); the FP32 tensor-core form at FP32_TOL."""
+    import json
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden', 'c2_qft_n%d_L2_s0.npz' % n)
+    if not os.path.exists(path):
+        pytest.skip('fixture %s not generated' % os.path.basename(path))
+    fx = np.load(path)
+    meta = json.loads(str(fx['meta']))
+    qc = dmg.random_layer_circuit(n, meta['layers'], meta['seed'], barrier_after_gate=True, qft=True)
+    opts = dict(meta['options'])
+    for precision, tol in (('double', 1e-12), ('single', FP32_TOL)):
+        got, _ = run_gpu(qc.to_experiment(), opts, precision=precision)
+        assert got['number_of_clock_cycles'] == int(fx['clock_cycles'])
+        a = np.asarray(got['data']['coeffmatrix'])
+        p = np.array(list(got['data']['ensemble_probability'].values()))
+        assert list(got['data']['ensemble_probability'].keys())[1] == '0' * (n - 1) + '1'
+        np.testing.assert_allclose(p, fx['probs'], rtol=0, atol=tol)
+        np.testing.assert_allclose(a[fx['z_idx'].astype(np.int64)] * 2 ** n, fx['z_val'] * 2 ** n, rtol=0, atol=tol)
+        np.testing.assert_allclose(a[fx['idx'].astype(np.int64)] * 2 ** n, fx['val'] * 2 ** n, rtol=0, atol=tol)
+        if precision == 'double':
+            # checksums of all 4**n coefficients (each agreeing to ~1e-15 in units of 2**-n)
+            assert abs(a.sum() - float(fx['coeff_sum'])) * 2 ** n <= 1e-6
+            assert abs(np.abs(a).sum() - float(fx['coeff_abs_sum'])) * 2 ** n <= 1e-6
+        else:
+            assert np.abs(p - fx['probs']).sum() <= tol
+        del a
