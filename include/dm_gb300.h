@@ -200,6 +200,16 @@ int dm_max_abs_diff(const void *a_dev, int dtype_a, const void *b_dev, int dtype
 int dm_fp64_fma_probe_threads(void);
 int dm_fp64_fma_probe(double *out_dev, int64_t iters, void *stream);
 
+/* Page-locked host memory mapped into the device's address space
+ * (cudaHostAlloc, mapped and portable), exactly `bytes` long, or NULL.  The
+ * copy-out writes a result block of this kind directly from the chop kernel
+ * (dm_chop_copy with out_dev = dm_host_device_pointer(block)), in one pass
+ * over the CPU-GPU link, with no device staging buffer.  No reference
+ * counterpart (the reference's state lives in host memory). */
+void *dm_host_alloc(size_t bytes);
+void *dm_host_device_pointer(void *host);
+int dm_host_free(void *host);
+
 /* ------------------------------------------------------------------ levelling */
 
 /* Instruction kinds for dm_levelize. */

@@ -183,6 +183,9 @@ SIGNATURES = {
     'dm_fp64_fma_probe_threads': (_i, []),
     'dm_fp64_fma_probe': (_i, [_vp, ctypes.c_int64, _vp]),
     'dm_levelize': (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    'dm_host_alloc': (_vp, [_sz]),
+    'dm_host_device_pointer': (_vp, [_vp]),
+    'dm_host_free': (_i, [_vp]),
     'dm_batch_run': (_i, [_i, _vp, _sz, _vp, _sz, _vp, _sz, ctypes.POINTER(DmBatchInstance), _vp, _i,
                           ctypes.POINTER(DmBatchPass), _vp, _i, _vp, _vp, _vp]),
     'dm_batch_tc_scratch_bytes': (_sz, []),

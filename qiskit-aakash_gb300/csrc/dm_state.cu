@@ -51,6 +51,18 @@ __global__ void __launch_bounds__(256) chop_kernel(const T *__restrict__ st, int
     }
 }
 
+// The same over pairs: 16-byte stores (out may be mapped host memory, written over the
+// CPU-GPU link), total even, both pointers 16-byte aligned.
+template <typename T>
+__global__ void __launch_bounds__(256) chop_pairs_kernel(const T *__restrict__ st, int64_t pairs, double thr,
+                                                         double2 *__restrict__ out) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < pairs;
+         i += int64_t(gridDim.x) * blockDim.x) {
+        const double a = double(st[2 * i]), b = double(st[2 * i + 1]);
+        out[i] = make_double2(fabs(a) < thr ? 0.0 : a, fabs(b) < thr ? 0.0 : b);
+    }
+}
+
 struct GatherIdx {
     int64_t idx[64];
 };
@@ -241,14 +253,49 @@ extern "C" int dm_chop_copy_range(const void *state_dev, int n, int dtype, int64
     else
         state_dev = static_cast<const float *>(state_dev) + offset;
     cudaStream_t s = as_stream(stream);
-    if (dtype == DM_F64)
+    if (total % 2 == 0 && (reinterpret_cast<uintptr_t>(out_dev) & 15) == 0) {
+        const int64_t pairs = total / 2;
+        auto *out2 = reinterpret_cast<double2 *>(out_dev);
+        if (dtype == DM_F64)
+            chop_pairs_kernel<double><<<grid_for(pairs, 256), 256, 0, s>>>(static_cast<const double *>(state_dev),
+                                                                          pairs, threshold, out2);
+        else
+            chop_pairs_kernel<float><<<grid_for(pairs, 256), 256, 0, s>>>(static_cast<const float *>(state_dev),
+                                                                         pairs, threshold, out2);
+    } else if (dtype == DM_F64) {
         chop_kernel<double><<<grid_for(total, 256), 256, 0, s>>>(static_cast<const double *>(state_dev), total,
                                                                  threshold, out_dev);
-    else
+    } else {
         chop_kernel<float><<<grid_for(total, 256), 256, 0, s>>>(static_cast<const float *>(state_dev), total,
                                                                 threshold, out_dev);
+    }
     count_launch();
     return launch_status();
+}
+
+extern "C" void *dm_host_alloc(size_t bytes) {
+    if (bytes == 0) return nullptr;
+    void *p = nullptr;
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+extern "C" void *dm_host_device_pointer(void *host) {
+    void *d = nullptr;
+    if (!host || cudaHostGetDevicePointer(&d, host, 0) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return d;
+}
+
+extern "C" int dm_host_free(void *host) {
+    if (!host) return DM_ERR_ARG;
+    DM_CUDA_TRY(cudaFreeHost(host));
+    return DM_OK;
 }
 
 extern "C" int dm_gather(const void *state_dev, int n, int dtype, const int64_t *idx, int count, double *out_dev,

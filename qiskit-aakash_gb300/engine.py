@@ -43,18 +43,33 @@ _BLOCKS_PER_SIZE = 2
 
 
 class _ResultBlock:
-    def __init__(self, nbytes, buf):
+    """Page-locked host memory of exactly nbytes, mapped into the device's address space
+    (dm_host_alloc): the chop kernel writes a result into it directly over the CPU-GPU link."""
+
+    def __init__(self, nbytes, ptr):
         self.nbytes = nbytes
-        self.buf = buf          # page-locked host memory (torch uint8 tensor)
+        self.ptr = ptr
+        self.dev = N.lib().dm_host_device_pointer(ctypes.c_void_p(ptr))
         self.free = True
+
+    def array(self):
+        return np.ctypeslib.as_array((ctypes.c_double * (self.nbytes // 8)).from_address(self.ptr))
 
 
 def _pinned_host(nbytes):
-    """nbytes of page-locked host memory as a torch uint8 tensor, or None if it cannot be had."""
-    try:
-        return _torch().empty(nbytes, dtype=_torch().uint8, pin_memory=True)
-    except RuntimeError:
-        return None
+    """Address of nbytes of mapped page-locked host memory, or None if it cannot be had."""
+    ptr = N.lib().dm_host_alloc(ctypes.c_size_t(nbytes))
+    return ptr or None
+
+
+def _free_blocks():
+    for blocks in _RESULT_BLOCKS.values():
+        for b in blocks:
+            try:
+                N.lib().dm_host_free(ctypes.c_void_p(b.ptr))
+            except Exception:  # noqa: BLE001 - interpreter shutdown: the process frees it anyway
+                pass
+    _RESULT_BLOCKS.clear()
 
 
 def _release_block(blk):
@@ -87,9 +102,12 @@ def _host_bytes_available():
 
 
 def _result_array(total):
-    """(float64 array of ``total`` values, the page-locked torch view of it or None) for one copy-out."""
+    """(float64 array of ``total`` values, its result block or None) for one copy-out."""
+    import atexit
     import weakref
     nbytes = total * 8
+    if not _RESULT_BLOCKS:
+        atexit.register(_free_blocks)
     blocks = _RESULT_BLOCKS.setdefault(nbytes, [])
     blk = next((b for b in blocks if b.free), None)
     if blk is None and blocks:
@@ -105,11 +123,10 @@ def _result_array(total):
             return np.empty(total, dtype=np.float64), None
         blk = _ResultBlock(nbytes, buf)
         blocks.append(blk)
-    host = blk.buf.view(_torch().float64)
-    arr = host.numpy()
+    arr = blk.array()
     blk.free = False
     weakref.finalize(arr, _release_block, blk)
-    return arr, host
+    return arr, blk
 
 
 def _copy_buffers(device):
@@ -419,22 +436,18 @@ class DeviceState:
                    ctypes.c_void_p(out.data_ptr()), self.stream)
             return self._to_host(out)
         t0 = time.perf_counter()
-        result, host = _result_array(total)
-        self.copy_stats = {'result_block': host is not None, 'block_seconds': time.perf_counter() - t0}
-        dev, pinned = _copy_buffers(self.device)
+        result, blk = _result_array(total)
+        self.copy_stats = {'result_block': blk is not None, 'block_seconds': time.perf_counter() - t0}
         stream = torch.cuda.current_stream(self.device)
-        if host is not None:
-            # page-locked result: each chunk goes from the device buffer straight into it
-            for i, off in enumerate(range(0, total, _COPY_CHUNK)):
-                b = i % 2
-                cnt = min(_COPY_CHUNK, total - off)
-                N.call('dm_chop_copy_range', self.ptr, self.n, self.dtype, ctypes.c_int64(off), ctypes.c_int64(cnt),
-                       float(chop_threshold), ctypes.c_void_p(dev[b].data_ptr()), self.stream)
-                host[off:off + cnt].copy_(dev[b][:cnt], non_blocking=True)
+        if blk is not None:
+            # mapped page-locked result block: the chop kernel writes it directly, one pass
+            N.call('dm_chop_copy', self.ptr, self.n, self.dtype, float(chop_threshold), ctypes.c_void_p(blk.dev),
+                   self.stream)
             stream.synchronize()
             self.d2h_bytes += total * 8
             self.copy_stats['seconds'] = time.perf_counter() - t0
             return result
+        dev, pinned = _copy_buffers(self.device)
         events = [None, None]
         pending = None
         pool = _host_pool()

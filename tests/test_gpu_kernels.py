@@ -259,7 +259,11 @@ def _tma_case(kind, n):
         import qiskit_aakash_gb300 as dmg
         qc = dmg.random_layer_circuit(n, 4, 5, barrier_after_gate=(n < 10))
         opts = dmg.noise_options(depolarisation=1e-3, decoherence=0.995, decay=0.998, rotation_sigma=1e-3)
-        ops = B.compile_experiment(qc.to_experiment(), opts).ops
+        rec = B.compile_experiment(qc.to_experiment(), opts)
+        st = np.array([1.0])
+        for v in rec.init[0]:
+            st = np.kron(st, v)
+        return rec.ops, st * rec.init[1]          # the circuit's own start: |0...0>
     st = rng.uniform(-1, 1, size=4 ** n) * 2.0 ** -n
     st[0] = 2.0 ** -n
     return ops, st
@@ -335,8 +339,8 @@ def test_tensor_core_pass_rejects_bad_programs(torch):
 
 @pytest.mark.parametrize('dtype', [N.DM_F64, N.DM_F32])
 def test_chunked_copy_out_equals_one_shot(torch, dtype, monkeypatch):
-    """DeviceState.coefficients in chunks (chop range kernel; straight into a page-locked result
-    block, or through pinned staging buffers when the blocks are held) = dm_chop_copy."""
+    """DeviceState.coefficients: written by the chop kernel straight into a mapped page-locked result
+    block, or in chunks through pinned staging buffers when the blocks are held, = dm_chop_copy."""
     from qiskit_aakash_gb300 import engine
     n = 7
     rng = np.random.default_rng(5)
@@ -351,10 +355,10 @@ def test_chunked_copy_out_equals_one_shot(torch, dtype, monkeypatch):
     chunked = ds.coefficients(1e-15)                     # page-locked block 1, device -> block copies
     assert np.array_equal(one, chunked)
     blocks = engine._RESULT_BLOCKS[8 * 4 ** n]
-    assert len(blocks) == 1 and blocks[0].buf.is_pinned() and not blocks[0].free
+    assert len(blocks) == 1 and blocks[0].dev and not blocks[0].free     # mapped into the device's space
     second = ds.coefficients(1e-15)                      # block 1 held: block 2
     third = ds.coefficients(1e-15)                       # both held: staging buffers + host copies
-    assert len(blocks) == 2 and blocks[1].buf.is_pinned()
+    assert len(blocks) == 2 and blocks[1].dev
     for got in (chunked, second, third):
         assert np.array_equal(one, got)
     del second

@@ -7,9 +7,18 @@ import torch
 from qiskit_aakash_gb300 import engine
 
 
+_KEEP = []
+
+
+def _host_memory(nbytes):
+    buf = torch.empty(nbytes, dtype=torch.uint8)     # stands in for dm_host_alloc's page-locked memory
+    _KEEP.append(buf)
+    return buf.data_ptr()
+
+
 def _fake_pinned(monkeypatch, room=1 << 40, blocks_per_size=None):
     monkeypatch.setattr(engine, '_RESULT_BLOCKS', {})
-    monkeypatch.setattr(engine, '_pinned_host', lambda nbytes: torch.empty(nbytes, dtype=torch.uint8))
+    monkeypatch.setattr(engine, '_pinned_host', _host_memory)
     monkeypatch.setattr(engine, '_host_bytes_available', lambda: room)
     if blocks_per_size is not None:
         monkeypatch.setattr(engine, '_BLOCKS_PER_SIZE', blocks_per_size)
@@ -20,7 +29,7 @@ def test_result_blocks_are_reused_only_after_every_view_is_released(monkeypatch)
     total = 1 << 16
     a, ha = engine._result_array(total)
     assert ha is not None and a.shape == (total,) and a.dtype == np.float64
-    assert a.ctypes.data == ha.data_ptr()          # the array is the page-locked block
+    assert a.ctypes.data == ha.ptr                 # the array is the page-locked block
     a[:] = 1.0
     view = a.reshape(256, 256)[3:]
     del a, ha
