@@ -210,6 +210,13 @@ void *dm_host_alloc(size_t bytes);
 void *dm_host_device_pointer(void *host);
 int dm_host_free(void *host);
 
+/* Self-test of the tensor-core kernels' bounded waits (no reference
+ * counterpart): one thread waits on an mbarrier that nothing arrives on, gives
+ * up after limit_ns (0 < limit_ns <= 1e8) and sets *status_dev = 1, the status
+ * a pass kernel reports when a wait for an MMA commit or a tile load runs out.
+ * Lets a test check the failure path without faulting or hanging a GPU. */
+int dm_tc_wait_selftest(int *status_dev, int64_t limit_ns, void *stream);
+
 /* ------------------------------------------------------------------ levelling */
 
 /* Instruction kinds for dm_levelize. */

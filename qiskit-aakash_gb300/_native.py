@@ -186,6 +186,7 @@ SIGNATURES = {
     'dm_host_alloc': (_vp, [_sz]),
     'dm_host_device_pointer': (_vp, [_vp]),
     'dm_host_free': (_i, [_vp]),
+    'dm_tc_wait_selftest': (_i, [_vp, ctypes.c_int64, _vp]),
     'dm_batch_run': (_i, [_i, _vp, _sz, _vp, _sz, _vp, _sz, ctypes.POINTER(DmBatchInstance), _vp, _i,
                           ctypes.POINTER(DmBatchPass), _vp, _i, _vp, _vp, _vp]),
     'dm_batch_tc_scratch_bytes': (_sz, []),

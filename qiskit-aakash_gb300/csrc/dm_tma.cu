@@ -532,3 +532,31 @@ extern "C" int dm_apply_pass_tma(void *state_dev, int n, const dm_tc_pass *pass,
     count_launch();
     return launch_status();
 }
+
+// ---------------------------------------------------------------------------
+// bounded-wait self-test: the failure path of every tensor-core kernel's waits
+// ---------------------------------------------------------------------------
+
+namespace dmg {
+namespace tma {
+
+// One thread waits, with a limit of limit_ns, on an mbarrier that nothing arrives on, as the
+// pass kernels wait for an MMA commit or a tile load; the wait gives up and the kernel reports
+// status 1, exactly as a pass kernel does before it drains and returns.
+__global__ void wait_selftest_kernel(int *status, int64_t limit_ns) {
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t b = smem_u32(&bar);
+    tcg::mbar_init(b, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (!tcg::mbar_wait(b, 0, uint64_t(limit_ns))) atomicExch(status, 1);
+}
+
+}  // namespace tma
+}  // namespace dmg
+
+extern "C" int dm_tc_wait_selftest(int *status_dev, int64_t limit_ns, void *stream) {
+    DM_CHECK_ARG(status_dev && limit_ns > 0 && limit_ns <= 100000000);   // at most 0.1 s
+    dmg::tma::wait_selftest_kernel<<<1, 1, 0, as_stream(stream)>>>(status_dev, limit_ns);
+    count_launch();
+    return launch_status();
+}

@@ -374,3 +374,25 @@ def test_chunked_copy_out_equals_one_shot(torch, dtype, monkeypatch):
         out = torch.empty(10, dtype=torch.float64, device='cuda')
         N.call('dm_chop_copy_range', ds.ptr, n, dtype, ctypes.c_int64(4 ** n - 5), ctypes.c_int64(10), 0.0,
                vp(out), stream(torch))
+
+
+def test_bounded_wait_gives_up_and_the_engine_raises(torch):
+    """A wait that nothing completes runs out after its limit and sets the status word; the engine
+    turns a set status into BasicAerError at its next flush (no fault, no hang: 20 ms limit)."""
+    from qiskit_aakash_gb300 import engine
+    from qiskit_aakash_gb300.exceptions import BasicAerError
+    from qiskit_aakash_gb300.program import IDENTITY4
+    ds = engine.DeviceState(8, precision='single')
+    assert ds.status is not None and int(ds.status.item()) == 0
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    N.call('dm_tc_wait_selftest', vp(ds.status), ctypes.c_int64(20_000_000), stream(torch))
+    t1.record()
+    torch.cuda.synchronize()
+    assert int(ds.status.item()) == 1
+    assert t0.elapsed_time(t1) >= 19.0           # it waited its limit, then gave up
+    ds.init_product(np.tile([1.0, 0.0, 0.0, 1.0], (8, 1)), 2.0 ** -8)
+    ds.map1(3, IDENTITY4)
+    with pytest.raises(BasicAerError, match='bounded wait'):
+        ds.flush()
