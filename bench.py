@@ -160,7 +160,7 @@ def measured_peaks():
 
 def profiled_value(key):
     """A figure of the pass kernel's committed ncu summary ('key: value' line), if any."""
-    path = os.path.join(ROOT, 'profiles', 'pass_tc_kernel_fp16_split_fp32_n14.md')
+    path = os.path.join(ROOT, 'profiles', 'pass_tma_kernel_fp16_split_fp32_n14.md')
     try:
         for line in open(path):
             if line.startswith(key + ':'):
