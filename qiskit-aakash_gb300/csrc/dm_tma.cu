@@ -19,8 +19,10 @@
 //   store of its current tile has read the slot, and the store is
 //   asynchronous (bulk group); no thread computes a global address;
 // * the pass's round images ([Uh ; Ul], 16 KB per round) are loaded once per
-//   CTA by bulk copies and stay in shared memory for the whole pass (up to
-//   kMaxRounds rounds; longer passes run on pass_tc_kernel).
+//   CTA by bulk copies and stay in shared memory for the whole pass when it
+//   has up to kUSlots rounds; a longer pass keeps its first kStreamFrom rounds
+//   resident and streams each later round's image, per team, into one spare
+//   slot (loaded as soon as the previous round's MMAs have read that slot).
 //
 // Tensor map.  The state is a 4**n vector whose flat index is the base-4
 // number of the qubits' Pauli labels (qubit n-1 the lowest digit).  The 7
@@ -61,16 +63,20 @@ using tcg::smem_u32;
 constexpr int kTeams = 2;
 constexpr int kTeamThreads = 256;
 constexpr int kThreads = kTeams * kTeamThreads;
-constexpr int kMaxRounds = 6;                                // round images resident in shared memory
+constexpr int kMaxRounds = 16;                               // rounds of one pass
+constexpr int kUSlots = 6;                                   // round-image slots in shared memory
+constexpr int kStreamFrom = 4;                               // longer passes: rounds >= 4 streamed (slot 4 + team)
 constexpr int kMaxDims = 5;                                  // tensor-map rank
 constexpr uint32_t kSlotBytes = 2 * kABytes;                 // 64 KB: AH | AL, or the FP32 tile
 constexpr uint32_t kUBytes = 2 * kBImage;                    // 16 KB per round: Uh | Ul (one 128-row operand)
 constexpr uint32_t kUHalves = kUBytes / 2;
-constexpr uint32_t kSmemBytes = kTeams * kSlotBytes + kMaxRounds * kUBytes + 1024;   // + alignment slack
+constexpr uint32_t kSmemBytes = kTeams * kSlotBytes + kUSlots * kUBytes + 1024;   // + alignment slack
 constexpr uint32_t kTmemCols = 512;                          // per team: two M = 128 blocks x (D1 | D2)
 
 struct TmaPass {
     int nrounds, ndims;
+    int nres;                        // rounds whose images stay resident (all of them, or kStreamFrom)
+    int last_vec;                    // the last round's K digit 0 is local axis 0: 16-byte stores
     float up, down;                  // 2**n, 2**-n
     int64_t ntiles;
     int8_t gap_first[kMaxDims];      // tile-index digit of the first non-resident digit above dimension i
@@ -179,6 +185,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     __shared__ __align__(8) uint64_t load_bar[kTeams];
     __shared__ __align__(8) uint64_t mma_bar[kTeams];
     __shared__ __align__(8) uint64_t u_bar;
+    __shared__ __align__(8) uint64_t stream_bar[kTeams];
     __shared__ uint32_t tmem_base_s;
     unsigned char *smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -187,11 +194,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     unsigned char *AH = smem + team * kSlotBytes, *AL = AH + kABytes;
     unsigned char *U = smem + kTeams * kSlotBytes;
     const uint32_t lbar = smem_u32(&load_bar[team]), mbar = smem_u32(&mma_bar[team]), ubar = smem_u32(&u_bar);
+    const uint32_t sbar = smem_u32(&stream_bar[team]);
+    // round r's images: resident slot r, or this team's streaming slot
+    auto uslot = [&](int r) -> uint32_t {
+        return smem_u32(U + (r < p.nres ? r : kStreamFrom + team) * kUBytes);
+    };
 
     if (tid == 0) {
         for (int i = 0; i < kTeams; ++i) {
             tcg::mbar_init(smem_u32(&load_bar[i]), 1);
             tcg::mbar_init(smem_u32(&mma_bar[i]), 1);
+            tcg::mbar_init(smem_u32(&stream_bar[i]), 1);
         }
         tcg::mbar_init(ubar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -210,8 +223,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int64_t stride = int64_t(gridDim.x) * kTeams;
     int64_t t = int64_t(blockIdx.x) * kTeams + team;
     if (tid == 0) {   // the pass's round images, once per CTA
-        tcg::mbar_expect_tx(ubar, uint32_t(p.nrounds) * kUBytes);
-        for (int r = 0; r < p.nrounds; ++r)
+        tcg::mbar_expect_tx(ubar, uint32_t(p.nres) * kUBytes);
+        for (int r = 0; r < p.nres; ++r)
             tcg::bulk_load(smem_u32(U + r * kUBytes), umats + p.uoff[r], kUBytes, ubar);
     }
     if (leader && t < p.ntiles) {
@@ -222,7 +235,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     bool load_pending = t < p.ntiles;
     bool mma_pending = false;
-    uint32_t lphase = 0, mphase = 0;
+    bool u_pending = false;                 // a streamed round image in flight (leader)
+    uint32_t lphase = 0, mphase = 0, uphase = 0;
+    auto stream_u = [&](int r) {            // leader: round r's images into the team's streaming slot
+        tcg::mbar_expect_tx(sbar, kUBytes);
+        tcg::bulk_load(uslot(r), umats + p.uoff[r], kUBytes, sbar);
+        u_pending = true;
+    };
     const bool u_ok = team_and(mbar_wait(ubar, 0), team);
     if (!u_ok && ttid == 0) atomicExch(status, 1);
 
@@ -239,6 +258,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         lphase ^= 1;
         load_pending = false;
         const int64_t tn = t + stride;
+        if (leader && p.nrounds > p.nres) stream_u(p.nres);   // the slot is free: the last round's MMAs are done
         if (leader && tn < p.ntiles) {   // the team's next tile heads for L2 while this one runs
             int c[kMaxDims];
             tile_coords(p, tn, c);
@@ -273,10 +293,18 @@ __global__ void __launch_bounds__(kThreads, 1)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             team_sync(team);
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            if (leader) {
+            bool issue = leader;
+            if (leader && r >= p.nres) {     // a streamed image: wait for its bulk copy
+                issue = mbar_wait(sbar, uphase);
+                if (issue) {
+                    uphase ^= 1;
+                    u_pending = false;
+                }                            // else no MMA and no commit: the team's wait below runs out
+            }
+            if (issue) {
                 // D[:, 0:64] = h Uh^T and D[:, 64:128] = h Ul^T (one N = 128 chain over [Uh ; Ul]),
                 // then D[:, 64:128] += l Uh^T (N = 64), for both M = 128 blocks
-                const uint32_t ah = smem_u32(AH), al = smem_u32(AL), ub = smem_u32(U + r * kUBytes);
+                const uint32_t ah = smem_u32(AH), al = smem_u32(AL), ub = uslot(r);
 #pragma unroll
                 for (int mb = 0; mb < 2; ++mb) {
                     const uint32_t aoff = mb * (kABytes / 2);
@@ -310,6 +338,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             mma_pending = false;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const bool last = r + 1 == p.nrounds;
+            if (leader && r >= p.nres && !last) stream_u(r + 1);   // this round's MMAs have read the slot
             if (last && leader && tn < p.ntiles) {
                 // the slot's operands are consumed: the next tile's load (from L2) overlaps this epilogue
                 int c[kMaxDims];
@@ -344,10 +373,15 @@ __global__ void __launch_bounds__(kThreads, 1)
                     for (int d1 = 0; d1 < 4; ++d1) {
                         float *q = row + o2 + (d1 & 1 ? p.lastg[10] : 0) + (d1 & 2 ? p.lastg[11] : 0);
                         const int j = 4 * d1 + 16 * d2;
-                        q[0] = v[j] * down;
-                        q[p.lastg[8]] = v[j + 1] * down;
-                        q[p.lastg[9]] = v[j + 2] * down;
-                        q[p.lastg[8] + p.lastg[9]] = v[j + 3] * down;
+                        if (p.last_vec) {    // K digit 0 is local axis 0: four contiguous coefficients
+                            *reinterpret_cast<float4 *>(q) =
+                                make_float4(v[j] * down, v[j + 1] * down, v[j + 2] * down, v[j + 3] * down);
+                        } else {
+                            q[0] = v[j] * down;
+                            q[p.lastg[8]] = v[j + 1] * down;
+                            q[p.lastg[9]] = v[j + 2] * down;
+                            q[p.lastg[8] + p.lastg[9]] = v[j + 3] * down;
+                        }
                     }
                 }
             }
@@ -360,6 +394,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (mma_pending) mbar_wait(mbar, mphase);
     if (load_pending) mbar_wait(lbar, lphase);
     if (!u_ok) mbar_wait(ubar, 0);
+    if (u_pending) mbar_wait(sbar, uphase);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
@@ -481,6 +516,7 @@ extern "C" int dm_apply_pass_tma(void *state_dev, int n, const dm_tc_pass *pass,
     cuuint32_t box[tma::kMaxDims], estride[tma::kMaxDims];
     if (!tma_dims(n, pass->axes, p, gdim, gstride, box)) return DM_ERR_PROGRAM;
     p.nrounds = nr;
+    p.nres = nr <= tma::kUSlots ? nr : tma::kStreamFrom;
     p.up = float(ldexp(1.0, n));
     p.down = float(ldexp(1.0, -n));
     p.ntiles = int64_t(1) << (2 * (n - tc::kAxes));
@@ -506,6 +542,9 @@ extern "C" int dm_apply_pass_tma(void *state_dev, int n, const dm_tc_pass *pass,
                 const int pos = n - 1 - pass->axes[b >> 1];
                 p.lastg[i] = (int64_t(1) << (b & 1)) << (2 * pos);
             }
+            // K digit 0 = local axis 0 (K bits 0, 1 at offsets 1, 2): every other bit is a multiple of
+            // 4 elements, so each group of four lands 16-byte aligned
+            p.last_vec = p.lastg[8] == 1 && p.lastg[9] == 2;
         }
         for (int i = 0; i < 8; ++i) o.rowc[i] = in.rowc[i];
         for (int i = 0; i < 6; ++i) o.kc[i] = in.kc[i];

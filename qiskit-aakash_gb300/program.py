@@ -669,21 +669,31 @@ def _tma_conversion_cost(layout):
 def _choose_layouts_tma_cached(rounds_axes):
     import itertools
     nlast = len(rounds_axes) - 1
-    if any(a in rounds_axes[0] or a in rounds_axes[nlast] for a in (0, 1)):
-        return None
     layouts = []
     prev = None
+
+    def fixed_next(nxt_axes):
+        """The layouts the next round may take when it is the last round (its rows are fixed)."""
+        return [TcLayout(list(d), r) for d, r in _tma_last_candidates(sorted(nxt_axes), None)]
+
     for ri, axes in enumerate(rounds_axes):
         axes = sorted(axes)
         nonround = [tb for tb in range(2 * TC_AXES) if tb // 2 not in axes]
         nxt_axes = set(rounds_axes[ri + 1]) if ri < nlast else None
         cands = []
-        if ri == 0 or ri == nlast:
-            rest = [tb for tb in nonround if tb not in TMA_FIXED_ROWS]
-            fifth = ([4] if 4 in rest else []) + [tb for tb in rest if tb != 4][:2]
-            for digits in itertools.permutations(axes):
-                for f in fifth:
-                    cands.append(TcLayout(list(digits), TMA_FIXED_ROWS + [f] + [tb for tb in rest if tb != f]))
+        if ri == nlast:
+            cands = [TcLayout(list(d), r) for d, r in _tma_last_candidates(axes, prev)]
+        elif ri == 0:
+            if all(tb in nonround for tb in TMA_FIXED_ROWS):
+                rest = [tb for tb in nonround if tb not in TMA_FIXED_ROWS]
+                fifth = ([4] if 4 in rest else []) + [tb for tb in rest if tb != 4][:2]
+                for digits in itertools.permutations(axes):
+                    for f in fifth:
+                        cands.append(TcLayout(list(digits), TMA_FIXED_ROWS + [f] + [tb for tb in rest if tb != f]))
+            else:            # round 0 acts on local axis 0 or 1: lanes on the lowest free tile bits
+                low = nonround[:5]
+                for digits in itertools.permutations(axes):
+                    cands.append(TcLayout(list(digits), low + [tb for tb in nonround if tb not in low]))
         else:
             lanes = [tb for tb in prev.rowbits[:5] if tb in nonround]
             keep = [tb for tb in prev.rowbits if tb in nonround]
@@ -703,11 +713,9 @@ def _choose_layouts_tma_cached(rounds_axes):
                 vec = 8 if _vec_digit(prev, cand.digits[0]) >= 0 else None
                 cost += _transition_cost(prev, cand.byte_of_bit, vec)
             if ri < nlast:
-                if ri + 1 == nlast:      # the next round's rows are fixed: its exact incoming cost
-                    cost += min(_transition_cost(cand, TcLayout(list(d), TMA_FIXED_ROWS + [
-                        tb for tb in range(2 * TC_AXES) if tb // 2 not in nxt_axes and tb not in TMA_FIXED_ROWS
-                    ]).byte_of_bit, 8 if _vec_digit(cand, d[0]) >= 0 else None)
-                        for d in itertools.permutations(sorted(nxt_axes)))
+                if ri + 1 == nlast:      # the last round's rows are fixed: its exact incoming cost
+                    cost += min(_transition_cost(cand, nxt.byte_of_bit, 8 if _vec_digit(cand, nxt.digits[0]) >= 0
+                                                 else None) for nxt in fixed_next(nxt_axes))
                 else:
                     cost += _best_next_cost(cand, nxt_axes)
             if best is None or cost < best[0]:
@@ -715,6 +723,28 @@ def _choose_layouts_tma_cached(rounds_axes):
         layouts.append(best[1])
         prev = best[1]
     return tuple(layouts)
+
+
+def _tma_last_candidates(axes, prev):
+    """(digits, rowbits) candidates of the last round of a TMA-fed pass, which stores its rows to
+    global memory: with local axis 0 among its axes, axis 0 is K digit 0 (four contiguous
+    coefficients per thread, 16-byte stores); otherwise tile bits 0-3 (axes 0 and 1, or axis 0
+    and the lowest free bits) are rows 0-3, so 16 lanes cover contiguous coefficients."""
+    import itertools
+    nonround = [tb for tb in range(2 * TC_AXES) if tb // 2 not in axes]
+    out = []
+    if 0 in axes:
+        others = [a for a in axes if a != 0]
+        rows = nonround
+        for perm in itertools.permutations(others):
+            out.append(([0] + list(perm), rows))
+        return out
+    head = [tb for tb in TMA_FIXED_ROWS if tb in nonround]
+    head += [tb for tb in nonround if tb not in head][:4 - len(head)]
+    rest = [tb for tb in nonround if tb not in head]
+    for digits in itertools.permutations(axes):
+        out.append((list(digits), head + rest))
+    return out
 
 
 def _choose_layouts(rounds_axes, nat='xor'):
@@ -783,15 +813,11 @@ def plan_tc_pass(p, n, nat='xor'):
     """Pad a pass to 7 axes, plan its rounds and their layouts, compose each round's U (FP64).
 
     nat='tma' plans for the TMA-fed kernel (first and last rounds with local
-    axes 0 and 1 on rows 0-3); its layouts are None when a first or last
-    round has axis 0 or 1 among its K axes."""
+    axes 0 and 1 on rows 0-3 where they are not among the round's axes)."""
     pp = pad_pass(p, n)
     rounds = plan_rounds(pp, 3, pad='neighbors')
     if nat == 'tma':
-        lay = _choose_layouts_tma_cached(tuple(tuple(sorted(a)) for a, _ in rounds))
-        layouts = list(lay) if lay is not None else None
-        if layouts is None:
-            return pp, None, None
+        layouts = list(_choose_layouts_tma_cached(tuple(tuple(sorted(a)) for a, _ in rounds)))
     else:
         layouts = _choose_layouts([axes for axes, _ in rounds], nat)
     mats = []
@@ -864,7 +890,7 @@ def encode_pass_tc(p, n, umats):
 # TMA-fed tensor-core pass (dm_apply_pass_tma)
 # ---------------------------------------------------------------------------
 
-TMA_MAX_ROUNDS = 6        # round images resident in shared memory
+TMA_MAX_ROUNDS = 16       # rounds of one pass (up to 6 with every round image resident, more streamed)
 TMA_MAX_DIMS = 5          # tensor-map rank
 TMA_IMAGE_HALVES = 2 * 4096
 
@@ -917,12 +943,10 @@ def encode_pass_tma(p, n, umats):
     """DmTcPass for dm_apply_pass_tma: natural-tile tables as plain element offsets (the TMA box is
     unswizzled; the last round's are turned into global offsets by the library), [Uh ; Ul] images.
 
-    Raises TcPlanError when the pass has more rounds than stay resident, its
-    resident digits need more tensor-map dimensions than TMA has, or its first
-    or last round acts on local axis 0 or 1."""
+    Raises TcPlanError when the pass has more than TMA_MAX_ROUNDS rounds or
+    its resident digits need more tensor-map dimensions than TMA has."""
     pp, layouts, mats = plan_tc_pass(p, n, nat='tma')
     if not tma_eligible(pp, n, layouts):
-        raise TcPlanError('pass does not fit the TMA-fed kernel (%s rounds, dims %s)'
-                          % (len(layouts) if layouts else 'first/last round on axis 0 or 1',
-                             tma_box_dims(n, pp.axes)))
+        raise TcPlanError('pass does not fit the TMA-fed kernel (%d rounds, dims %s)'
+                          % (len(layouts), tma_box_dims(n, pp.axes)))
     return _encode_tc(pp, layouts, mats, 'linear', tc_round_image_tma, umats)

@@ -254,6 +254,8 @@ def _tma_case(kind, n):
     rng = np.random.default_rng(4000 + n)
     if kind == 'random':
         ops = [op for op in _physical_ops(rng, n, 60) if all(q < n - 2 for q in op.axes)]
+    elif kind == 'dense':      # every qubit: long passes (streamed round images), axis 0 in first / last rounds
+        ops = _physical_ops(rng, n, 90)
     else:
         from qiskit_aakash_gb300 import batch as B
         import qiskit_aakash_gb300 as dmg
@@ -269,7 +271,8 @@ def _tma_case(kind, n):
     return ops, st
 
 
-@pytest.mark.parametrize('kind,n', [('random', 7), ('random', 9), ('layered', 8), ('layered', 9), ('layered', 10)])
+@pytest.mark.parametrize('kind,n', [('random', 7), ('random', 9), ('layered', 8), ('layered', 9), ('layered', 10),
+                                    ('dense', 7), ('dense', 9)])
 def test_tma_pass_equals_program_order(torch, kind, n):
     """dm_apply_pass_tma (TMA-fed tiles, resident round images, last round straight to global memory)
     against the ops applied in FP64, and against dm_apply_pass_tc on the same passes."""
