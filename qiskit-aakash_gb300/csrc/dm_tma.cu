@@ -46,6 +46,7 @@
 #include <cuda.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "dm_common.cuh"
@@ -77,6 +78,8 @@ struct TmaPass {
     int nrounds, ndims;
     int nres;                        // rounds whose images stay resident (all of them, or kStreamFrom)
     int last_vec;                    // the last round's K digit 0 is local axis 0: 16-byte stores
+    int group_prefetch;              // pmap's box spans the 4 tiles of the lowest non-resident digit
+    int group_half;                  // coordinate step of its second half (outermost dimension)
     float up, down;                  // 2**n, 2**-n
     int64_t ntiles;
     int8_t gap_first[kMaxDims];      // tile-index digit of the first non-resident digit above dimension i
@@ -179,7 +182,8 @@ __device__ __forceinline__ bool team_and(bool ok, int team) {
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
-    pass_tma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ TmaPass p,
+    pass_tma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap pmap,
+                    const __grid_constant__ TmaPass p,
                     float *__restrict__ st, const uint16_t *__restrict__ umats, int *status) {
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t load_bar[kTeams];
@@ -259,10 +263,20 @@ __global__ void __launch_bounds__(kThreads, 1)
         load_pending = false;
         const int64_t tn = t + stride;
         if (leader && p.nrounds > p.nres) stream_u(p.nres);   // the slot is free: the last round's MMAs are done
-        if (leader && tn < p.ntiles) {   // the team's next tile heads for L2 while this one runs
+        if (leader && tn < p.ntiles) {
+            // the team's next tile heads for L2 while this one runs; with a group box, the team holding
+            // the first of the four tiles that differ only in the lowest non-resident digit (adjacent
+            // in memory, run by this CTA and the next at the same time) prefetches all four at once,
+            // so DRAM sees runs of four times the tile's contiguous rows
             int c[kMaxDims];
             tile_coords(p, tn, c);
-            tma_prefetch_l2(&tmap, p.ndims, c);
+            if (!p.group_prefetch) {
+                tma_prefetch_l2(&tmap, p.ndims, c);
+            } else if ((tn & 3) == 0) {     // the group in two halves of its outermost dimension
+                tma_prefetch_l2(&pmap, p.ndims, c);
+                c[p.ndims - 1] += p.group_half;
+                tma_prefetch_l2(&pmap, p.ndims, c);
+            }
         }
         // ---- natural tile -> round 0's operand (h / l), in place: one operand row per thread ----
         // lanes hold rows 0-4, whose tile bits 0-3 are the 16 contiguous coefficients of the tile:
@@ -555,19 +569,38 @@ extern "C" int dm_apply_pass_tma(void *state_dev, int n, const dm_tc_pass *pass,
     EncodeTiled enc = encode_fn();
     if (!enc) return DM_ERR_CUDA;
     for (int i = 0; i < tma::kMaxDims; ++i) estride[i] = 1;
-    CUtensorMap map;
+    CUtensorMap map, pmap;
     if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, cuuint32_t(p.ndims), state_dev, gdim, gstride, box, estride,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return DM_ERR_CUDA;
+    // group prefetch box: dimension 0 widened over the lowest non-resident digit (tile-index digit 0),
+    // when that digit sits directly above dimension 0 and the widened row stays within 256 elements;
+    // the team stride must keep tile-index digit 0 per team (a multiple of 4 teams per iteration)
+    const int64_t grid = std::min<int64_t>(sm_count(), (p.ntiles + tma::kTeams - 1) / tma::kTeams);
+    // (the driver takes boxes of at most 128 KB, so the four tiles go in two halves of the outermost
+    // dimension)
+    p.group_prefetch = p.gap_len[0] >= 1 && p.box_log4[0] <= 3 && p.ntiles >= 4 && p.ndims >= 2 &&
+                       (grid * tma::kTeams) % 4 == 0;
+    pmap = map;
+    if (p.group_prefetch) {
+        cuuint32_t pbox[tma::kMaxDims];
+        for (int i = 0; i < tma::kMaxDims; ++i) pbox[i] = box[i];
+        pbox[0] = box[0] * 4;
+        pbox[p.ndims - 1] = box[p.ndims - 1] / 2;
+        p.group_half = int(pbox[p.ndims - 1]);
+        if (enc(&pmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, cuuint32_t(p.ndims), state_dev, gdim, gstride, pbox,
+                estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+            p.group_prefetch = 0;   // the driver refuses the wider box: prefetch tile by tile
+            pmap = map;
+        }
+    }
     if (ensure_max_dynamic_smem(reinterpret_cast<const void *>(tma::pass_tma_kernel), int(tma::kSmemBytes)) !=
         cudaSuccess)
         return DM_ERR_CUDA;
-    int64_t grid = sm_count();
-    const int64_t want = (p.ntiles + tma::kTeams - 1) / tma::kTeams;
-    if (grid > want) grid = want;
     tma::pass_tma_kernel<<<int(grid), tma::kThreads, tma::kSmemBytes, as_stream(stream)>>>(
-        map, p, static_cast<float *>(state_dev), umats_dev, status_dev);
+        map, pmap, p, static_cast<float *>(state_dev), umats_dev, status_dev);
     count_launch();
     return launch_status();
 }

@@ -685,11 +685,14 @@ def _choose_layouts_tma_cached(rounds_axes):
             cands = [TcLayout(list(d), r) for d, r in _tma_last_candidates(axes, prev)]
         elif ri == 0:
             if all(tb in nonround for tb in TMA_FIXED_ROWS):
+                # rows 0-4 hold tile bits 0-3 and one more bit in any order: conflict-free word loads
                 rest = [tb for tb in nonround if tb not in TMA_FIXED_ROWS]
                 fifth = ([4] if 4 in rest else []) + [tb for tb in rest if tb != 4][:2]
                 for digits in itertools.permutations(axes):
                     for f in fifth:
-                        cands.append(TcLayout(list(digits), TMA_FIXED_ROWS + [f] + [tb for tb in rest if tb != f]))
+                        tail = [tb for tb in rest if tb != f]
+                        for head in itertools.permutations(TMA_FIXED_ROWS + [f]):
+                            cands.append(TcLayout(list(digits), list(head) + tail))
             else:            # round 0 acts on local axis 0 or 1: lanes on the lowest free tile bits
                 low = nonround[:5]
                 for digits in itertools.permutations(axes):
@@ -743,7 +746,8 @@ def _tma_last_candidates(axes, prev):
     head += [tb for tb in nonround if tb not in head][:4 - len(head)]
     rest = [tb for tb in nonround if tb not in head]
     for digits in itertools.permutations(axes):
-        out.append((list(digits), head + rest))
+        for h in itertools.permutations(head):      # rows 0-3 in any order: lanes 0-15 stay contiguous
+            out.append((list(digits), list(h) + rest))
     return out
 
 
@@ -933,10 +937,15 @@ def tma_box_dims(n, axes):
 
 
 def tma_eligible(pp, n, layouts):
-    """True when dm_apply_pass_tma takes the pass planned as ``layouts`` (plan_tc_pass(..., nat='tma'))."""
+    """True when dm_apply_pass_tma takes the pass planned as ``layouts`` (plan_tc_pass(..., nat='tma')).
+
+    Not when the last round acts on both local axes 0 and 1: its rows then hold
+    none of the tile's contiguous coefficients, so every lane's stores land in
+    a different place (measured: about three times the pass's time on
+    pass_tc_kernel)."""
     dims = tma_box_dims(n, pp.axes)
     return layouts is not None and dims is not None and len(dims) <= TMA_MAX_DIMS \
-        and len(layouts) <= TMA_MAX_ROUNDS
+        and len(layouts) <= TMA_MAX_ROUNDS and not {0, 1} <= set(layouts[-1].digits)
 
 
 def encode_pass_tma(p, n, umats):
