@@ -274,8 +274,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                 tma_prefetch_l2(&tmap, p.ndims, c);
             } else if ((tn & 3) == 0) {     // the group in two halves of its outermost dimension
                 tma_prefetch_l2(&pmap, p.ndims, c);
-                c[p.ndims - 1] += p.group_half;
-                tma_prefetch_l2(&pmap, p.ndims, c);
+                int c2[kMaxDims];
+#pragma unroll
+                for (int i = 0; i < kMaxDims; ++i) c2[i] = c[i] + (i == p.ndims - 1 ? p.group_half : 0);
+                tma_prefetch_l2(&pmap, p.ndims, c2);
             }
         }
         // ---- natural tile -> round 0's operand (h / l), in place: one operand row per thread ----
