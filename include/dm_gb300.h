@@ -178,7 +178,8 @@ int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, const uint1
  * natural-tile tables (natrow / natk, and rowc / kc of the last round) are
  * plain element offsets (the TMA box is unswizzled); each round's images are
  * 8192 FP16 values, Uh then Ul = fp16(2**11 (U - Uh)) (no 2**11 Uh image);
- * at most 6 rounds; the resident axes must fit a 5-dimensional tensor map
+ * at most 16 rounds (up to 6 with every image resident in shared memory,
+ * the later ones streamed per round); the resident axes must fit a 5-dimensional tensor map
  * (runs of consecutive qubits, at most 4 per dimension).  Returns
  * DM_ERR_PROGRAM for a pass outside these limits (the caller then uses
  * dm_apply_pass_tc).  Same role as dm_apply_pass (dm_simulator.py:1005-1177). */
@@ -256,6 +257,26 @@ typedef struct dm_batch_pass {
     int16_t round_end[DM_MAX_ROUNDS];
     dm_op ops[DM_MAX_PASS_OPS];        /* moff relative to the instance's coefficient block */
 } dm_batch_pass;
+
+/* Round image formats of dm_compose_rounds. */
+#define DM_IMAGE_TC 1    /* 12288 FP16 values per round: 2**11 Uh | Ul | Uh (dm_apply_pass_tc) */
+#define DM_IMAGE_TMA 2   /* 8192 FP16 values per round: Uh | Ul (dm_apply_pass_tma) */
+
+/* The round images of one tensor-core pass, composed in FP64 on the device:
+ * round r's 64x64 transfer matrix U (input and output index j = d0 + 4 d1
+ * + 16 d2 over the round's local axes pass->round_axes[r][0..2]) is ops
+ * [round_end[r-1], round_end[r]) applied to the 64 unit vectors, written at
+ * images_dev + r * (values per round) as Uh = fp16(U) and
+ * Ul = fp16(2**11 (U - Uh)) in the K-major core-matrix order the passes
+ * read.  Op coefficients (moff in doubles) come from mats_dev; ops may be
+ * DM_OP_MAP1, DM_OP_MAP2, DM_OP_DIAG2 and DM_OP_CX, with their digit
+ * positions in the flags as in the register rounds.  pass->k and
+ * pass->axes are not read.  One launch of nrounds CTAs, stream-ordered
+ * before the pass that reads the images.  The reference multiplies the
+ * same per-gate maps one gate at a time on the host (dm_simulator.py:1005-1177);
+ * here they are folded into one matrix per round. */
+int dm_compose_rounds(int format, const dm_batch_pass *pass, const double *mats_dev, size_t mats_count,
+                      uint16_t *images_dev, size_t images_count, void *stream);
 
 /* One independent circuit instance of a batched program. */
 typedef struct dm_batch_instance {

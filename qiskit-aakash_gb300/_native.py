@@ -35,6 +35,7 @@ DM_OP_MAP1, DM_OP_MAP2, DM_OP_DIAG2, DM_OP_CX = 1, 2, 3, 4
 DM_MAP1_ROW0_IDENTITY = 1
 DM_MAP1_XY_UNITAL = 2
 DM_CX_IDEAL = 1
+DM_IMAGE_TC, DM_IMAGE_TMA = 1, 2
 DM_SCHED_GATE1, DM_SCHED_CX, DM_SCHED_MEASURE, DM_SCHED_RESET, DM_SCHED_BARRIER, DM_SCHED_OTHER = 1, 2, 3, 4, 5, 6
 
 
@@ -179,6 +180,7 @@ SIGNATURES = {
     'dm_apply_pass': (_i, [_vp, _i, _i, ctypes.POINTER(DmPass), _vp, _sz, _vp]),
     'dm_apply_pass_tc': (_i, [_vp, _i, ctypes.POINTER(DmTcPass), _vp, _sz, _vp, _vp]),
     'dm_apply_pass_tma': (_i, [_vp, _i, ctypes.POINTER(DmTcPass), _vp, _sz, _vp, _vp]),
+    'dm_compose_rounds': (_i, [_i, ctypes.POINTER(DmBatchPass), _vp, _sz, _vp, _sz, _vp]),
     'dm_max_abs_diff': (_i, [_vp, _i, _vp, _i, _i, _vp, _vp]),
     'dm_fp64_fma_probe_threads': (_i, []),
     'dm_fp64_fma_probe': (_i, [_vp, ctypes.c_int64, _vp]),

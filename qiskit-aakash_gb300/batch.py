@@ -236,52 +236,16 @@ class _Plan:
 
     def _fill(self, bp, pp, rounds, digit_orders):
         """Pass header, round axes (in ``digit_orders``) and ops of one dm_batch_pass."""
-        bp.k = len(pp.axes)
-        for r, q in enumerate(pp.axes):
-            bp.axes[r] = q
-        bp.nrounds = len(rounds)
-        if bp.nrounds > N.DM_MAX_ROUNDS:
-            raise P.TcPlanError('pass needs %d rounds (> %d)' % (len(rounds), N.DM_MAX_ROUNDS))
-        o = 0
-        for ri, ((_, rops), axes) in enumerate(zip(rounds, digit_orders)):
-            axes = list(axes)
-            for i, a in enumerate(axes):
-                bp.round_axes[ri][i] = a
-            for i in range(len(axes), 4):
-                bp.round_axes[ri][i] = -1
-            for op in rops:
-                d = bp.ops[o]
-                d.a = op.axes[0]
-                d.moff = self.mats_len
-                flags = axes.index(op.axes[0]) << 8
-                if op.kind == 'map1':
-                    d.kind = N.DM_OP_MAP1
-                    d.b = 0
-                    m = np.asarray(op.data).reshape(16)
-                    row0 = m[0] == 1.0 and not m[1:4].any()
-                    flags |= N.DM_MAP1_ROW0_IDENTITY if row0 else 0
-                    flags |= N.DM_MAP1_XY_UNITAL if (m[4] == 0.0 and m[8] == 0.0) else 0
-                    size = 16
-                elif op.kind == 'cx':
-                    d.kind = N.DM_OP_CX
-                    d.b = op.axes[1]
-                    flags |= (N.DM_CX_IDEAL if op.ideal else 0) | (axes.index(op.axes[1]) << 12)
-                    size = 5
-                elif op.kind == 'diag2':
-                    d.kind = N.DM_OP_DIAG2
-                    d.b = op.axes[1]
-                    flags |= axes.index(op.axes[1]) << 12
-                    size = 16
-                else:
-                    raise BasicAerError('batched programs hold 4x4 maps, CX and diagonal pair maps only')
-                d.flags = flags
-                self.slots.append((op.kind, list(op.src), op.ideal,
-                                   (flags & (N.DM_MAP1_ROW0_IDENTITY | N.DM_MAP1_XY_UNITAL))
-                                   if op.kind == 'map1' else 0))
-                self.mats_len += size
-                o += 1
-            bp.round_end[ri] = o
-        bp.nops = o
+        def place(op, flags, size):
+            if op.kind not in ('map1', 'cx', 'diag2'):
+                raise BasicAerError('batched programs hold 4x4 maps, CX and diagonal pair maps only')
+            self.slots.append((op.kind, list(op.src), op.ideal,
+                               (flags & (N.DM_MAP1_ROW0_IDENTITY | N.DM_MAP1_XY_UNITAL))
+                               if op.kind == 'map1' else 0))
+            self.mats_len += size
+            return self.mats_len - size
+
+        P.fill_round_ops(bp, pp, rounds, digit_orders, place)
 
     def table_bytes(self):
         return bytes((N.DmBatchPass * len(self.passes))(*self.passes))

@@ -4,8 +4,8 @@
 // coefficients is streamed into shared memory (cp.async, 16-byte chunks),
 // then the pass's register rounds run as matrix products on the tensor
 // cores.  A round names 3 of the tile's axes; the round's operations,
-// composed in FP64 (on the host, or per instance on the device for the
-// batched sweeps), form one 64x64 real transfer matrix U acting
+// composed in FP64 on the device (compose_pass_kernel before the pass, or
+// per instance inside the batched sweeps), form one 64x64 real transfer matrix U acting
 // on the 64 coefficients that differ only in those axes.  With the tile
 // viewed as 256 groups x 64 (one row per group), the round is
 //     D[g][j'] = sum_j X[g][j] * U[j'][j]           (M = 256, N = 64, K = 64)
@@ -366,6 +366,8 @@ __device__ void batch_tc_setup(Pass &ps, const dm_batch_tc_pass &bp, int n) {
 // One operation on a 64-coefficient column in shared memory (index j = d0 +
 // 4 d1 + 16 d2 over the round's digits; digit positions from the op flags),
 // in FP64: the same maps as the register rounds, with runtime digits.
+// Map2: 16x16 general maps too (the single-state passes; the batched plans hold none).
+template <bool Map2>
 __device__ void col_apply(double *col, const dm_op &op, const double *__restrict__ mats) {
     const double *mg = mats + op.moff;
     const int da = (op.flags >> 8) & 3, db = (op.flags >> 12) & 3;
@@ -396,6 +398,16 @@ __device__ void col_apply(double *col, const dm_op &op, const double *__restrict
         double x[16];
 #pragma unroll
         for (int i = 0; i < 16; ++i) x[i] = col[j0 + (i >> 2) * SA + (i & 3) * SB];
+        if (Map2 && op.kind == DM_OP_MAP2) {   // y[4 pa + pb] = sum_s mg[16 (4 pa + pb) + s] x[s]
+#pragma unroll 1
+            for (int i = 0; i < 16; ++i) {
+                double acc = 0.0;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) acc = fma(mg[16 * i + j], x[j], acc);
+                col[j0 + (i >> 2) * SA + (i & 3) * SB] = acc;
+            }
+            continue;
+        }
         if (op.kind == DM_OP_CX) {
             cx16(x, cx, ideal);
         } else {   // DM_OP_DIAG2: entry (pa, pb) scaled by mg[4 pa + pb]
@@ -409,14 +421,40 @@ __device__ void col_apply(double *col, const dm_op &op, const double *__restrict
 
 // Round r's matrix U (64 x 64 in its K-digit order) is the round's operations
 // applied to the 64 unit vectors: column k of U = ops(e_k), composed in FP64
-// on a column held in shared memory (one thread per column, two rounds at a
-// time; the pass's operand and matrix regions are free between passes).
-// Written as the three FP16 images the MMAs read (2**11 Uh,
-// Ul = fp16(2**11 (U - Uh)), Uh; value (n%8)*8 + k%8 + (k/8)*64 + (n/8)*512
-// for output n, input k).
+// on a column held in shared memory, one thread per column.  Written as FP16
+// images that the MMAs read, K-major (value (n%8)*8 + k%8 + (k/8)*64 +
+// (n/8)*512 for output n, input k), with Uh = fp16(U) and
+// Ul = fp16(2**11 (U - Uh)): three images 2**11 Uh | Ul | Uh for the
+// cp.async-fed kernels, two images Uh | Ul for the TMA-fed one.
 constexpr int kColStride = 65;   // doubles per column: a warp's 32 columns spread over the banks
 static_assert(2 * 64 * kColStride * 8 <= int(kSmemBytes), "two rounds of FP64 columns fit the pass's shared memory");
 
+template <bool Map2>
+__device__ void compose_column(const dm_batch_pass &bp, int r, int k, const double *__restrict__ mats, double *col) {
+#pragma unroll 1
+    for (int j = 0; j < 64; ++j) col[j] = j == k ? 1.0 : 0.0;
+    const int ob = r > 0 ? bp.round_end[r - 1] : 0, oe = bp.round_end[r];
+    for (int o = ob; o < oe; ++o) col_apply<Map2>(col, bp.ops[o], mats);
+}
+
+__device__ void write_column(uint16_t *__restrict__ img, int k, const double *col, bool three) {
+    const uint32_t kpos = uint32_t(k & 7) + uint32_t(k >> 3) * 64;
+    const int uh = three ? 8192 : 0;   // three: 2**11 Uh at 0, Ul at 4096, Uh at 8192; two: Uh at 0, Ul at 4096
+#pragma unroll 4
+    for (int j = 0; j < 64; ++j) {
+        const uint32_t pos = kpos + uint32_t(j & 7) * 8 + uint32_t(j >> 3) * 512;
+        const double u = col[j];
+        const __half h = __double2half(u);
+        const double hd = double(__half2float(h));
+        if (three) img[pos] = __half_as_ushort(__float2half_rn(float(hd * double(kLoScale))));
+        img[4096 + pos] = __half_as_ushort(__double2half((u - hd) * double(kLoScale)));
+        img[uh + pos] = __half_as_ushort(h);
+    }
+}
+
+// All rounds of a batched pass into per-CTA scratch (three images per round),
+// 128 threads, two rounds at a time; the pass's operand and matrix regions
+// are free between passes.
 __device__ void compose_rounds(const dm_batch_pass &bp, const double *__restrict__ mats, uint16_t *__restrict__ umats,
                                double *work) {
     const int nr = bp.nrounds;
@@ -426,23 +464,21 @@ __device__ void compose_rounds(const dm_batch_pass &bp, const double *__restrict
     for (int r0 = 0; r0 < nr; r0 += 2) {
         const int r = r0 + (tid >> 6), k = tid & 63;
         if (r >= nr) break;
-#pragma unroll 1
-        for (int j = 0; j < 64; ++j) col[j] = j == k ? 1.0 : 0.0;
-        const int ob = r > 0 ? bp.round_end[r - 1] : 0, oe = bp.round_end[r];
-        for (int o = ob; o < oe; ++o) col_apply(col, bp.ops[o], mats);
-        uint16_t *img = umats + int64_t(r) * kUHalves;
-        const uint32_t kpos = uint32_t(k & 7) + uint32_t(k >> 3) * 64;
-#pragma unroll 4
-        for (int j = 0; j < 64; ++j) {
-            const uint32_t pos = kpos + uint32_t(j & 7) * 8 + uint32_t(j >> 3) * 512;
-            const double u = col[j];
-            const __half h = __double2half(u);
-            const double hd = double(__half2float(h));
-            img[pos] = __half_as_ushort(__float2half_rn(float(hd * double(kLoScale))));
-            img[4096 + pos] = __half_as_ushort(__double2half((u - hd) * double(kLoScale)));
-            img[8192 + pos] = __half_as_ushort(h);
-        }
+        compose_column<false>(bp, r, k, mats, col);
+        write_column(umats + int64_t(r) * kUHalves, k, col, true);
     }
+}
+
+// One pass's round images for the single-state kernels: one CTA per round,
+// one thread per column.
+__global__ void __launch_bounds__(64)
+    compose_pass_kernel(const __grid_constant__ dm_batch_pass bp, const double *__restrict__ mats,
+                        uint16_t *__restrict__ images, int image_halves) {
+    __shared__ double cols[64 * kColStride];
+    const int r = blockIdx.x, k = threadIdx.x;
+    double *col = cols + k * kColStride;
+    compose_column<true>(bp, r, k, mats, col);
+    write_column(images + int64_t(r) * image_halves, k, col, image_halves == kUHalves);
 }
 
 __global__ void __launch_bounds__(kThreads, kCtasPerSm)
@@ -636,26 +672,21 @@ extern "C" size_t dm_batch_tc_scratch_bytes(void) {
     return size_t(sm_count()) * tc::kCtasPerSm * size_t(tc::kScratchHalves) * sizeof(uint16_t);
 }
 
-// One tensor-core batched pass against an instance of n qubits with a coefficient block of mats_len values.
-static int validate_batch_tc_pass(const dm_batch_tc_pass &bp, int n, int64_t mats_len) {
-    const dm_batch_pass &o = bp.ops;
-    if (o.k != tc::kAxes || o.nrounds < 1 || o.nrounds > DM_MAX_ROUNDS) return DM_ERR_PROGRAM;
+// The rounds and operations of a tensor-core pass (round_axes[r][0..2] the
+// round's local axes in K-digit order, each op on axes of its round, digit
+// positions in its flags, coefficients inside mats_len values); 16x16
+// general maps only where the caller composes them.
+static int validate_round_ops(const dm_batch_pass &o, int64_t mats_len, bool map2) {
+    if (o.nrounds < 1 || o.nrounds > DM_MAX_ROUNDS) return DM_ERR_PROGRAM;
     if (o.nops < 0 || o.nops > DM_MAX_PASS_OPS) return DM_ERR_PROGRAM;
-    if (o.axes[0] != n - 1) return DM_ERR_PROGRAM;   // 16-byte chunks need the lowest axis resident
-    for (int r = 0; r < tc::kAxes; ++r)
-        if (o.axes[r] < 0 || o.axes[r] >= n || (r > 0 && o.axes[r] >= o.axes[r - 1])) return DM_ERR_PROGRAM;
-    const int vec0 = bp.tables.vec0 == 0 ? 0 : -1;
-    if (!valid_tables(bp.tables.natrow, bp.tables.natk, vec0, true)) return DM_ERR_PROGRAM;
     int prev_end = 0;
     for (int r = 0; r < o.nrounds; ++r) {
-        const dm_tc_round &tr = bp.tables.rounds[r];
         for (int i = 0; i < 3; ++i) {
             const int a = o.round_axes[r][i];
-            if (a < 0 || a >= tc::kAxes || tr.digits[i] != a) return DM_ERR_PROGRAM;
+            if (a < 0 || a >= tc::kAxes) return DM_ERR_PROGRAM;
             for (int j = 0; j < i; ++j)
                 if (o.round_axes[r][j] == a) return DM_ERR_PROGRAM;
         }
-        if (!valid_tables(tr.rowc, tr.kc, tr.vec, r + 1 == o.nrounds)) return DM_ERR_PROGRAM;
         const int end = o.round_end[r];
         if (end < prev_end || end > o.nops) return DM_ERR_PROGRAM;
         for (int i = prev_end; i < end; ++i) {
@@ -665,6 +696,10 @@ static int validate_batch_tc_pass(const dm_batch_tc_pass &bp, int n, int64_t mat
                 case DM_OP_MAP1: need = 16; break;
                 case DM_OP_DIAG2: need = 16; break;
                 case DM_OP_CX: need = 5; break;
+                case DM_OP_MAP2:
+                    if (!map2) return DM_ERR_PROGRAM;
+                    need = 256;
+                    break;
                 default: return DM_ERR_PROGRAM;
             }
             if (op.moff < 0 || op.moff + need > mats_len) return DM_ERR_PROGRAM;
@@ -677,6 +712,38 @@ static int validate_batch_tc_pass(const dm_batch_tc_pass &bp, int n, int64_t mat
         prev_end = end;
     }
     return prev_end == o.nops ? DM_OK : DM_ERR_PROGRAM;
+}
+
+// One tensor-core batched pass against an instance of n qubits with a coefficient block of mats_len values.
+static int validate_batch_tc_pass(const dm_batch_tc_pass &bp, int n, int64_t mats_len) {
+    const dm_batch_pass &o = bp.ops;
+    if (o.k != tc::kAxes || o.nrounds < 1 || o.nrounds > DM_MAX_ROUNDS) return DM_ERR_PROGRAM;
+    if (o.axes[0] != n - 1) return DM_ERR_PROGRAM;   // 16-byte chunks need the lowest axis resident
+    for (int r = 0; r < tc::kAxes; ++r)
+        if (o.axes[r] < 0 || o.axes[r] >= n || (r > 0 && o.axes[r] >= o.axes[r - 1])) return DM_ERR_PROGRAM;
+    const int vec0 = bp.tables.vec0 == 0 ? 0 : -1;
+    if (!valid_tables(bp.tables.natrow, bp.tables.natk, vec0, true)) return DM_ERR_PROGRAM;
+    for (int r = 0; r < o.nrounds; ++r) {
+        const dm_tc_round &tr = bp.tables.rounds[r];
+        for (int i = 0; i < 3; ++i)
+            if (tr.digits[i] != o.round_axes[r][i]) return DM_ERR_PROGRAM;
+        if (!valid_tables(tr.rowc, tr.kc, tr.vec, r + 1 == o.nrounds)) return DM_ERR_PROGRAM;
+    }
+    return validate_round_ops(o, mats_len, false);
+}
+
+extern "C" int dm_compose_rounds(int format, const dm_batch_pass *pass, const double *mats_dev, size_t mats_count,
+                                 uint16_t *images_dev, size_t images_count, void *stream) {
+    DM_CHECK_ARG(pass && mats_dev && images_dev && (format == DM_IMAGE_TC || format == DM_IMAGE_TMA));
+    if (reinterpret_cast<uintptr_t>(images_dev) & 15 || reinterpret_cast<uintptr_t>(mats_dev) & 7) return DM_ERR_ARG;
+    if (mats_count > size_t(INT32_MAX)) return DM_ERR_RANGE;
+    const int rc = validate_round_ops(*pass, int64_t(mats_count), true);
+    if (rc) return rc;
+    const int halves = format == DM_IMAGE_TC ? tc::kUHalves : 2 * 4096;
+    if (images_count < size_t(pass->nrounds) * size_t(halves)) return DM_ERR_ARG;
+    tc::compose_pass_kernel<<<pass->nrounds, 64, 0, as_stream(stream)>>>(*pass, mats_dev, images_dev, halves);
+    count_launch();
+    return launch_status();
 }
 
 extern "C" int dm_batch_run_tc(float *states_dev, size_t states_count, double *probs_dev, size_t probs_count,

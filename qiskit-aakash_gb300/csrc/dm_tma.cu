@@ -14,15 +14,19 @@
 // * one persistent CTA per SM with two teams of 256 threads; each team owns
 //   one 64 KB tile slot and 256 TMEM columns and streams its own tiles, so
 //   one team's MMAs, loads and stores overlap the other team's epilogues;
-// * tiles move by TMA (cp.async.bulk.tensor): one thread of the team issues
-//   the load of its next tile (completing on an mbarrier) as soon as the TMA
-//   store of its current tile has read the slot, and the store is
-//   asynchronous (bulk group); no thread computes a global address;
+// * tiles arrive by TMA (cp.async.bulk.tensor, completing on an mbarrier):
+//   one thread of the team issues the load of its next tile as soon as the
+//   last round's MMAs have read the slot, so the load overlaps the last
+//   round's epilogue; that epilogue writes each thread's row straight to
+//   global memory (lanes 0-15 on 16 contiguous coefficients);
 // * the pass's round images ([Uh ; Ul], 16 KB per round) are loaded once per
 //   CTA by bulk copies and stay in shared memory for the whole pass when it
 //   has up to kUSlots rounds; a longer pass keeps its first kStreamFrom rounds
 //   resident and streams each later round's image, per team, into one spare
 //   slot (loaded as soon as the previous round's MMAs have read that slot).
+// (An L2 prefetch of the next tile by cp.async.bulk.prefetch.tensor, tried in
+// several forms, made the step slower: its issue holds the issuing thread,
+// and with it the team, for thousands of cycles.)
 //
 // Tensor map.  The state is a 4**n vector whose flat index is the base-4
 // number of the qubits' Pauli labels (qubit n-1 the lowest digit).  The 7
@@ -39,10 +43,10 @@
 // a multiple of 4 elements (16 bytes), as TMA requires.
 //
 // Shared memory (dynamic, 1024-byte aligned): slot 0 | slot 1 (64 KB each:
-// AH | AL, 32 KB per FP16 operand image; the natural FP32 tile on load and
-// store) | round images (16 KB per round).  Every mbarrier wait is bounded in
-// time; a wait that gives up sets *status, the team stops, drains what it has
-// in flight (MMA, tile load, tile store) and the kernel returns.
+// AH | AL, 32 KB per FP16 operand image; the natural FP32 tile on load) |
+// round images (16 KB per round).  Every mbarrier wait is bounded in time; a
+// wait that gives up sets *status, the team stops, drains what it has in
+// flight (MMA, tile load, round image) and the kernel returns.
 #include <cuda.h>
 #include <cuda_fp16.h>
 
@@ -78,8 +82,6 @@ struct TmaPass {
     int nrounds, ndims;
     int nres;                        // rounds whose images stay resident (all of them, or kStreamFrom)
     int last_vec;                    // the last round's K digit 0 is local axis 0: 16-byte stores
-    int group_prefetch;              // pmap's box spans the 4 tiles of the lowest non-resident digit
-    int group_half;                  // coordinate step of its second half (outermost dimension)
     float up, down;                  // 2**n, 2**-n
     int64_t ntiles;
     int8_t gap_first[kMaxDims];      // tile-index digit of the first non-resident digit above dimension i
@@ -106,32 +108,6 @@ __device__ __forceinline__ int64_t tile_base(const TmaPass &p, const int (&c)[kM
 #pragma unroll
     for (int i = 0; i < kMaxDims; ++i) b += int64_t(c[i]) << (2 * p.start[i]);
     return b;
-}
-
-// TMA prefetch of tile coordinates c into L2 (no shared memory, no completion).
-__device__ __forceinline__ void tma_prefetch_l2(const CUtensorMap *map, int nd, const int (&c)[kMaxDims]) {
-    const uint64_t m = reinterpret_cast<uint64_t>(map);
-    switch (nd) {
-    case 1:
-        asm volatile("cp.async.bulk.prefetch.tensor.1d.L2.global [%0, {%1}];" ::"l"(m), "r"(c[0]) : "memory");
-        break;
-    case 2:
-        asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global [%0, {%1, %2}];" ::"l"(m), "r"(c[0]), "r"(c[1])
-                     : "memory");
-        break;
-    case 3:
-        asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global [%0, {%1, %2, %3}];" ::"l"(m), "r"(c[0]),
-                     "r"(c[1]), "r"(c[2]) : "memory");
-        break;
-    case 4:
-        asm volatile("cp.async.bulk.prefetch.tensor.4d.L2.global [%0, {%1, %2, %3, %4}];" ::"l"(m), "r"(c[0]),
-                     "r"(c[1]), "r"(c[2]), "r"(c[3]) : "memory");
-        break;
-    default:
-        asm volatile("cp.async.bulk.prefetch.tensor.5d.L2.global [%0, {%1, %2, %3, %4, %5}];" ::"l"(m), "r"(c[0]),
-                     "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]) : "memory");
-        break;
-    }
 }
 
 // TMA tile load of tile coordinates c into shared memory at dst, completing on mbar.
@@ -182,7 +158,7 @@ __device__ __forceinline__ bool team_and(bool ok, int team) {
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
-    pass_tma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap pmap,
+    pass_tma_kernel(const __grid_constant__ CUtensorMap tmap,
                     const __grid_constant__ TmaPass p,
                     float *__restrict__ st, const uint16_t *__restrict__ umats, int *status) {
     extern __shared__ unsigned char smem_raw[];
@@ -263,23 +239,6 @@ __global__ void __launch_bounds__(kThreads, 1)
         load_pending = false;
         const int64_t tn = t + stride;
         if (leader && p.nrounds > p.nres) stream_u(p.nres);   // the slot is free: the last round's MMAs are done
-        if (leader && tn < p.ntiles) {
-            // the team's next tile heads for L2 while this one runs; with a group box, the team holding
-            // the first of the four tiles that differ only in the lowest non-resident digit (adjacent
-            // in memory, run by this CTA and the next at the same time) prefetches all four at once,
-            // so DRAM sees runs of four times the tile's contiguous rows
-            int c[kMaxDims];
-            tile_coords(p, tn, c);
-            if (!p.group_prefetch) {
-                tma_prefetch_l2(&tmap, p.ndims, c);
-            } else if ((tn & 3) == 0) {     // the group in two halves of its outermost dimension
-                tma_prefetch_l2(&pmap, p.ndims, c);
-                int c2[kMaxDims];
-#pragma unroll
-                for (int i = 0; i < kMaxDims; ++i) c2[i] = c[i] + (i == p.ndims - 1 ? p.group_half : 0);
-                tma_prefetch_l2(&pmap, p.ndims, c2);
-            }
-        }
         // ---- natural tile -> round 0's operand (h / l), in place: one operand row per thread ----
         // lanes hold rows 0-4, whose tile bits 0-3 are the 16 contiguous coefficients of the tile:
         // the word loads of a warp hit distinct banks, the 16-byte chunk stores whole core matrices
@@ -571,38 +530,17 @@ extern "C" int dm_apply_pass_tma(void *state_dev, int n, const dm_tc_pass *pass,
     EncodeTiled enc = encode_fn();
     if (!enc) return DM_ERR_CUDA;
     for (int i = 0; i < tma::kMaxDims; ++i) estride[i] = 1;
-    CUtensorMap map, pmap;
+    CUtensorMap map;
     if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, cuuint32_t(p.ndims), state_dev, gdim, gstride, box, estride,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return DM_ERR_CUDA;
-    // group prefetch box: dimension 0 widened over the lowest non-resident digit (tile-index digit 0),
-    // when that digit sits directly above dimension 0 and the widened row stays within 256 elements;
-    // the team stride must keep tile-index digit 0 per team (a multiple of 4 teams per iteration)
     const int64_t grid = std::min<int64_t>(sm_count(), (p.ntiles + tma::kTeams - 1) / tma::kTeams);
-    // (the driver takes boxes of at most 128 KB, so the four tiles go in two halves of the outermost
-    // dimension)
-    p.group_prefetch = p.gap_len[0] >= 1 && p.box_log4[0] <= 3 && p.ntiles >= 4 && p.ndims >= 2 &&
-                       (grid * tma::kTeams) % 4 == 0;
-    pmap = map;
-    if (p.group_prefetch) {
-        cuuint32_t pbox[tma::kMaxDims];
-        for (int i = 0; i < tma::kMaxDims; ++i) pbox[i] = box[i];
-        pbox[0] = box[0] * 4;
-        pbox[p.ndims - 1] = box[p.ndims - 1] / 2;
-        p.group_half = int(pbox[p.ndims - 1]);
-        if (enc(&pmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, cuuint32_t(p.ndims), state_dev, gdim, gstride, pbox,
-                estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
-            p.group_prefetch = 0;   // the driver refuses the wider box: prefetch tile by tile
-            pmap = map;
-        }
-    }
     if (ensure_max_dynamic_smem(reinterpret_cast<const void *>(tma::pass_tma_kernel), int(tma::kSmemBytes)) !=
         cudaSuccess)
         return DM_ERR_CUDA;
     tma::pass_tma_kernel<<<int(grid), tma::kThreads, tma::kSmemBytes, as_stream(stream)>>>(
-        map, pmap, p, static_cast<float *>(state_dev), umats_dev, status_dev);
+        map, p, static_cast<float *>(state_dev), umats_dev, status_dev);
     count_launch();
     return launch_status();
 }

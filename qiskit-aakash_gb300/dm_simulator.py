@@ -32,7 +32,10 @@ default and the parity form, or 'single'), ``fusion`` (fused tile passes,
 default True), ``tile_axes`` (resident axes per tile), ``register_rounds``
 (apply a pass's operations in register rounds, default True), ``tensor_cores``
 (FP32 passes on tcgen05 as 64x64 transfer matrices in a 3-way FP16 split, default True), ``tma``
-(tensor-core passes with TMA-fed tiles where a pass fits them, default True) and
+(tensor-core passes with TMA-fed tiles where a pass fits them, default True),
+``compose`` ('device', the default: each tensor-core round's 64x64 matrix is
+composed in FP64 on the GPU from the operations' coefficients; 'host': in
+numpy, with the FP16 images uploaded) and
 ``coefficients_to_host`` (default True; False leaves ``coeffmatrix`` /
 ``densitymatrix`` out of the result, for callers that only need the
 measurement data of a large register) and ``counts_shots`` / ``counts_seed``
@@ -242,6 +245,7 @@ class DmSimulatorGPU(_Base):
         self._register_rounds = True
         self._tensor_cores = True
         self._tma = True
+        self._compose = 'device'
         self._fp64_check = False
         self.last_run_stats = {}
         self._record_next = False
@@ -364,6 +368,10 @@ class DmSimulatorGPU(_Base):
             self._tensor_cores = bool(backend_options['tensor_cores'])
         if 'tma' in backend_options:
             self._tma = bool(backend_options['tma'])
+        if 'compose' in backend_options:
+            if backend_options['compose'] not in ('device', 'host'):
+                raise BasicAerError("compose must be 'device' or 'host'")
+            self._compose = backend_options['compose']
         if 'register_rounds' in backend_options:
             self._register_rounds = bool(backend_options['register_rounds'])
         if 'coefficients_to_host' in backend_options:
@@ -613,7 +621,8 @@ class DmSimulatorGPU(_Base):
             raise BasicAerError('dm_simulator does not support conditional (bfunc) operations')
         self._dev = self._state_factory(n, precision=self._precision, fusion=self._fusion,
                                         tile_axes=self._tile_axes, rounds=self._register_rounds,
-                                        tensor_cores=self._tensor_cores, tma=self._tma)
+                                        tensor_cores=self._tensor_cores, tma=self._tma,
+                                        compose=self._compose)
         if self._record_next:
             self._dev.record()
         launches0 = N.lib().dm_kernel_launch_count()
@@ -750,7 +759,9 @@ class DmSimulatorGPU(_Base):
         self.last_run_stats = {'passes': self._dev.passes_run, 'levels': levels,
                                'kernel_launches': N.lib().dm_kernel_launch_count() - launches0,
                                'h2d_bytes': self._dev.h2d_bytes, 'd2h_bytes': self._dev.d2h_bytes,
-                               'copy_out': dict(getattr(self._dev, 'copy_stats', {}))}
+                               'copy_out': dict(getattr(self._dev, 'copy_stats', {})),
+                               'passes_by_kernel': dict(getattr(self._dev, 'passes_by_kernel', {})),
+                               'composed_on': dict(getattr(self._dev, 'composed_on', {}))}
         if self._record_next:
             self.recorded_state = self._dev
             self._record_next = False

@@ -14,7 +14,8 @@ import numpy as np
 
 from . import _native as N
 from .exceptions import BasicAerError
-from .program import (TC_AXES, Op, TcPlanError, cx_coefficients, encode_pass, encode_pass_tc, encode_pass_tma,
+from .program import (TC_AXES, Op, OpTableError, TcPlanError, cx_coefficients, encode_pass, encode_pass_tc,
+                      encode_pass_tc_ops, encode_pass_tma,
                       plan_passes)
 
 # Tile sizes of the fused pass: 4**6 FP64 = 32 KB and 4**7 FP32 = 64 KB of
@@ -156,7 +157,7 @@ class DeviceState:
     """An n-qubit Pauli-coefficient vector on a CUDA device."""
 
     def __init__(self, n, precision='double', fusion=True, tile_axes=None, low_axes=DEFAULT_LOW_AXES,
-                 device=None, rounds=True, tensor_cores=True, tma=True):
+                 device=None, rounds=True, tensor_cores=True, tma=True, compose='device'):
         torch = _torch()
         if not torch.cuda.is_available():
             raise BasicAerError('dm_simulator (GB300) needs a CUDA device; none is visible')
@@ -177,7 +178,14 @@ class DeviceState:
         # FP32 passes of 7 resident axes run on the tensor cores (3-way FP16 split)
         self.tensor_cores = bool(tensor_cores) and precision == 'single' and n >= TC_AXES
         self.tma = bool(tma)      # TMA-fed tensor-core passes where a pass fits them
+        if compose not in ('device', 'host'):
+            raise BasicAerError("compose must be 'device' or 'host'")
+        # where the tensor-core rounds' 64x64 matrices are composed in FP64:
+        # 'device' (dm_compose_rounds from the ops' coefficients) or 'host' (numpy, FP16 images uploaded)
+        self.compose = compose
         self.passes_by_kernel = {'tma': 0, 'tc': 0, 'cuda_cores': 0}
+        self.composed_on = {'device': 0, 'host': 0}
+        self._images = None       # device round images of the pass in flight (DM_MAX_ROUNDS x 12288 FP16)
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device) if self.tensor_cores else None
         self.kmax = min(tile_axes or DEFAULT_TILE_AXES[precision], N.DM_MAX_TILE_AXES)
         self.low = low_axes
@@ -292,25 +300,46 @@ class DeviceState:
             self._run_passes(passes)
 
     def _encode_tc(self, p):
-        """(entry point, descriptor, FP16 images) of a pass on the tensor cores, or None.
+        """(entry point, descriptor, ops table or None, coefficients or FP16 images) of a tensor-core pass, or None.
 
-        The TMA-fed kernel takes passes of up to 6 rounds whose resident axes
+        The TMA-fed kernel takes passes of up to 16 rounds whose resident axes
         fit a 5-dimensional tensor map; other passes run on the cp.async-fed
-        kernel; a pass with more rounds than a descriptor holds, on neither."""
-        if self.tma:
+        kernel; a pass with more rounds than a descriptor holds, on neither.
+        With compose='device' the round matrices are composed by
+        dm_compose_rounds from the ops' FP64 coefficients; a pass with more
+        ops than its table holds is composed on the host."""
+        kernels = (('tma', 'dm_apply_pass_tma', encode_pass_tma),) if self.tma else ()
+        kernels += (('tc', 'dm_apply_pass_tc', encode_pass_tc),)
+        for kernel, name, host_encoder in kernels:
+            if self.compose == 'device':
+                coefs = []
+                try:
+                    d, bp = encode_pass_tc_ops(p, self.n, coefs, kernel)
+                    return name, d, bp, coefs
+                except OpTableError:
+                    pass
+                except TcPlanError:
+                    continue
             umats = []
             try:
-                return 'dm_apply_pass_tma', encode_pass_tma(p, self.n, umats), umats
+                return name, host_encoder(p, self.n, umats), None, umats
             except TcPlanError:
-                pass
-        umats = []
-        try:
-            return 'dm_apply_pass_tc', encode_pass_tc(p, self.n, umats), umats
-        except TcPlanError:
-            return None
+                continue
+        return None
+
+    def _image_buffer(self):
+        if self._images is None:
+            torch = _torch()
+            self._images = torch.empty(N.DM_MAX_ROUNDS * 3 * 4096, dtype=torch.int16, device=self.device)
+        return self._images
 
     def _run_passes_tc(self, passes):
-        """Encode and launch pass by pass: the host plans pass i+1 while the GPU runs pass i."""
+        """Encode and launch pass by pass: the host plans pass i+1 while the GPU runs pass i.
+
+        Device composition: the ops' coefficients go up (a few KB), one
+        dm_compose_rounds launch writes the round images into one device
+        buffer, and the pass reads them; the stream orders each pass's
+        composition after the previous pass's reads."""
         torch = _torch()
         sp = ctypes.c_void_p(self.status.data_ptr())
         keep = []
@@ -320,14 +349,29 @@ class DeviceState:
                 self._run_passes([p])     # more rounds than a descriptor holds: the CUDA-core pass
                 self.passes_by_kernel['cuda_cores'] += 1
                 continue
-            name, d, umats = enc
+            name, d, bp, data = enc
             self.passes_by_kernel['tma' if name == 'dm_apply_pass_tma' else 'tc'] += 1
-            host = np.concatenate(umats).view(np.int16)      # FP16 bit patterns
+            if bp is not None:
+                host = np.concatenate(data) if data else np.zeros(1)
+                h = torch.from_numpy(host).pin_memory()
+                dev = h.to(self.device, non_blocking=True)
+                self.h2d_bytes += host.nbytes
+                img = self._image_buffer()
+                fmt = N.DM_IMAGE_TMA if name == 'dm_apply_pass_tma' else N.DM_IMAGE_TC
+                ip, isz = ctypes.c_void_p(img.data_ptr()), ctypes.c_size_t(img.numel())
+                self._call('dm_compose_rounds', fmt, ctypes.byref(bp), ctypes.c_void_p(dev.data_ptr()),
+                           ctypes.c_size_t(host.size), ip, isz, self.stream, keep=(bp, dev))
+                self._call(name, self.ptr, self.n, ctypes.byref(d), ip, isz, sp, self.stream, keep=(d,))
+                self.composed_on['device'] += 1
+                keep.append((h, dev, d, bp))
+                continue
+            host = np.concatenate(data).view(np.int16)      # FP16 bit patterns
             h = torch.from_numpy(host).pin_memory()
             dev = h.to(self.device, non_blocking=True)
             self.h2d_bytes += host.nbytes
             self._call(name, self.ptr, self.n, ctypes.byref(d), ctypes.c_void_p(dev.data_ptr()),
                        ctypes.c_size_t(host.size), sp, self.stream, keep=(d, dev))
+            self.composed_on['host'] += 1
             keep.append((h, dev, d))
         self.passes_run += len(keep)
         self._keep = keep

@@ -377,6 +377,10 @@ TC_AXES = 7   # resident axes of a tensor-core pass (tiles of 4**7 FP32 coeffici
 class TcPlanError(RuntimeError):
     """A pass that does not fit a tensor-core descriptor (more rounds than DM_MAX_ROUNDS)."""
 
+
+class OpTableError(TcPlanError):
+    """A tensor-core pass with more ops than a DmBatchPass holds (its rounds fit; the host composes them)."""
+
 # digits (d0, d1, d2) of the 64 round indices j = d0 + 4 d1 + 16 d2
 _J = np.arange(64)
 _DIG = np.stack([_J & 3, (_J >> 2) & 3, _J >> 4])
@@ -813,8 +817,8 @@ def epilogue_wavefronts(src, dst, natural=False):
     return total
 
 
-def plan_tc_pass(p, n, nat='xor'):
-    """Pad a pass to 7 axes, plan its rounds and their layouts, compose each round's U (FP64).
+def plan_tc_rounds(p, n, nat='xor'):
+    """Pad a pass to 7 axes, plan its rounds and their layouts: (pass, [(axes, ops)], layouts).
 
     nat='tma' plans for the TMA-fed kernel (first and last rounds with local
     axes 0 and 1 on rows 0-3 where they are not among the round's axes)."""
@@ -824,13 +828,81 @@ def plan_tc_pass(p, n, nat='xor'):
         layouts = list(_choose_layouts_tma_cached(tuple(tuple(sorted(a)) for a, _ in rounds)))
     else:
         layouts = _choose_layouts([axes for axes, _ in rounds], nat)
+    return pp, rounds, layouts
+
+
+def compose_round_matrices(rounds, layouts):
+    """Each round's 64x64 U in its layout's digit order, composed in FP64 with numpy.
+
+    The host statement of what dm_compose_rounds computes on the device."""
     mats = []
     for (axes, rops), lay in zip(rounds, layouts):
         U = np.eye(64)
         for op in rops:
             U = op_matrix64(op, lay.digits) @ U
         mats.append(U)
-    return pp, layouts, mats
+    return mats
+
+
+def plan_tc_pass(p, n, nat='xor'):
+    """plan_tc_rounds with each round's U composed on the host: (pass, layouts, [U])."""
+    pp, rounds, layouts = plan_tc_rounds(p, n, nat)
+    return pp, layouts, compose_round_matrices(rounds, layouts)
+
+
+_ROUND_OP_KINDS = {'map1': (1, 16), 'cx': (4, 5), 'diag2': (3, 16), 'map2': (2, 256)}
+
+
+def fill_round_ops(bp, pp, rounds, digit_orders, place):
+    """Pass header, round axes (in ``digit_orders``) and ops of a DmBatchPass.
+
+    ``place(op, flags, size)`` returns the op's coefficient offset (moff)
+    after recording or storing its ``size`` coefficients.  The digit
+    position of each op axis within its round goes into the flags (bits 8
+    and 12), as the register rounds and the device composition read them."""
+    bp.k = len(pp.axes)
+    for r, q in enumerate(pp.axes):
+        bp.axes[r] = q
+    if len(rounds) > N.DM_MAX_ROUNDS:
+        raise TcPlanError('pass needs %d rounds (> %d)' % (len(rounds), N.DM_MAX_ROUNDS))
+    if sum(len(rops) for _, rops in rounds) > N.DM_MAX_PASS_OPS:
+        raise OpTableError('pass holds more than %d ops' % N.DM_MAX_PASS_OPS)
+    bp.nrounds = len(rounds)
+    o = 0
+    for ri, ((_, rops), axes) in enumerate(zip(rounds, digit_orders)):
+        axes = list(axes)
+        for i, a in enumerate(axes):
+            bp.round_axes[ri][i] = a
+        for i in range(len(axes), 4):
+            bp.round_axes[ri][i] = -1
+        for op in rops:
+            if op.kind not in _ROUND_OP_KINDS:
+                raise ValueError(op.kind)
+            kind, size = _ROUND_OP_KINDS[op.kind]
+            d = bp.ops[o]
+            d.kind = kind
+            d.a = op.axes[0]
+            flags = axes.index(op.axes[0]) << 8
+            if op.kind == 'map1':
+                d.b = 0
+                m = np.asarray(op.data).reshape(16)
+                flags |= N.DM_MAP1_ROW0_IDENTITY if (m[0] == 1.0 and not m[1:4].any()) else 0
+                flags |= N.DM_MAP1_XY_UNITAL if (m[4] == 0.0 and m[8] == 0.0) else 0
+            else:
+                d.b = op.axes[1]
+                flags |= axes.index(op.axes[1]) << 12
+                if op.kind == 'cx' and op.ideal:
+                    flags |= N.DM_CX_IDEAL
+            d.flags = flags
+            d.moff = place(op, flags, size)
+            o += 1
+        bp.round_end[ri] = o
+    bp.nops = o
+
+
+def round_op_coefficients(op):
+    """The FP64 coefficients of one op as a dm_op reads them (16, 5, 16 or 256 values)."""
+    return np.ascontiguousarray(op.data, dtype=np.float64).reshape(-1)
 
 
 def tc_tables(layouts, nat='xor'):
@@ -854,7 +926,8 @@ def tc_tables(layouts, nat='xor'):
     return conv, rounds
 
 
-def _encode_tc(pp, layouts, mats, nat, image, umats):
+def _encode_tc(pp, layouts, nat, umoff0, halves):
+    """DmTcPass tables of a planned pass; round r reads its image at umoff0 + r * halves."""
     if len(layouts) > N.DM_MAX_ROUNDS:
         raise TcPlanError('pass needs %d rounds (> %d)' % (len(layouts), N.DM_MAX_ROUNDS))
     conv, rounds = tc_tables(layouts, nat)
@@ -867,8 +940,7 @@ def _encode_tc(pp, layouts, mats, nat, image, umats):
         dp.natrow[i] = conv['natrow'][i]
     for i in range(6):
         dp.natk[i] = conv['natk'][i]
-    off = sum(m.size for m in umats)          # in FP16 values
-    for ri, (rd, U) in enumerate(zip(rounds, mats)):
+    for ri, rd in enumerate(rounds):
         o = dp.rounds[ri]
         for i in range(3):
             o.digits[i] = rd['digits'][i]
@@ -877,17 +949,46 @@ def _encode_tc(pp, layouts, mats, nat, image, umats):
             o.rowc[i] = rd['rowc'][i]
         for i in range(6):
             o.kc[i] = rd['kc'][i]
-        o.umoff = off
-        img = image(U)
-        umats.append(img)
-        off += img.size
+        o.umoff = umoff0 + ri * halves
     return dp
 
 
 def encode_pass_tc(p, n, umats):
     """DmTcPass for dm_apply_pass_tc; appends the rounds' FP16 matrix images (uint16) to ``umats``."""
     pp, layouts, mats = plan_tc_pass(p, n)
-    return _encode_tc(pp, layouts, mats, 'xor', tc_round_image, umats)
+    dp = _encode_tc(pp, layouts, 'xor', sum(m.size for m in umats), TC_IMAGE_HALVES)
+    umats.extend(tc_round_image(U) for U in mats)
+    return dp
+
+
+def encode_pass_tc_ops(p, n, coefs, kernel='tc'):
+    """(DmTcPass, DmBatchPass) of a tensor-core pass whose round images the device composes.
+
+    kernel 'tc' (dm_apply_pass_tc, images of TC_IMAGE_HALVES) or 'tma'
+    (dm_apply_pass_tma, TMA_IMAGE_HALVES).  The DmTcPass reads round r's
+    image at r * (image values): dm_compose_rounds writes them there from the
+    DmBatchPass's ops, whose FP64 coefficients are appended to ``coefs``
+    (a list of arrays; moff counts from its start).  Raises TcPlanError for
+    a pass that does not fit the kernel or the op table."""
+    nat = 'tma' if kernel == 'tma' else 'xor'
+    pp, rounds, layouts = plan_tc_rounds(p, n, nat)
+    if kernel == 'tma' and not tma_eligible(pp, n, layouts):
+        raise TcPlanError('pass does not fit the TMA-fed kernel (%d rounds, dims %s)'
+                          % (len(layouts), tma_box_dims(n, pp.axes)))
+    halves = TMA_IMAGE_HALVES if kernel == 'tma' else TC_IMAGE_HALVES
+    bp = N.DmBatchPass()
+    off = [sum(c.size for c in coefs)]
+
+    def place(op, flags, size):
+        c = round_op_coefficients(op)
+        assert c.size == size
+        coefs.append(c)
+        off[0] += size
+        return off[0] - size
+
+    dp = _encode_tc(pp, layouts, 'linear' if kernel == 'tma' else 'xor', 0, halves)
+    fill_round_ops(bp, pp, rounds, [L.digits for L in layouts], place)
+    return dp, bp
 
 
 # ---------------------------------------------------------------------------
@@ -958,4 +1059,6 @@ def encode_pass_tma(p, n, umats):
     if not tma_eligible(pp, n, layouts):
         raise TcPlanError('pass does not fit the TMA-fed kernel (%d rounds, dims %s)'
                           % (len(layouts), tma_box_dims(n, pp.axes)))
-    return _encode_tc(pp, layouts, mats, 'linear', tc_round_image_tma, umats)
+    dp = _encode_tc(pp, layouts, 'linear', sum(m.size for m in umats), TMA_IMAGE_HALVES)
+    umats.extend(tc_round_image_tma(U) for U in mats)
+    return dp

@@ -208,3 +208,52 @@ def test_malformed_tensor_core_batch_tables_are_rejected_on_host(lib):
     bad = (N.DmBatchTcPass * prog.npasses).from_buffer_copy(bytes(prog.passes))
     bad[0].ops.ops[0].kind = N.DM_OP_CX if bad[0].ops.ops[0].kind == N.DM_OP_MAP1 else N.DM_OP_MAP1
     assert run_params(bad) == N.DM_ERR_PROGRAM                          # slot recipe no longer fits the op
+
+
+def test_malformed_compose_table_is_rejected_on_host(lib):
+    """dm_compose_rounds checks its op table before any CUDA call (here there is no GPU)."""
+    import numpy as np
+    from qiskit_aakash_gb300 import program as P
+    n = 9
+    rng = np.random.default_rng(3)
+    ops = [P.Op('map1', (q,), rng.normal(size=(4, 4))) for q in range(n)]
+    ops += [P.Op('cx', (n - 1, n - 2), (1.0, 0.0, 1.0, 0.0, 0.0), True),
+            P.Op('map2', (n - 3, n - 4), rng.normal(size=(16, 16)))]
+    coefs = []
+    _, good = P.encode_pass_tc_ops(P.plan_passes(ops, n, 7, 2)[0], n, coefs, 'tc')
+    count = sum(c.size for c in coefs)
+    halves = good.nrounds * P.TC_IMAGE_HALVES
+    dev = ctypes.c_void_p(1 << 20)
+
+    def run(bp, fmt=N.DM_IMAGE_TC, cnt=count, images=dev, nimg=halves):
+        return lib.dm_compose_rounds(fmt, ctypes.byref(bp), dev, ctypes.c_size_t(cnt), images,
+                                     ctypes.c_size_t(nimg), None)
+
+    def copy():
+        return N.DmBatchPass.from_buffer_copy(bytes(good))
+
+    assert run(copy(), fmt=7) == N.DM_ERR_ARG                                    # unknown image format
+    assert run(copy(), images=ctypes.c_void_p(None)) == N.DM_ERR_ARG
+    assert run(copy(), images=ctypes.c_void_p((1 << 20) + 8)) == N.DM_ERR_ARG    # images not 16-byte aligned
+    assert run(copy(), nimg=halves - 1) == N.DM_ERR_ARG                          # images beyond the buffer
+    assert run(copy(), nimg=good.nrounds * P.TMA_IMAGE_HALVES) == N.DM_ERR_ARG  # 12288 values per round
+    assert run(copy(), cnt=count - 1) == N.DM_ERR_PROGRAM                        # coefficients beyond mats
+    bad = copy()
+    bad.nrounds = 0
+    assert run(bad) == N.DM_ERR_PROGRAM
+    bad = copy()
+    bad.round_end[bad.nrounds - 1] -= 1                                          # an op left outside every round
+    assert run(bad) == N.DM_ERR_PROGRAM
+    bad = copy()
+    bad.ops[0].kind = 9
+    assert run(bad) == N.DM_ERR_PROGRAM
+    bad = copy()
+    bad.ops[0].flags |= 3 << 8                                                   # digit position 3 of a 3-digit round
+    assert run(bad) == N.DM_ERR_PROGRAM
+    bad = copy()
+    bad.round_axes[0][1] = bad.round_axes[0][0]                                  # repeated round axis
+    assert run(bad) == N.DM_ERR_PROGRAM
+    pair = next(i for i in range(good.nops) if good.ops[i].kind != N.DM_OP_MAP1)
+    bad = copy()
+    bad.ops[pair].flags = (bad.ops[pair].flags & ~(3 << 12)) | (((bad.ops[pair].flags >> 8) & 3) << 12)
+    assert run(bad) == N.DM_ERR_PROGRAM                                          # both axes on one digit

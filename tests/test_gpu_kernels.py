@@ -183,8 +183,38 @@ def test_init_product(torch, n):
     np.testing.assert_allclose(t.cpu().numpy(), ref * 0.5 ** n, rtol=1e-15, atol=0)
 
 
+def _tc_launch(torch, kernel, p, n, t, status, compose, images):
+    """Run pass ``p`` on ``t`` with dm_apply_pass_tma (kernel 'tma') or dm_apply_pass_tc ('tc'), the
+    round images composed on the host and uploaded, or by dm_compose_rounds into ``images``.
+    False when the pass does not fit that kernel."""
+    name = 'dm_apply_pass_tma' if kernel == 'tma' else 'dm_apply_pass_tc'
+    try:
+        if compose == 'host':
+            umats = []
+            d = (P.encode_pass_tma if kernel == 'tma' else P.encode_pass_tc)(p, n, umats)
+            m = np.concatenate(umats)
+            md = torch.from_numpy(m.view(np.int16)).cuda()
+        else:
+            coefs = []
+            d, bp = P.encode_pass_tc_ops(p, n, coefs, kernel)
+            c = dev(torch, np.concatenate(coefs))
+            md = images
+            N.call('dm_compose_rounds', N.DM_IMAGE_TMA if kernel == 'tma' else N.DM_IMAGE_TC, ctypes.byref(bp),
+                   vp(c), ctypes.c_size_t(c.numel()), vp(md), ctypes.c_size_t(md.numel()), stream(torch))
+    except P.TcPlanError:
+        return False
+    N.call(name, vp(t), n, ctypes.byref(d), vp(md), ctypes.c_size_t(md.numel()), vp(status), stream(torch))
+    torch.cuda.synchronize()
+    return True
+
+
+def _image_buffer(torch):
+    return torch.empty(N.DM_MAX_ROUNDS * P.TC_IMAGE_HALVES, dtype=torch.int16, device='cuda')
+
+
+@pytest.mark.parametrize('compose', ['host', 'device'])
 @pytest.mark.parametrize('n', [7, 8, 10])
-def test_tensor_core_pass_equals_program_order(torch, n):
+def test_tensor_core_pass_equals_program_order(torch, n, compose):
     """dm_apply_pass_tc (FP16-split tcgen05 rounds) against the ops applied one by one in FP64.
 
     The FP16 form holds the tile in units of 2**-n with an absolute floor of
@@ -214,15 +244,11 @@ def test_tensor_core_pass_equals_program_order(torch, n):
     for op in ops:
         ref = apply_op(ref, n, op)
     passes = P.plan_passes(ops, n, 7, 2)
-    umats = []
-    descs = [P.encode_pass_tc(p, n, umats) for p in passes]
-    m = np.concatenate(umats)
-    md = torch.from_numpy(m.view(np.int16)).cuda()
     t = dev(torch, st, np.float32)
     status = torch.zeros(1, dtype=torch.int32, device='cuda')
-    for d in descs:
-        N.call('dm_apply_pass_tc', vp(t), n, ctypes.byref(d), vp(md), ctypes.c_size_t(m.size), vp(status),
-               stream(torch))
+    images = _image_buffer(torch)
+    for p in passes:
+        assert _tc_launch(torch, 'tc', p, n, t, status, compose, images)
     got = t.double().cpu().numpy()
     assert status.item() == 0
     assert np.max(np.abs(got - ref)) * 2.0 ** n < 2e-6
@@ -271,9 +297,10 @@ def _tma_case(kind, n):
     return ops, st
 
 
+@pytest.mark.parametrize('compose', ['host', 'device'])
 @pytest.mark.parametrize('kind,n', [('random', 7), ('random', 9), ('layered', 8), ('layered', 9), ('layered', 10),
                                     ('dense', 7), ('dense', 9)])
-def test_tma_pass_equals_program_order(torch, kind, n):
+def test_tma_pass_equals_program_order(torch, kind, n, compose):
     """dm_apply_pass_tma (TMA-fed tiles, resident round images, last round straight to global memory)
     against the ops applied in FP64, and against dm_apply_pass_tc on the same passes."""
     from test_planner import apply_op
@@ -285,29 +312,62 @@ def test_tma_pass_equals_program_order(torch, kind, n):
     status = torch.zeros(1, dtype=torch.int32, device='cuda')
     t_tma = dev(torch, st, np.float32)
     t_tc = dev(torch, st, np.float32)
+    images = _image_buffer(torch)
     used = 0
     for p in passes:
-        for name, enc, t in (('dm_apply_pass_tma', P.encode_pass_tma, t_tma), ('dm_apply_pass_tc', P.encode_pass_tc, t_tc)):
-            umats = []
-            try:
-                d = enc(p, n, umats)
-            except P.TcPlanError:
-                d = None
-            if d is None:     # a pass the TMA kernel does not take: the cp.async kernel for both
-                umats = []
-                d, name = P.encode_pass_tc(p, n, umats), 'dm_apply_pass_tc'
-            elif name == 'dm_apply_pass_tma':
-                used += 1
-            m = np.concatenate(umats)
-            md = torch.from_numpy(m.view(np.int16)).cuda()
-            N.call(name, vp(t), n, ctypes.byref(d), vp(md), ctypes.c_size_t(m.size), vp(status), stream(torch))
-            torch.cuda.synchronize()
+        if _tc_launch(torch, 'tma', p, n, t_tma, status, compose, images):
+            used += 1
+        else:     # a pass the TMA kernel does not take: the cp.async kernel for both
+            assert _tc_launch(torch, 'tc', p, n, t_tma, status, compose, images)
+        assert _tc_launch(torch, 'tc', p, n, t_tc, status, compose, images)
     assert used > 0
     assert status.item() == 0
     got = t_tma.double().cpu().numpy()
     other = t_tc.double().cpu().numpy()
     assert np.max(np.abs(got - ref)) * 2.0 ** n < 2e-6
     assert np.max(np.abs(got - other)) * 2.0 ** n < 1e-6
+
+
+@pytest.mark.parametrize('kernel', ['tc', 'tma'])
+def test_device_composed_round_images(torch, kernel):
+    """dm_compose_rounds (FP64 on the device) against the host composition (numpy FP64 products):
+    Uh + 2**-11 Ul within the split's own rounding of U, and the FP16 values equal except where
+    the last FP64 bit of an entry moves it across an FP16 rounding boundary.  (Values, not bits:
+    the device's op-by-op columns keep the sign of a zero that a negated or negatively scaled
+    zero gets, -0.0, where the host's matrix products sum it into +0.0.)"""
+    rng = np.random.default_rng(77)
+    n = 10
+    ops = _physical_ops(rng, n, 120)
+    halves = P.TMA_IMAGE_HALVES if kernel == 'tma' else P.TC_IMAGE_HALVES
+    host_image = P.tc_round_image_tma if kernel == 'tma' else P.tc_round_image
+    uh_at = 0 if kernel == 'tma' else 8192
+    images = _image_buffer(torch)
+    checked, differ, total = 0, 0, 0
+    for p in P.plan_passes(ops, n, 7, 2):
+        coefs = []
+        try:
+            dp, bp = P.encode_pass_tc_ops(p, n, coefs, kernel)
+        except P.TcPlanError:
+            continue
+        c = dev(torch, np.concatenate(coefs))
+        N.call('dm_compose_rounds', N.DM_IMAGE_TMA if kernel == 'tma' else N.DM_IMAGE_TC, ctypes.byref(bp),
+               vp(c), ctypes.c_size_t(c.numel()), vp(images), ctypes.c_size_t(images.numel()), stream(torch))
+        got = images[:bp.nrounds * halves].cpu().numpy().view(np.uint16)
+        _, rounds, layouts = P.plan_tc_rounds(p, n, 'tma' if kernel == 'tma' else 'xor')
+        for r, U in enumerate(P.compose_round_matrices(rounds, layouts)):
+            g = got[r * halves:(r + 1) * halves]
+            want = host_image(U)
+            differ += int(np.count_nonzero(g.view(np.float16) != want.view(np.float16)))
+            total += g.size
+            uh = g[uh_at + P._KMAJOR].view(np.float16).astype(np.float64).reshape(64, 64)
+            ul = g[4096 + P._KMAJOR].view(np.float16).astype(np.float64).reshape(64, 64)
+            assert np.all(np.abs(uh + ul * 2.0 ** -11 - U) <= 2.0 ** -21 * np.abs(U) + 2.0 ** -34)
+            if kernel == 'tc':
+                big = g[P._KMAJOR].view(np.float16).astype(np.float64).reshape(64, 64)
+                np.testing.assert_array_equal(big, uh * 2048.0)
+        checked += 1
+    assert checked > 0
+    assert differ <= 1e-4 * total
 
 
 def test_tensor_core_pass_rejects_bad_programs(torch):

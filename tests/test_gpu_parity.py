@@ -98,6 +98,7 @@ def test_workloads_match_oracle(n, layers, seed, every_gate, qft):
     for kw, tol in (({}, 1e-12), ({'tile_axes': 7}, 1e-12), ({'tile_axes': 4}, 1e-12),
                     ({'register_rounds': False}, 1e-12), ({'precision': 'single'}, FP32_TOL),
                     ({'precision': 'single', 'tma': False}, FP32_TOL),
+                    ({'precision': 'single', 'compose': 'host'}, FP32_TOL),
                     ({'precision': 'single', 'tensor_cores': False}, FP32_TOL),
                     ({'precision': 'single', 'tensor_cores': False, 'register_rounds': False}, FP32_TOL)):
         got, b = run_gpu(qc.to_experiment(), opts, **kw)
@@ -204,9 +205,10 @@ def test_tensor_core_fp32_against_fp64_twelve_qubits_twenty_layers():
     ref, _ = run_gpu(qc.to_experiment(), opts)
     a = ref['data']['coeffmatrix']
     p = np.array(list(ref['data']['ensemble_probability'].values()))
-    for kw in ({}, {'tma': False}):
+    for kw in ({}, {'tma': False}, {'compose': 'host'}):
         got, b = run_gpu(qc.to_experiment(), opts, precision='single', **kw)
         assert b.last_run_stats['passes'] > 0
+        assert b.last_run_stats['composed_on'][kw.get('compose', 'device')] > 0
         err = np.abs(got['data']['coeffmatrix'] - a).max() * 2 ** n
         p32 = np.array(list(got['data']['ensemble_probability'].values()))
         assert err <= FP32_TOL, (kw, err)

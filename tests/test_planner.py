@@ -582,3 +582,70 @@ def test_too_many_tensor_core_rounds_raise_a_plan_error():
     with pytest.raises(P.TcPlanError):
         for p in passes:
             P.encode_pass_tc(p, n, [])
+
+
+def _compose_from_table(bp, coefs):
+    """Each round's 64x64 U rebuilt from a DmBatchPass and its coefficients alone (what
+    dm_compose_rounds reads): ops act on digit positions taken from their flags."""
+    mats = np.concatenate(coefs)
+    out = []
+    kinds = {N.DM_OP_MAP1: 'map1', N.DM_OP_CX: 'cx', N.DM_OP_DIAG2: 'diag2', N.DM_OP_MAP2: 'map2'}
+    o = 0
+    for r in range(bp.nrounds):
+        U = np.eye(64)
+        for i in range(o, bp.round_end[r]):
+            d = bp.ops[i]
+            da, db = (d.flags >> 8) & 3, (d.flags >> 12) & 3
+            kind = kinds[d.kind]
+            size = {'map1': 16, 'cx': 5, 'diag2': 16, 'map2': 256}[kind]
+            c = mats[d.moff:d.moff + size]
+            if kind == 'map1':
+                op = P.Op(kind, (da,), c.reshape(4, 4))
+            elif kind == 'map2':
+                op = P.Op(kind, (da, db), c.reshape(16, 16))
+            else:
+                op = P.Op(kind, (da, db), c if kind == 'diag2' else tuple(c), bool(d.flags & N.DM_CX_IDEAL))
+            U = P.op_matrix64(op, (0, 1, 2)) @ U
+        o = bp.round_end[r]
+        out.append(U)
+    return out
+
+
+@pytest.mark.parametrize('kernel', ['tc', 'tma'])
+def test_device_composition_table_restates_the_rounds(kernel):
+    """The op table of a device-composed pass gives the host-composed round matrices, and its
+    conversion / epilogue tables are the host encoder's with round r's images at r * image size."""
+    rng = np.random.default_rng(11)
+    n = 10
+    ops = []
+    for layer in range(6):
+        for q in range(n - 2):
+            ops.append(P.Op('map1', (q,), rng.uniform(-0.6, 0.6, size=(4, 4))))
+        for q in range(layer % 2, n - 3, 2):
+            ops.append(P.Op('cx', (q, q + 1), P.cx_coefficients((0.99, 0.01))[0]))
+        ops.append(P.Op('diag2', (2, 5), rng.uniform(-1, 1, size=16)))
+        ops.append(P.Op('map2', (4, 1), rng.uniform(-0.25, 0.25, size=(16, 16))))
+    checked = 0
+    for p in P.plan_passes(ops, n, 7, 2):
+        coefs = []
+        try:
+            dp, bp = P.encode_pass_tc_ops(p, n, coefs, kernel)
+        except P.TcPlanError:
+            continue
+        nat = 'tma' if kernel == 'tma' else 'xor'
+        pp, rounds, layouts = P.plan_tc_rounds(p, n, nat)
+        want = P.compose_round_matrices(rounds, layouts)
+        got = _compose_from_table(bp, coefs)
+        assert len(got) == len(want) == dp.nrounds == bp.nrounds
+        for g, w in zip(got, want):
+            np.testing.assert_allclose(g, w, rtol=0, atol=1e-12 * max(1.0, np.abs(w).max()))
+        umats = []
+        host = (P.encode_pass_tma if kernel == 'tma' else P.encode_pass_tc)(p, n, umats)
+        halves = P.TMA_IMAGE_HALVES if kernel == 'tma' else P.TC_IMAGE_HALVES
+        for r in range(dp.nrounds):
+            assert dp.rounds[r].umoff == host.rounds[r].umoff == r * halves
+            assert list(dp.rounds[r].rowc) == list(host.rounds[r].rowc)
+            assert list(dp.rounds[r].kc) == list(host.rounds[r].kc)
+        assert list(dp.natrow) == list(host.natrow) and list(dp.natk) == list(host.natk)
+        checked += 1
+    assert checked > 0
