@@ -225,6 +225,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     const bool u_ok = team_and(mbar_wait(ubar, 0), team);
     if (!u_ok && ttid == 0) atomicExch(status, 1);
 
+    // operand descriptors of the two M = 128 blocks of h and l (shared addresses < 256 KB: the
+    // start-address field never carries into the next field)
+    uint64_t adesc_h[2], adesc_l[2];
+#pragma unroll
+    for (int mb = 0; mb < 2; ++mb) {
+        adesc_h[mb] = smem_desc(smem_u32(AH) + mb * (kABytes / 2));
+        adesc_l[mb] = smem_desc(smem_u32(AL) + mb * (kABytes / 2));
+    }
+
     // epilogue geometry: the thread holds row ttid of the 256-row operand, i.e. row ttid % 128 of
     // M block ttid / 128, in TMEM lane quadrant warp % 4
     const int mb_own = ttid >> 7;
@@ -279,20 +288,21 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (issue) {
                 // D[:, 0:64] = h Uh^T and D[:, 64:128] = h Ul^T (one N = 128 chain over [Uh ; Ul]),
                 // then D[:, 64:128] += l Uh^T (N = 64), for both M = 128 blocks
-                const uint32_t ah = smem_u32(AH), al = smem_u32(AL), ub = uslot(r);
+                const uint64_t ub = smem_desc(uslot(r));
 #pragma unroll
                 for (int mb = 0; mb < 2; ++mb) {
-                    const uint32_t aoff = mb * (kABytes / 2);
                     const uint32_t d = tmem + mb * 128;
 #pragma unroll
                     for (int term = 0; term < 2; ++term) {
                         const uint32_t dd = d + (term == 0 ? 0u : 64u);
-                        const uint32_t a = (term == 0 ? ah : al) + aoff;
+                        const uint64_t a = term == 0 ? adesc_h[mb] : adesc_l[mb];
                         const uint32_t idesc = term == 0 ? kIdesc128 : kIdesc64;
 #pragma unroll
                         for (int ks = 0; ks < 4; ++ks) {
-                            const uint64_t da = smem_desc(a + ks * 2 * kLBO);
-                            const uint64_t db = smem_desc(ub + ks * 2 * kLBO);
+                            // a K step of 16 values is two core matrices (256 bytes): +16 in the
+                            // descriptor's start-address field (address >> 4, bits 0-13)
+                            const uint64_t da = a + uint64_t(ks * (2 * kLBO >> 4));
+                            const uint64_t db = ub + uint64_t(ks * (2 * kLBO >> 4));
                             const uint32_t acc = (term | ks) ? 1u : 0u;
                             asm volatile(
                                 "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
