@@ -306,6 +306,39 @@ def pass_kernel_profile(torch, state):
     return out
 
 
+def tile_pattern_ceiling(torch, N, state, entry):
+    """DRAM rate of the tiles that the recorded step's `entry` passes stream: dm_tile_copy_probe (an
+    in-place read and write of every tile, 16-byte accesses, values unchanged) over each such pass's
+    resident qubits, CUDA events on the current stream; algorithmic bytes / probe time."""
+    import ctypes
+    shapes = {}
+    for name, args in state.tape:
+        if name == entry:
+            ax = tuple(int(a) for a in args[2]._obj.axes)
+            shapes[ax] = shapes.get(ax, 0) + 1
+    if not shapes:
+        return None
+    L = N.lib()
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    ptr = ctypes.c_void_p(state.state.data_ptr())
+    total_ms, count = 0.0, 0
+    for ax, k in shapes.items():
+        a = (ctypes.c_int32 * 7)(*ax)
+        N.call('dm_tile_copy_probe', ptr, state.n, a, sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(2):
+            N.call('dm_tile_copy_probe', ptr, state.n, a, sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        total_ms += k * e0.elapsed_time(e1) / 2
+        count += k
+    gbs = count * 2 * 4.0 ** state.n * 4 / (total_ms / 1e3) / 1e9
+    return {'gbs': gbs, 'passes': count, 'tile_shapes': len(shapes),
+            'probe': 'dm_tile_copy_probe over the same passes\' tiles (in-place read + write, 16-byte accesses)'}
+
+
 def all_durations(by_kernel):
     """Durations of the pass launches (the round-matrix composition launches are listed apart)."""
     return [d for k, v in by_kernel.items() if k != 'compose_pass_kernel' for d in v]
@@ -656,6 +689,8 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
     value32, ms32 = replica_throughput(torch, world, float(layers), ms32)
     by_kernel = pass_kernel_profile(torch, st32)     # a full replay: leaves the final FP32 state
     passes_by_kernel = dict(st32.passes_by_kernel)
+    top_kernel = max(by_kernel, key=lambda k: sum(by_kernel[k]))
+    pattern = tile_pattern_ceiling(torch, N, st32, {v: k for k, v in PASS_KERNELS.items()}[top_kernel])
     prob32 = np.array(list(r32['data']['ensemble_probability'].values()))
 
     # --- plain FP64 (the parity form) ---------------------------------------
@@ -759,7 +794,8 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
                      'mean_launch_ms': mean_pass_ms,
                      'tensor_pipe_active': profiled_value('tensor_pipe_active'),
                      'tensor_pipe_source': 'sm__pipe_tensor_cycles_active of the committed ncu capture at n = 14',
-                     'algorithmic_bytes_per_launch': 2 * N4 * 4, 'peak_kind': peak_kind},
+                     'algorithmic_bytes_per_launch': 2 * N4 * 4, 'peak_kind': peak_kind,
+                     'tile_pattern': dict(pattern, frac=achieved / pattern['gbs']) if pattern else None},
         'e2e': {'value': world * layers / e2e_s, 'unit': 'gate-layers/s', 'seconds_per_step': e2e_s,
                 'seconds_each': each, 'copy_out_each': copies,
                 'h2d_bytes_per_step': int(st['h2d_bytes']), 'd2h_bytes_per_step': int(st['d2h_bytes']),

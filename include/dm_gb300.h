@@ -201,6 +201,14 @@ int dm_max_abs_diff(const void *a_dev, int dtype_a, const void *b_dev, int dtype
 int dm_fp64_fma_probe_threads(void);
 int dm_fp64_fma_probe(double *out_dev, int64_t iters, void *stream);
 
+/* Tile-pattern copy probe (measurement only, no reference counterpart):
+ * reads and writes the FP32 state at state_dev (4**n values) in place, tile by
+ * tile, for the 7 resident qubits axes[0..6] (strictly decreasing, axes[0] =
+ * n-1) with 16-byte accesses and no change to any value.  Its rate is the DRAM
+ * rate this tile shape allows; bench.py times it over the tiles of the
+ * headline's tensor-core passes beside their own rate. */
+int dm_tile_copy_probe(float *state_dev, int n, const int32_t *axes, void *stream);
+
 /* Page-locked host memory mapped into the device's address space
  * (cudaHostAlloc, mapped and portable), exactly `bytes` long, or NULL.  The
  * copy-out writes a result block of this kind directly from the chop kernel

@@ -182,6 +182,7 @@ SIGNATURES = {
     'dm_apply_pass_tma': (_i, [_vp, _i, ctypes.POINTER(DmTcPass), _vp, _sz, _vp, _vp]),
     'dm_compose_rounds': (_i, [_i, ctypes.POINTER(DmBatchPass), _vp, _sz, _vp, _sz, _vp]),
     'dm_max_abs_diff': (_i, [_vp, _i, _vp, _i, _i, _vp, _vp]),
+    'dm_tile_copy_probe': (_i, [_vp, _i, _vp, _vp]),
     'dm_fp64_fma_probe_threads': (_i, []),
     'dm_fp64_fma_probe': (_i, [_vp, ctypes.c_int64, _vp]),
     'dm_levelize': (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

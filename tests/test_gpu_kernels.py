@@ -459,3 +459,18 @@ def test_bounded_wait_gives_up_and_the_engine_raises(torch):
     ds.map1(3, IDENTITY4)
     with pytest.raises(BasicAerError, match='bounded wait'):
         ds.flush()
+
+
+def test_tile_copy_probe_leaves_the_state(torch):
+    """dm_tile_copy_probe rewrites every tile in place without changing a bit."""
+    n = 9
+    rng = np.random.default_rng(8)
+    st = rng.normal(size=4 ** n).astype(np.float32)
+    t = dev(torch, st, np.float32)
+    for axes in ([8, 7, 6, 5, 4, 3, 2], [8, 7, 5, 3, 2, 1, 0]):
+        a = (ctypes.c_int32 * 7)(*axes)
+        N.call('dm_tile_copy_probe', vp(t), n, a, stream(torch))
+    torch.cuda.synchronize()
+    assert np.array_equal(t.cpu().numpy().view(np.uint32), st.view(np.uint32))
+    bad = (ctypes.c_int32 * 7)(7, 6, 5, 4, 3, 2, 1)          # lowest qubit not resident
+    assert N.lib().dm_tile_copy_probe(vp(t), n, bad, stream(torch)) == N.DM_ERR_ARG
