@@ -658,7 +658,10 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
     stcc = bcc.recorded_state
     stcc.replay()
     ms_cc = time_replays(torch, stcc, 1)
-    durs_cc = all_durations(pass_kernel_profile(torch, stcc))
+    by_cc = pass_kernel_profile(torch, stcc)
+    durs_cc = all_durations(by_cc)
+    kernels_cc = {k: {'launches': len(v), 'mean_ms': float(np.mean(v)),
+                      'achieved_gbs': 2 * 4.0 ** n * 4 / (float(np.mean(v)) / 1e3) / 1e9} for k, v in by_cc.items()}
     del stcc, bcc
     torch.cuda.empty_cache()
 
@@ -780,8 +783,11 @@ def headline_leg(args, pkg, torch, N, DmSimulatorGPU, world, rank):
         'fp32_over_fp64': ms64 / ms32,
         'fp32_cuda_cores': {'value': world * layers / (ms_cc / 1e3), 'unit': 'gate-layers/s', 'ms_per_step': ms_cc,
                             'kernel': 'pass_pipe_kernel<float,3>',
+                            'pass_kernels': kernels_cc,
                             'mean_pass_ms': float(np.mean(durs_cc)) if durs_cc else None,
-                            'pass_achieved_gbs': (2 * N4 * 4 / (float(np.mean(durs_cc)) / 1e3) / 1e9) if durs_cc else None},
+                            'pass_achieved_gbs': (2 * N4 * 4 / (float(np.mean(durs_cc)) / 1e3) / 1e9) if durs_cc else None,
+                            'pass_frac_of_hbm': (2 * N4 * 4 / (float(np.mean(durs_cc)) / 1e3) / 1e9 / hbm)
+                            if durs_cc else None},
         'fp32_tc_cp_async': {'value': world * layers / (ms_ca / 1e3), 'unit': 'gate-layers/s', 'ms_per_step': ms_ca,
                              'kernel': 'pass_tc_kernel only (tiles by cp.async, two CTAs per SM)',
                              'mean_pass_ms': float(np.mean(durs_ca)) if durs_ca else None},
