@@ -154,7 +154,12 @@ typedef struct dm_tc_pass {
     int32_t axes[7];      /* resident qubits, strictly decreasing; axes[0] must be n-1 */
     int32_t nrounds;
     int8_t vec0;          /* 0 when round 0's digit 0 is local axis 0 (128-bit conversion loads), else -1 */
-    int8_t pad[3];
+    int8_t direct_last;   /* dm_apply_pass_tc and the batched tensor-core sweeps: 1 = the last round stores
+                             straight to global memory (its rowc / kc are the linear natural offsets 2**b
+                             of tile bits b, rows 0-3 on tile bits 0-3) and the next tile's load overlaps
+                             it; 0 = through the natural tile in shared memory.  dm_apply_pass_tma always
+                             stores its last round directly and ignores this field. */
+    int8_t pad[2];
     uint32_t natrow[8];   /* natural-tile element offset of round 0's row bit i */
     uint32_t natk[6];     /* natural-tile element offset of round 0's K bit i */
     dm_tc_round rounds[DM_MAX_ROUNDS];

@@ -106,7 +106,7 @@ class DmTcRound(ctypes.Structure):
 
 class DmTcPass(ctypes.Structure):
     _fields_ = [('axes', ctypes.c_int32 * 7), ('nrounds', ctypes.c_int32), ('vec0', ctypes.c_int8),
-                ('pad', ctypes.c_int8 * 3), ('natrow', ctypes.c_uint32 * 8), ('natk', ctypes.c_uint32 * 6),
+                ('direct_last', ctypes.c_int8), ('pad', ctypes.c_int8 * 2), ('natrow', ctypes.c_uint32 * 8), ('natk', ctypes.c_uint32 * 6),
                 ('rounds', DmTcRound * DM_MAX_ROUNDS)]
 
 

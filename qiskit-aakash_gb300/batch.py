@@ -275,9 +275,10 @@ class _Plan:
         return out.astype(dtype)
 
 
-def fill_tc_tables(t, pp, layouts):
+def fill_tc_tables(t, pp, layouts, direct=False):
     """The conversion and epilogue tables of a 7-axis pass (dm_tc_pass; umoff left 0)."""
-    conv, rtables = P.tc_tables(layouts)
+    conv, rtables = P.tc_tables(layouts, 'xor', direct)
+    t.direct_last = 1 if direct else 0
     for r, q in enumerate(pp.axes):
         t.axes[r] = q
     t.nrounds = len(layouts)
@@ -314,10 +315,11 @@ class _TcPlan(_Plan):
             rounds = P.plan_rounds(pp, 3, pad='neighbors')
             if len(rounds) > N.DM_MAX_ROUNDS:
                 raise P.TcPlanError('pass needs %d rounds (> %d)' % (len(rounds), N.DM_MAX_ROUNDS))
-            layouts = P._choose_layouts([axes for axes, _ in rounds])
+            direct = P.direct_last_eligible([axes for axes, _ in rounds])
+            layouts = P._choose_layouts([axes for axes, _ in rounds], direct=direct)
             bp = N.DmBatchTcPass()
             self._fill(bp.ops, pp, rounds, [L.digits for L in layouts])
-            fill_tc_tables(bp.tables, pp, layouts)
+            fill_tc_tables(bp.tables, pp, layouts, direct)
             self.passes.append(bp)
 
     def table_bytes(self):

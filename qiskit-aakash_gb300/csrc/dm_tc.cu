@@ -61,12 +61,25 @@ __device__ __forceinline__ int nat_swz(int e) { return e ^ ((((e >> 5) ^ (e >> 8
 struct Pass {
     int n, m, low, nrounds;
     int vec0;
+    int direct;                      // the last round stores straight to global memory (offsets lastg)
     float up, down;                  // 2**n, 2**-n
     int64_t res_stride[kAxes];
     int64_t nonres_stride[DM_MAX_QUBITS];
     uint32_t natrow[8], natk[6];
+    int64_t lastg[14];               // direct: global element offsets of the last round's row bits 0-7, K bits 0-5
     Round rounds[DM_MAX_ROUNDS];
 };
+
+// Global offsets of a direct last round's 14 bits: its tables hold the linear natural offset
+// 2**b of tile bit b, i.e. bit b % 2 of local axis b / 2.
+__host__ __device__ inline void direct_offsets(Pass &p, const uint32_t *rowc, const uint32_t *kc) {
+    for (int i = 0; i < 14; ++i) {
+        const uint32_t c = i < 8 ? rowc[i] : kc[i - 8];
+        int b = 0;
+        while (b < 2 * kAxes - 1 && (1u << b) != c) ++b;
+        p.lastg[i] = p.res_stride[b >> 1] << (b & 1);
+    }
+}
 
 __device__ __forceinline__ int64_t tile_offset(const Pass &p, int e) {
     int64_t off = e & ((1 << (2 * p.low)) - 1);
@@ -162,8 +175,10 @@ __device__ __forceinline__ bool tc_pass_tiles(float *__restrict__ st, const Pass
     };
 
     load_u(0);
+    bool loaded = false;   // the tile's load went out during the previous tile's last round
     for (int64_t t = t0; t < ntiles; t += dt) {
-        load_tile(t);
+        if (!loaded) load_tile(t);
+        loaded = false;
         cp_async_wait_all();
         __syncthreads();
         // ---- natural tile -> round 0's operand (h / l), in place ----
@@ -266,6 +281,12 @@ __device__ __forceinline__ bool tc_pass_tiles(float *__restrict__ st, const Pass
             uint32_t tk[3][4];
             digit_tables(R.kc, tk);
             const bool last = r + 1 == p.nrounds;
+            if (last && p.direct && t + dt < ntiles) {
+                // the operands are consumed and this round writes straight to global memory: the next
+                // tile's load overlaps the epilogue
+                load_tile(t + dt);
+                loaded = true;
+            }
 #pragma unroll 1
             for (int i = 0; i < kBlocksPerThread; ++i) {
                 const int mb = kBlocksPerThread == 1 ? (warp >> 2) : i;
@@ -277,6 +298,30 @@ __device__ __forceinline__ bool tc_pass_tiles(float *__restrict__ st, const Pass
                 const uint32_t base = xor_bits<8>(uint32_t((tid & 127) + 128 * mb), R.rowc);
                 if (!last) {
                     store_all<true>(v, R.vec, base, tk, AH, AL);   // split from the accumulator scale
+                } else if (p.direct) {
+                    // the row straight to global memory: rows 0-3 are tile bits 0-3 (16 contiguous
+                    // coefficients on lanes 0-15)
+                    const float down = p.down * kLoUnscale;
+                    const int row = (tid & 127) + 128 * mb;
+                    int64_t rowg = tile_base(t);
+#pragma unroll
+                    for (int b = 0; b < 8; ++b)
+                        if ((row >> b) & 1) rowg += p.lastg[b];
+                    float *row_ptr = st + rowg;
+                    const int64_t k0 = p.lastg[8], k1 = p.lastg[9];
+#pragma unroll
+                    for (int d2 = 0; d2 < 4; ++d2) {
+                        const int64_t o2 = (d2 & 1 ? p.lastg[12] : 0) + (d2 & 2 ? p.lastg[13] : 0);
+#pragma unroll
+                        for (int d1 = 0; d1 < 4; ++d1) {
+                            float *q = row_ptr + o2 + (d1 & 1 ? p.lastg[10] : 0) + (d1 & 2 ? p.lastg[11] : 0);
+                            const int j = 4 * d1 + 16 * d2;
+                            q[0] = v[j] * down;
+                            q[k0] = v[j + 1] * down;
+                            q[k1] = v[j + 2] * down;
+                            q[k0 + k1] = v[j + 3] * down;
+                        }
+                    }
                 } else {
                     const float down = p.down * kLoUnscale;   // back to coefficients
 #pragma unroll
@@ -288,6 +333,7 @@ __device__ __forceinline__ bool tc_pass_tiles(float *__restrict__ st, const Pass
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         }
         if (abort_s) break;
+        if (p.direct) continue;   // written by the last round
         __syncthreads();
         // ---- write the tile back with 128-bit stores; the next load waits for these reads ----
         {
@@ -339,6 +385,7 @@ __device__ void batch_tc_setup(Pass &ps, const dm_batch_tc_pass &bp, int n) {
         ps.low = low;
         ps.nrounds = bp.ops.nrounds;
         ps.vec0 = bp.tables.vec0 == 0 ? 0 : -1;
+        ps.direct = bp.tables.direct_last ? 1 : 0;
         ps.up = ldexpf(1.0f, n);
         ps.down = ldexpf(1.0f, -n);
         unsigned resident = 0;
@@ -351,6 +398,10 @@ __device__ void batch_tc_setup(Pass &ps, const dm_batch_tc_pass &bp, int n) {
             if (!((resident >> q) & 1)) ps.nonres_stride[m++] = int64_t(1) << (2 * (n - 1 - q));
         for (int i = 0; i < 8; ++i) ps.natrow[i] = bp.tables.natrow[i];
         for (int i = 0; i < 6; ++i) ps.natk[i] = bp.tables.natk[i];
+        if (ps.direct) {
+            const dm_tc_round &L = bp.tables.rounds[bp.ops.nrounds - 1];
+            direct_offsets(ps, L.rowc, L.kc);
+        }
     }
     for (int r = tid; r < bp.ops.nrounds; r += kThreads) {
         const dm_tc_round &in = bp.tables.rounds[r];
@@ -608,6 +659,18 @@ static bool valid_tables(const uint32_t *rowc, const uint32_t *kc, int vec, bool
     return true;
 }
 
+// A direct last round's tables: the linear natural offsets 2**b of 14 distinct tile bits, rows 0-3
+// on tile bits 0-3 (lanes 0-15 of a warp store 16 contiguous coefficients).
+static bool direct_tables(const uint32_t *rowc, const uint32_t *kc) {
+    uint32_t seen = 0;
+    for (int i = 0; i < 14; ++i) {
+        const uint32_t c = i < 8 ? rowc[i] : kc[i - 8];
+        if (c == 0 || (c & (c - 1)) || c >= uint32_t(tc::kTile) || (seen & c)) return false;
+        seen |= c;
+    }
+    return (rowc[0] | rowc[1] | rowc[2] | rowc[3]) == 15u;
+}
+
 extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, const uint16_t *umats_dev,
                                 size_t umats_count, int *status_dev, void *stream) {
     DM_CHECK_ARG(state_dev && pass && umats_dev && status_dev && valid_n(n));
@@ -637,6 +700,8 @@ extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, 
     for (int u = m; u < DM_MAX_QUBITS; ++u) p.nonres_stride[u] = 0;
     p.nrounds = nr;
     p.vec0 = pass->vec0 == 0 ? 0 : -1;
+    p.direct = pass->direct_last ? 1 : 0;
+    if (pass->direct_last != 0 && pass->direct_last != 1) return DM_ERR_PROGRAM;
     // round 0 conversion reads: natural offsets of round 0's bits
     if (!valid_tables(pass->natrow, pass->natk, p.vec0, true)) return DM_ERR_PROGRAM;
     for (int i = 0; i < 8; ++i) p.natrow[i] = pass->natrow[i];
@@ -649,9 +714,12 @@ extern "C" int dm_apply_pass_tc(void *state_dev, int n, const dm_tc_pass *pass, 
             o.digits[i] = in.digits[i];
         }
         o.vec = in.vec;
-        if (!valid_tables(in.rowc, in.kc, in.vec, r + 1 == nr)) return DM_ERR_PROGRAM;
+        const bool direct_round = p.direct && r + 1 == nr;
+        if (!(direct_round ? direct_tables(in.rowc, in.kc) : valid_tables(in.rowc, in.kc, in.vec, r + 1 == nr)))
+            return DM_ERR_PROGRAM;
         for (int i = 0; i < 8; ++i) o.rowc[i] = in.rowc[i];
         for (int i = 0; i < 6; ++i) o.kc[i] = in.kc[i];
+        if (direct_round) tc::direct_offsets(p, in.rowc, in.kc);
         if (in.umoff < 0 || (in.umoff & 7) || size_t(in.umoff) + tc::kUHalves > umats_count) return DM_ERR_PROGRAM;
         o.umoff = in.umoff;
     }
@@ -723,11 +791,14 @@ static int validate_batch_tc_pass(const dm_batch_tc_pass &bp, int n, int64_t mat
         if (o.axes[r] < 0 || o.axes[r] >= n || (r > 0 && o.axes[r] >= o.axes[r - 1])) return DM_ERR_PROGRAM;
     const int vec0 = bp.tables.vec0 == 0 ? 0 : -1;
     if (!valid_tables(bp.tables.natrow, bp.tables.natk, vec0, true)) return DM_ERR_PROGRAM;
+    if (bp.tables.direct_last != 0 && bp.tables.direct_last != 1) return DM_ERR_PROGRAM;
     for (int r = 0; r < o.nrounds; ++r) {
         const dm_tc_round &tr = bp.tables.rounds[r];
         for (int i = 0; i < 3; ++i)
             if (tr.digits[i] != o.round_axes[r][i]) return DM_ERR_PROGRAM;
-        if (!valid_tables(tr.rowc, tr.kc, tr.vec, r + 1 == o.nrounds)) return DM_ERR_PROGRAM;
+        const bool direct_round = bp.tables.direct_last && r + 1 == o.nrounds;
+        if (!(direct_round ? direct_tables(tr.rowc, tr.kc) : valid_tables(tr.rowc, tr.kc, tr.vec, r + 1 == o.nrounds)))
+            return DM_ERR_PROGRAM;
     }
     return validate_round_ops(o, mats_len, false);
 }

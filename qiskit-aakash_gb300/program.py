@@ -607,7 +607,7 @@ def _best_next_cost(cand, next_axes):
 
 
 @functools.lru_cache(maxsize=4096)
-def _choose_layouts_cached(rounds_axes, nat='xor'):
+def _choose_layouts_cached(rounds_axes, nat='xor', direct=False):
     import itertools
     layouts = []
     prev = None
@@ -616,6 +616,18 @@ def _choose_layouts_cached(rounds_axes, nat='xor'):
         axes = sorted(axes)
         nonround = [tb for tb in range(2 * TC_AXES) if tb // 2 not in axes]
         nxt_axes = set(rounds_axes[ri + 1]) if ri < nlast else None
+        if direct and ri == nlast and prev is not None:
+            # the last round stores to global memory: rows 0-3 on tile bits 0-3, chosen by the cost
+            # of the epilogue into it
+            best = None
+            for d, rows in _tma_last_candidates(axes, prev):
+                cand = TcLayout(list(d), rows)
+                vec = 8 if _vec_digit(prev, cand.digits[0]) >= 0 else None
+                cost = _transition_cost(prev, cand.byte_of_bit, vec)
+                if best is None or cost < best[0]:
+                    best = (cost, cand)
+            layouts.append(best[1])
+            break
         if prev is None:
             # round 0: its rows 0-2 and K bits 3-4 are the lanes of the conversion's natural-tile
             # loads; its rows 0-4 the lanes of its own epilogue
@@ -755,7 +767,14 @@ def _tma_last_candidates(axes, prev):
     return out
 
 
-def _choose_layouts(rounds_axes, nat='xor'):
+def direct_last_eligible(rounds_axes):
+    """True when a cp.async-fed tensor-core pass can store its last round straight to global memory:
+    at least two rounds, and the last one leaves local axes 0 and 1 alone (its rows 0-3 then hold
+    tile bits 0-3, 16 contiguous coefficients per 16 lanes)."""
+    return len(rounds_axes) >= 2 and not {0, 1} & set(rounds_axes[-1])
+
+
+def _choose_layouts(rounds_axes, nat='xor', direct=False):
     """Pick each round's digit order and row-bit order (greedy along the rounds, one round of lookahead).
 
     The epilogue of round r (one source row per thread) writes round r+1's
@@ -768,7 +787,7 @@ def _choose_layouts(rounds_axes, nat='xor'):
     outgoing one; the last round pays for its stores into the natural tile
     (``nat`` names that tile's layout, see NAT_MAPS).
     """
-    return list(_choose_layouts_cached(tuple(tuple(sorted(a)) for a in rounds_axes), nat))
+    return list(_choose_layouts_cached(tuple(tuple(sorted(a)) for a in rounds_axes), nat, bool(direct)))
 
 
 def _vec_digit(src, dst_first_axis):
@@ -827,7 +846,8 @@ def plan_tc_rounds(p, n, nat='xor'):
     if nat == 'tma':
         layouts = list(_choose_layouts_tma_cached(tuple(tuple(sorted(a)) for a, _ in rounds)))
     else:
-        layouts = _choose_layouts([axes for axes, _ in rounds], nat)
+        axes = [a for a, _ in rounds]
+        layouts = _choose_layouts(axes, nat, direct=nat == 'xor' and direct_last_eligible(axes))
     return pp, rounds, layouts
 
 
@@ -905,8 +925,9 @@ def round_op_coefficients(op):
     return np.ascontiguousarray(op.data, dtype=np.float64).reshape(-1)
 
 
-def tc_tables(layouts, nat='xor'):
-    """Conversion and per-round epilogue tables of a tensor-core pass (see dm_tc_pass)."""
+def tc_tables(layouts, nat='xor', direct=False):
+    """Conversion and per-round epilogue tables of a tensor-core pass (see dm_tc_pass); with
+    ``direct`` the last round's are the linear natural offsets of its bits (global stores)."""
     f = NAT_MAPS[nat]
     L0 = layouts[0]
     conv = {'natrow': [f(1 << tb) for tb in L0.rowbits], 'natk': [f(1 << tb) for tb in L0.kbits],
@@ -918,6 +939,10 @@ def tc_tables(layouts, nat='xor'):
             rowc = [nxt.byte_of_bit(tb) for tb in L.rowbits]
             kc = [nxt.byte_of_bit(tb) for tb in L.kbits]
             vec = _vec_digit(L, nxt.digits[0])
+        elif direct:
+            rowc = [1 << tb for tb in L.rowbits]
+            kc = [1 << tb for tb in L.kbits]
+            vec = -1
         else:
             rowc = [f(1 << tb) for tb in L.rowbits]
             kc = [f(1 << tb) for tb in L.kbits]
@@ -930,8 +955,10 @@ def _encode_tc(pp, layouts, nat, umoff0, halves):
     """DmTcPass tables of a planned pass; round r reads its image at umoff0 + r * halves."""
     if len(layouts) > N.DM_MAX_ROUNDS:
         raise TcPlanError('pass needs %d rounds (> %d)' % (len(layouts), N.DM_MAX_ROUNDS))
-    conv, rounds = tc_tables(layouts, nat)
+    direct = nat == 'xor' and direct_last_eligible([L.digits for L in layouts])
+    conv, rounds = tc_tables(layouts, nat, direct)
     dp = N.DmTcPass()
+    dp.direct_last = 1 if direct else 0
     for r, q in enumerate(pp.axes):
         dp.axes[r] = q
     dp.nrounds = len(layouts)

@@ -125,7 +125,8 @@ class TemplateProgram:
             rounds = P.plan_rounds(pp, 3, pad='neighbors')
             if len(rounds) > N.DM_MAX_ROUNDS:
                 raise P.TcPlanError('pass needs %d rounds (> %d)' % (len(rounds), N.DM_MAX_ROUNDS))
-            layouts = P._choose_layouts([axes for axes, _ in rounds])
+            direct = P.direct_last_eligible([axes for axes, _ in rounds])
+            layouts = P._choose_layouts([axes for axes, _ in rounds], direct=direct)
             bp = N.DmBatchTcPass()
             o = bp.ops
             o.k = len(pp.axes)
@@ -156,7 +157,7 @@ class TemplateProgram:
                     idx += 1
                 o.round_end[ri] = idx
             o.nops = idx
-            fill_tc_tables(bp.tables, pp, layouts)
+            fill_tc_tables(bp.tables, pp, layouts, direct)
             passes.append(bp)
         self.passes = (N.DmBatchTcPass * len(passes))(*passes)
         self.npasses = len(passes)

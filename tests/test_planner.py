@@ -250,7 +250,10 @@ def test_register_rounds_equal_program_order(n, kmax, low, width):
 def _emulate_tc_pass(st, n, p):
     """numpy model of dm_apply_pass_tc's data movement (exact arithmetic, no FP16 split)."""
     pp, layouts, mats = P.plan_tc_pass(p, n)
-    conv, rounds = P.tc_tables(layouts)
+    direct = P.direct_last_eligible([L.digits for L in layouts])
+    conv, rounds = P.tc_tables(layouts, 'xor', direct)
+    if direct:   # the last round's rows 0-3: the 16 contiguous coefficients of the tile
+        assert sorted(rounds[-1]['rowc'][:4]) == [1, 2, 4, 8]
     k = 7
     non = [q for q in range(n - 1, -1, -1) if q not in pp.axes]
     out = st.copy()
@@ -289,7 +292,8 @@ def _emulate_tc_pass(st, n, p):
                         newA[o // 2] = D[row, j]
             if not last:
                 A = newA
-        out[idx] = natout[[P.nat_swz(e) for e in range(4 ** k)]]
+        # a direct last round writes linear natural positions straight to global memory
+        out[idx] = natout if direct else natout[[P.nat_swz(e) for e in range(4 ** k)]]
     return out
 
 
