@@ -19,10 +19,15 @@
 // scales by 2**-11.
 // FP16 runs at twice the TF32 rate and halves the operand bytes.  The
 // epilogue reads D from TMEM (tcgen05.ld, one group per thread) and writes
-// the h / l split directly in the operand layout of the next round; after
-// the last round it writes the tile back in its natural FP32 layout for
-// 128-bit stores.  Every wait on an mbarrier is bounded: a wait that gives
-// up records an error in *status and the kernel drains and returns.
+// the h / l split directly in the operand layout of the next round.  The
+// last round either stores each thread's row straight to global memory (a
+// "direct" last round: its rows 0-3 are tile bits 0-3, so lanes 0-15 write
+// 16 contiguous coefficients) while the next tile's cp.async load, issued as
+// soon as the round's MMAs have read the operands, lands in the freed
+// operand region; or, when it acts on local axes 0 and 1, it writes the tile
+// back in its natural FP32 layout for 128-bit stores.  Every wait on an
+// mbarrier is bounded: a wait that gives up records an error in *status and
+// the kernel drains and returns.
 //
 // Two CTAs of 256 threads share an SM, so one CTA's tile load, barriers
 // and MMA waits overlap the other's work.  Shared memory per CTA (dynamic,
