@@ -257,3 +257,42 @@ def test_malformed_compose_table_is_rejected_on_host(lib):
     bad = copy()
     bad.ops[pair].flags = (bad.ops[pair].flags & ~(3 << 12)) | (((bad.ops[pair].flags >> 8) & 3) << 12)
     assert run(bad) == N.DM_ERR_PROGRAM                                          # both axes on one digit
+
+
+def test_direct_last_round_tables_are_checked_on_host(lib):
+    """dm_apply_pass_tc checks a direct last round's tables (linear offsets of 14 distinct tile bits,
+    rows 0-3 on tile bits 0-3) before any CUDA call (here there is no GPU)."""
+    import numpy as np
+    from qiskit_aakash_gb300 import program as P
+    from test_planner import random_ops
+    n = 10
+    ops = [op for op in random_ops(np.random.default_rng(21), n, 120) if all(q < n - 2 for q in op.axes)]
+    good = None
+    for p in P.plan_passes(ops, n, 7, 2):
+        d, _ = P.encode_pass_tc_ops(p, n, [], 'tc')
+        if d.direct_last:
+            good = d
+            break
+    assert good is not None
+    dev = ctypes.c_void_p(1 << 20)
+
+    def run(d):
+        return lib.dm_apply_pass_tc(dev, n, ctypes.byref(d), dev, ctypes.c_size_t(1 << 20), dev, None)
+
+    def copy():
+        return N.DmTcPass.from_buffer_copy(bytes(good))
+
+    last = good.nrounds - 1
+    assert sorted(good.rounds[last].rowc[:4]) == [1, 2, 4, 8]
+    bad = copy()
+    bad.direct_last = 2
+    assert run(bad) == N.DM_ERR_PROGRAM
+    bad = copy()
+    bad.rounds[last].rowc[0], bad.rounds[last].rowc[4] = bad.rounds[last].rowc[4], bad.rounds[last].rowc[0]
+    assert run(bad) == N.DM_ERR_PROGRAM                                  # rows 0-3 not the contiguous bits
+    bad = copy()
+    bad.rounds[last].kc[0] = bad.rounds[last].kc[1]                      # a tile bit twice
+    assert run(bad) == N.DM_ERR_PROGRAM
+    bad = copy()
+    bad.rounds[last].kc[0] = 3                                           # not a power of two
+    assert run(bad) == N.DM_ERR_PROGRAM
