@@ -340,17 +340,25 @@ __device__ __forceinline__ bool tc_pass_tiles(float *__restrict__ st, const Pass
         if (abort_s) break;
         if (p.direct) continue;   // written by the last round
         __syncthreads();
-        // ---- write the tile back with 128-bit stores; the next load waits for these reads ----
+        // ---- write the tile back with 128-bit stores, each chunk's slot refilled with the next
+        // tile's chunk as soon as it is read: a chunk is read and reloaded by the same thread ----
         {
             float *dst = st + tile_base(t) + off_tid;
             const float *out = reinterpret_cast<const float *>(AH);
+            const bool next = t + dt < ntiles;
+            const float *src = st + (next ? tile_base(t + dt) : 0) + off_tid;
 #pragma unroll 8
             for (int i = 0; i < kTile / 4 / kThreads; ++i) {
                 const int e = 4 * (tid + kThreads * i);
-                *reinterpret_cast<float4 *>(dst + hi_off[i]) = *reinterpret_cast<const float4 *>(out + nat_swz(e));
+                const float4 v = *reinterpret_cast<const float4 *>(out + nat_swz(e));
+                *reinterpret_cast<float4 *>(dst + hi_off[i]) = v;
+                if (next) cp_async16(AH + 4 * nat_swz(e), src + hi_off[i]);
+            }
+            if (next) {
+                cp_async_commit();
+                loaded = true;
             }
         }
-        __syncthreads();
     }
     cp_async_wait_all();   // round 0's images prefetched for a tile that does not come
     __syncthreads();
