@@ -297,18 +297,28 @@ def _emulate_tc_pass(st, n, p):
     return out
 
 
-def test_tensor_core_tables_emulated():
-    """The tensor-core pass's layouts and tables, replayed in numpy, equal program order."""
-    n = 8
+@pytest.mark.parametrize('kind', ['random', 'off_low'])
+def test_tensor_core_tables_emulated(kind):
+    """The tensor-core pass's layouts and tables, replayed in numpy, equal program order.  'off_low':
+    ops off the two lowest-stride qubits, so last rounds leave local axes 0 and 1 alone and store
+    straight to global memory (direct last rounds)."""
+    n = 8 if kind == 'random' else 9
     rng = np.random.default_rng(21)
-    ops = random_ops(rng, n, 40)
+    ops = random_ops(rng, n, 40 if kind == 'random' else 90)
+    if kind == 'off_low':
+        ops = [op for op in ops if all(q < n - 2 for q in op.axes)]
     st0 = rng.normal(size=4 ** n)
     ref = st0.copy()
     for op in ops:
         ref = apply_op(ref, n, op)
     got = st0.copy()
+    direct = 0
     for p in P.plan_passes(ops, n, 7, 2):
+        _, layouts, _ = P.plan_tc_pass(p, n)
+        direct += P.direct_last_eligible([L.digits for L in layouts])
         got = _emulate_tc_pass(got, n, p)
+    if kind == 'off_low':
+        assert direct > 0
     np.testing.assert_allclose(got, ref, rtol=0, atol=1e-10 * np.abs(ref).max())
 
 
