@@ -167,6 +167,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     __shared__ __align__(8) uint64_t u_bar;
     __shared__ __align__(8) uint64_t stream_bar[kTeams];
     __shared__ uint32_t tmem_base_s;
+    __shared__ volatile int pipe_busy;      // team 0's MMAs are in flight (a scheduling hint for team 1)
     unsigned char *smem = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
     const int tid = threadIdx.x, warp = tid >> 5;
     const int team = tid / kTeamThreads, ttid = tid % kTeamThreads;
@@ -187,6 +188,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             tcg::mbar_init(smem_u32(&stream_bar[i]), 1);
         }
         tcg::mbar_init(ubar, 1);
+        pipe_busy = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
@@ -286,6 +288,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }                            // else no MMA and no commit: the team's wait below runs out
             }
             if (issue) {
+                // The tensor pipe interleaves the two teams' MMAs when they are issued together, so
+                // both finish together and the teams stay in step, each waiting for both teams' MMAs.
+                // Team 1 holds its MMAs back (at most 20 us) while team 0's are in flight, which lets
+                // one team's MMAs overlap the other team's epilogue instead.
+                if (team == 0) {
+                    pipe_busy = 1;
+                } else {
+                    const uint64_t t0 = tcg::global_ns();
+                    while (pipe_busy && tcg::global_ns() - t0 < 20000) __nanosleep(64);
+                }
                 // D[:, 0:64] = h Uh^T and D[:, 64:128] = h Ul^T (one N = 128 chain over [Uh ; Ul]),
                 // then D[:, 64:128] += l Uh^T (N = 64), for both M = 128 blocks
                 const uint64_t ub = smem_desc(uslot(r));
@@ -321,6 +333,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             mphase ^= 1;
             mma_pending = false;
+            if (team == 0 && leader) pipe_busy = 0;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const bool last = r + 1 == p.nrounds;
             if (leader && r >= p.nres && !last) stream_u(r + 1);   // this round's MMAs have read the slot
