@@ -296,3 +296,20 @@ def test_direct_last_round_tables_are_checked_on_host(lib):
     bad = copy()
     bad.rounds[last].kc[0] = 3                                           # not a power of two
     assert run(bad) == N.DM_ERR_PROGRAM
+
+
+def test_tile_copy_probe_rejects_bad_tiles_on_host(lib):
+    """dm_tile_copy_probe checks its arguments before any CUDA call (here there is no GPU)."""
+    dev = ctypes.c_void_p(1 << 20)
+
+    def run(axes, n=10, state=dev):
+        a = (ctypes.c_int32 * 7)(*axes)
+        return lib.dm_tile_copy_probe(state, n, a, None)
+
+    good = [9, 8, 6, 5, 3, 2, 0]
+    assert run(good, state=ctypes.c_void_p(None)) == N.DM_ERR_ARG
+    assert run(good, state=ctypes.c_void_p((1 << 20) + 4)) == N.DM_ERR_ARG      # unaligned state
+    assert run(good, n=6) == N.DM_ERR_ARG                                       # fewer than 7 qubits
+    assert run([8, 7, 6, 5, 3, 2, 0]) == N.DM_ERR_ARG                           # lowest qubit not resident
+    assert run([9, 8, 8, 5, 3, 2, 0]) == N.DM_ERR_ARG                           # not strictly decreasing
+    assert run([9, 8, 6, 5, 3, 2, -1]) == N.DM_ERR_ARG                          # qubit out of range
