@@ -514,18 +514,22 @@ def nat_linear(e):
 NAT_MAPS = {'xor': nat_swz, 'linear': nat_linear}
 
 
+_ROW_BIT_BYTES = tuple(_row_off(1 << i) for i in range(8))   # operand byte offset of row bit i
+_K_BIT_BYTES = tuple(_k_off(1 << i) for i in range(6))       # operand byte offset of K bit i
+
+
 class TcLayout:
     """Digit order (3 local axes) and row-bit order (8 tile bits) of one round's operand."""
+
+    __slots__ = ('digits', 'rowbits', 'kbits', '_byte')
 
     def __init__(self, digits, rowbits):
         self.digits = list(digits)
         self.rowbits = list(rowbits)
         self.kbits = [2 * a + b for a in self.digits for b in (0, 1)]
-        self._byte = {}
-        for i, tb in enumerate(self.rowbits):
-            self._byte[tb] = _row_off(1 << i)
-        for i, tb in enumerate(self.kbits):
-            self._byte[tb] = _k_off(1 << i)
+        byte = dict(zip(self.rowbits, _ROW_BIT_BYTES))
+        byte.update(zip(self.kbits, _K_BIT_BYTES))
+        self._byte = byte
 
     def byte_of_bit(self, tb):
         return self._byte[tb]
@@ -591,17 +595,30 @@ def _fill_rows(first, lanes, keep, nonround):
 
 
 def _best_next_cost(cand, next_axes):
-    """Cheapest epilogue from ``cand`` into a round on next_axes (lookahead of the greedy choice)."""
+    """Cheapest epilogue from ``cand`` into a round on next_axes (lookahead of the greedy choice).
+
+    It depends only on the candidate's row order and its set of axes (which
+    decides whether the next round's digit 0 can take 8-byte stores)."""
+    return _best_next_cost_cached(tuple(cand.rowbits), frozenset(cand.digits), tuple(sorted(next_axes)))
+
+
+@functools.lru_cache(maxsize=65536)
+def _best_next_cost_cached(rowbits, digit_set, next_axes):
     import itertools
     nonround = [tb for tb in range(2 * TC_AXES) if tb // 2 not in next_axes]
-    lanes = [tb for tb in cand.rowbits[:5] if tb in nonround]
-    keep = [tb for tb in cand.rowbits if tb in nonround]
+    lanes = [tb for tb in rowbits[:5] if tb in nonround]
+    keep = [tb for tb in rowbits if tb in nonround]
     rows = _fill_rows(lanes[:3], lanes, keep, nonround)
+    lane_bits = rowbits[:5]
     best = None
-    for digits in itertools.permutations(sorted(next_axes)):
+    for digits in itertools.permutations(next_axes):
         nxt = TcLayout(list(digits), rows)
-        vec = 8 if _vec_digit(cand, nxt.digits[0]) >= 0 else None
-        c = _transition_cost(cand, nxt.byte_of_bit, vec)
+        vec = 8 if nxt.digits[0] in digit_set else None
+        lane_offs = tuple(nxt.byte_of_bit(tb) for tb in lane_bits)
+        if vec:
+            c = 16 * _store_wavefronts(lane_offs, vec) + 4
+        else:
+            c = 64 * _store_wavefronts(lane_offs, 2) + 16
         best = c if best is None or c < best else best
     return best
 
@@ -688,9 +705,15 @@ def _choose_layouts_tma_cached(rounds_axes):
     layouts = []
     prev = None
 
+    fixed_cache = {}
+    into_last = {}
+
     def fixed_next(nxt_axes):
         """The layouts the next round may take when it is the last round (its rows are fixed)."""
-        return [TcLayout(list(d), r) for d, r in _tma_last_candidates(sorted(nxt_axes), None)]
+        key = tuple(sorted(nxt_axes))
+        if key not in fixed_cache:
+            fixed_cache[key] = [TcLayout(list(d), r) for d, r in _tma_last_candidates(list(key), None)]
+        return fixed_cache[key]
 
     for ri, axes in enumerate(rounds_axes):
         axes = sorted(axes)
@@ -733,8 +756,13 @@ def _choose_layouts_tma_cached(rounds_axes):
                 cost += _transition_cost(prev, cand.byte_of_bit, vec)
             if ri < nlast:
                 if ri + 1 == nlast:      # the last round's rows are fixed: its exact incoming cost
-                    cost += min(_transition_cost(cand, nxt.byte_of_bit, 8 if _vec_digit(cand, nxt.digits[0]) >= 0
-                                                 else None) for nxt in fixed_next(nxt_axes))
+                    # (it depends only on the candidate's lane bits and its set of axes)
+                    key = (tuple(cand.rowbits[:5]), frozenset(cand.digits), tuple(sorted(nxt_axes)))
+                    if key not in into_last:
+                        into_last[key] = min(
+                            _transition_cost(cand, nxt.byte_of_bit, 8 if _vec_digit(cand, nxt.digits[0]) >= 0
+                                             else None) for nxt in fixed_next(nxt_axes))
+                    cost += into_last[key]
                 else:
                     cost += _best_next_cost(cand, nxt_axes)
             if best is None or cost < best[0]:
